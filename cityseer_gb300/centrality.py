@@ -1,0 +1,441 @@
+"""Centrality drivers and result classes (the reference's rust/src/centrality.rs surface).
+
+Host logic mirrored here, kernels in libcsgpu.so:
+  validate_tolerance          rust/src/centrality.rs:34-48
+  prepare_source_sampling     rust/src/centrality.rs:1032-1104
+  sample_source_weight        rust/src/centrality.rs:1107-1139
+  scale_metric_results        rust/src/centrality.rs:875-893 (betweenness post-scale)
+  result getters              rust/src/centrality.rs:152-355, MetricResult.load_compact common.rs:37-53
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native, device
+from .common import WALKING_SPEED, pair_distances_betas_time
+from .graph import NodeVisit
+
+TIE_EPSILON = np.float32(1e-4)
+TOLERANCE_WARN_PCT = 2.0
+
+
+def validate_tolerance(tolerance: float | None) -> float:
+    """Percent -> decimal, clamped to at least TIE_EPSILON (rust/src/centrality.rs:34-48)."""
+    pct = np.float32(0.0 if tolerance is None else tolerance)
+    if pct < 0.0 or pct > 100.0:
+        raise ValueError(f"Tolerance must be between 0 and 100 (percent), got {tolerance}")
+    return float(max(np.float32(pct / np.float32(100.0)), TIE_EPSILON))
+
+
+# ---------------------------------------------------------------------------------------------
+# Results
+# ---------------------------------------------------------------------------------------------
+class _Result:
+    _rows: tuple[str, ...] = ()
+
+    def __init__(self, distances, node_keys_py, node_indices, data: np.ndarray):
+        self.distances = list(distances)
+        self.node_keys_py = list(node_keys_py)
+        self.node_indices = list(node_indices)
+        self._data = data  # [M][K][node_bound] f64
+        self._idx = np.asarray(self.node_indices, dtype=np.int64)
+        self.reachability_totals: list[int] = []
+        self.sampled_source_count = 0
+
+    def _load_compact(self, m: int) -> dict[int, np.ndarray]:
+        return {d: self._data[m, i][self._idx].copy() for i, d in enumerate(self.distances)}
+
+    def __getattr__(self, name):
+        rows = type(self)._rows
+        if name in rows:
+            return self._load_compact(rows.index(name))
+        raise AttributeError(name)
+
+
+class CentralityShortestResult(_Result):
+    _rows = ("node_density", "node_farness", "node_cycles", "node_harmonic", "node_beta", "node_betweenness",
+             "node_betweenness_beta")
+
+
+class CentralitySimplestResult(_Result):
+    _rows = ("node_density", "node_farness", "node_harmonic", "node_betweenness")
+
+
+class CentralitySegmentResult(_Result):
+    _rows = ("segment_density", "segment_harmonic", "segment_beta", "segment_betweenness")
+
+
+# ---------------------------------------------------------------------------------------------
+# Source sampling plan
+# ---------------------------------------------------------------------------------------------
+@dataclass
+class SourcePlan:
+    process: np.ndarray       # node indices handed to the kernel, in order
+    src_wt: np.ndarray        # f32 [node_bound]
+    eligible: np.ndarray      # u8 [node_bound]
+    is_source_indexed: bool
+    sample_probability: float | None
+    n_sources: int
+    n_live: int
+    sampled_count: int
+
+
+def prepare_source_sampling(ns, sample_probability, sampling_weights, random_seed, source_indices) -> SourcePlan:
+    nb = ns.node_bound()
+    nc = ns.node_count()
+    node_indices = np.asarray(ns.node_indices(), dtype=np.int64)
+    a = ns.arrays()
+    live = a["live"][:nb].astype(bool)
+    weight = a["weight"][:nb]
+    sw = None
+    if sampling_weights is not None:
+        w = np.asarray(sampling_weights, dtype=np.float32)
+        if len(w) not in (nb, nc):
+            raise ValueError(
+                f"sampling_weights length ({len(w)}) must match node_count ({nc}) or node_bound ({nb})")
+        bad = np.nonzero((w < 0.0) | (w > 1.0))[0]
+        if len(bad):
+            raise ValueError(f"sampling_weights[{bad[0]}] = {w[bad[0]]} is out of range [0.0, 1.0]")
+        if len(w) == nb:
+            sw = w
+        else:
+            sw = np.zeros(nb, np.float32)
+            sw[node_indices] = w
+    prob = None
+    if sample_probability is not None:
+        prob = np.float32(sample_probability)
+        if prob <= 0.0 or prob > 1.0:
+            raise ValueError("sample_probability must be in (0.0, 1.0]")
+    if source_indices is not None and sw is not None:
+        raise ValueError("source_indices and sampling_weights are mutually exclusive")
+    exists = a["node_exists"]
+    if source_indices is not None:
+        src = np.asarray(list(source_indices), dtype=np.int64)
+        for s in src:
+            if s < 0 or s >= nb or not exists[s]:
+                raise ValueError(f"node index {int(s)} does not exist in the graph")
+    n_live = int(live[node_indices].sum())
+    is_indexed = source_indices is not None
+    sources = src if is_indexed else node_indices
+    eligible = np.zeros(nb, np.uint8)
+    if is_indexed:
+        eligible[sources] = 1
+    else:
+        eligible[node_indices[live[node_indices]]] = 1
+    randoms = None
+    if prob is not None and not is_indexed:
+        # The reference draws from rand's StdRng (ChaCha12); this stream differs, so sampled runs
+        # agree with it in distribution, not source by source.
+        rng = np.random.default_rng(random_seed)
+        randoms = rng.random(nb, dtype=np.float32)
+    src_wt = np.zeros(nb, np.float32)
+    take = np.zeros(len(sources), bool)
+    count = 0
+    for j, s in enumerate(sources):
+        if not eligible[s]:
+            continue
+        wt = weight[s]
+        if is_indexed:
+            if prob is not None:
+                wt = np.float32(wt / prob)
+            count += 1
+        elif prob is not None:
+            p = prob
+            if sw is not None:
+                p = np.float32(p * sw[s])
+            if p <= 0.0:
+                continue
+            if randoms[s] >= p:
+                continue
+            count += 1
+            wt = np.float32(wt / p)
+        take[j] = True
+        src_wt[s] = wt
+    return SourcePlan(
+        process=sources[take].astype(np.int32),
+        src_wt=src_wt,
+        eligible=eligible,
+        is_source_indexed=is_indexed,
+        sample_probability=None if prob is None else float(prob),
+        n_sources=len(sources),
+        n_live=n_live,
+        sampled_count=count,
+    )
+
+
+# ---------------------------------------------------------------------------------------------
+# Device state cache per NetworkStructure
+# ---------------------------------------------------------------------------------------------
+def _primal_host(ns) -> device.PrimalHost:
+    c = ns._cache.get("primal_host")
+    if c is None:
+        c = device.PrimalHost(ns)
+        ns._cache["primal_host"] = c
+    return c
+
+
+def _primal_csr(ns) -> device.PrimalCSR:
+    """Device CSR of the graph, uploaded on first use and kept resident until the graph changes
+    (or drop_device_state() is called)."""
+    c = ns._cache.get("primal_csr")
+    if c is None:
+        c = device.PrimalCSR(_primal_host(ns))
+        ns._cache["primal_csr"] = c
+    return c
+
+
+def drop_device_state(ns, keep_workspace: bool = True) -> None:
+    """Forgets the device-resident CSR (and optionally the workspaces) of a graph."""
+    for k in list(ns._cache):
+        if k == "primal_csr" or k == "dual_csr" or (not keep_workspace and isinstance(k, tuple) and k[0] == "ws"):
+            del ns._cache[k]
+
+
+def _workspace(ns, csr, mode: int, k: int, speed: float, key_extra=()) -> device.Workspace:
+    key = ("ws", mode, k) + tuple(key_extra)
+    ws = ns._cache.get(key)
+    if ws is None:
+        # free other workspaces of this graph first: they can be large
+        for kk in [kk for kk in ns._cache if isinstance(kk, tuple) and kk and kk[0] == "ws"]:
+            del ns._cache[kk]
+        torch.cuda.empty_cache()
+        plan = device.plan_primal(csr, mode, k, speed)
+        ws = device.Workspace(plan, csr.n_bound, csr.device)
+        ns._cache[key] = ws
+    return ws
+
+
+def _groups(k: int):
+    """Threshold groups of at most CS_MAX_THRESHOLDS (each group is one launch)."""
+    step = _native.MAX_K
+    return [(i, min(k, i + step)) for i in range(0, k, step)]
+
+
+def _make_query(dists, betas, secs, speed, tol, closeness, betweenness, track_reach, proc_t, wt_t, el_t,
+                asu=180.0, fso=1.0) -> _native.Query:
+    q = _native.Query()
+    q.k = len(dists)
+    for i, (d, b, s) in enumerate(zip(dists, betas, secs)):
+        q.distances[i] = int(d)
+        q.betas[i] = float(b)
+        q.seconds[i] = int(s)
+    q.speed_m_s = float(speed)
+    q.tolerance = float(tol)
+    q.angular_scaling_unit = float(asu)
+    q.farness_scaling_offset = float(fso)
+    q.compute_closeness = 1 if closeness else 0
+    q.compute_betweenness = 1 if betweenness else 0
+    q.track_reach = 1 if track_reach else 0
+    q.n_sources = int(proc_t.numel())
+    q.sources = proc_t.data_ptr() if proc_t.numel() else None
+    q.src_wt = wt_t.data_ptr()
+    q.eligible = el_t.data_ptr()
+    return q
+
+
+def _stream_ptr():
+    return torch.cuda.current_stream().cuda_stream
+
+
+# ---------------------------------------------------------------------------------------------
+# centrality_shortest (rust/src/centrality.rs:1624-1874)
+# ---------------------------------------------------------------------------------------------
+def centrality_shortest(ns, distances=None, betas=None, minutes=None, compute_closeness=None,
+                        compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, tolerance=None,
+                        sample_probability=None, sampling_weights=None, random_seed=None, source_indices=None,
+                        pbar_disabled=None) -> CentralityShortestResult:
+    closeness = True if compute_closeness is None else bool(compute_closeness)
+    betweenness = True if compute_betweenness is None else bool(compute_betweenness)
+    if not closeness and not betweenness:
+        raise ValueError(
+            "Either or both closeness and betweenness flags is required, but both parameters are False.")
+    speed = WALKING_SPEED if speed_m_s is None else float(speed_m_s)
+    tol = validate_tolerance(tolerance)
+    dists, bets, secs = pair_distances_betas_time(speed, distances, betas, minutes, min_threshold_wt)
+    sp = prepare_source_sampling(ns, sample_probability, sampling_weights, random_seed, source_indices)
+    nb = ns.node_bound()
+    node_indices = ns.node_indices()
+    K = len(dists)
+    data = np.zeros((7, K, nb), np.float64)
+    reach_tot = np.zeros(K, np.int64)
+    track = sp.sample_probability is not None or sp.is_source_indexed
+    csr = _primal_csr(ns)
+    dev = csr.device
+    proc_t = torch.from_numpy(sp.process).to(dev)
+    wt_t = torch.from_numpy(sp.src_wt).to(dev)
+    el_t = torch.from_numpy(sp.eligible).to(dev)
+    g = csr.struct(speed)
+    lib = _native.load()
+    for lo, hi in _groups(K):
+        k = hi - lo
+        ws = _workspace(ns, csr, 0, k, speed)
+        out = torch.zeros((7, k, nb), dtype=torch.float64, device=dev)
+        reach = torch.zeros(k, dtype=torch.int32, device=dev)
+        q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, tol, closeness, betweenness, track,
+                        proc_t, wt_t, el_t)
+        o = _native.Outputs(out.data_ptr(), reach.data_ptr())
+        rc = lib.cs_centrality_shortest(C.byref(g), C.byref(q), C.byref(ws.plan), ws.ptr, ws.nbytes, o,
+                                        _stream_ptr())
+        if rc != _native.CS_OK:
+            ws.init(_stream_ptr())
+        _native.check(rc, "cs_centrality_shortest")
+        data[:, lo:hi] = out.cpu().numpy()
+        reach_tot[lo:hi] = reach.cpu().numpy().astype(np.int64)
+    if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
+        scale = sp.n_live / sp.n_sources
+        if scale != 1.0:
+            idx = np.asarray(node_indices, np.int64)
+            data[5][:, idx] *= scale
+            data[6][:, idx] *= scale
+    ns._progress = sp.n_sources
+    res = CentralityShortestResult(dists, ns.node_keys_py(), node_indices, data)
+    if track:
+        res.sampled_source_count = sp.sampled_count
+        res.reachability_totals = [int(x) for x in reach_tot]
+    return res
+
+
+# ---------------------------------------------------------------------------------------------
+# centrality_simplest (rust/src/centrality.rs:1880-2132)
+# ---------------------------------------------------------------------------------------------
+def centrality_simplest(ns, distances=None, betas=None, minutes=None, compute_closeness=None,
+                        compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, tolerance=None,
+                        angular_scaling_unit=None, farness_scaling_offset=None, sample_probability=None,
+                        sampling_weights=None, random_seed=None, source_indices=None,
+                        pbar_disabled=None) -> CentralitySimplestResult:
+    from . import dual
+
+    ns.validate_dual_for_angular("centrality_simplest")
+    closeness = True if compute_closeness is None else bool(compute_closeness)
+    betweenness = True if compute_betweenness is None else bool(compute_betweenness)
+    tol = validate_tolerance(tolerance)
+    if not closeness and not betweenness:
+        raise ValueError(
+            "Either or both closeness and betweenness flags is required, but both parameters are False.")
+    speed = WALKING_SPEED if speed_m_s is None else float(speed_m_s)
+    asu = 180.0 if angular_scaling_unit is None else float(angular_scaling_unit)
+    fso = 1.0 if farness_scaling_offset is None else float(farness_scaling_offset)
+    dists, bets, secs = pair_distances_betas_time(speed, distances, betas, minutes, min_threshold_wt)
+    sp = prepare_source_sampling(ns, sample_probability, sampling_weights, random_seed, source_indices)
+    return dual.run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, betweenness, sp)
+
+
+# ---------------------------------------------------------------------------------------------
+# segment_centrality (rust/src/centrality.rs:2134-2407)
+# ---------------------------------------------------------------------------------------------
+def segment_centrality(ns, distances=None, betas=None, minutes=None, compute_closeness=None,
+                       compute_betweenness=None, min_threshold_wt=None, speed_m_s=None,
+                       pbar_disabled=None) -> CentralitySegmentResult:
+    speed = WALKING_SPEED if speed_m_s is None else float(speed_m_s)
+    dists, bets, secs = pair_distances_betas_time(speed, distances, betas, minutes, min_threshold_wt)
+    closeness = True if compute_closeness is None else bool(compute_closeness)
+    betweenness = True if compute_betweenness is None else bool(compute_betweenness)
+    if not closeness and not betweenness:
+        raise ValueError(
+            "Either or both closeness and betweenness flags is required, but both parameters are False.")
+    nb = ns.node_bound()
+    node_indices = ns.node_indices()
+    a = ns.arrays()
+    idx = np.asarray(node_indices, np.int64)
+    process = idx[a["live"][idx] == 1].astype(np.int32)
+    K = len(dists)
+    data = np.zeros((4, K, nb), np.float64)
+    csr = _primal_csr(ns)
+    if csr.has_missing_reverse:
+        raise ValueError("Edge not found")
+    dev = csr.device
+    proc_t = torch.from_numpy(process).to(dev)
+    wt_t = torch.zeros(max(nb, 1), dtype=torch.float32, device=dev)
+    el_t = torch.zeros(max(nb, 1), dtype=torch.uint8, device=dev)
+    g = csr.struct(speed)
+    lib = _native.load()
+    for lo, hi in _groups(K):
+        k = hi - lo
+        ws = _workspace(ns, csr, 1, k, speed)
+        out = torch.zeros((4, k, nb), dtype=torch.float64, device=dev)
+        q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, float(TIE_EPSILON), closeness, betweenness,
+                        False, proc_t, wt_t, el_t)
+        o = _native.Outputs(out.data_ptr(), None)
+        rc = lib.cs_segment_centrality(C.byref(g), C.byref(q), C.byref(ws.plan), ws.ptr, ws.nbytes, o,
+                                       _stream_ptr())
+        if rc != _native.CS_OK:
+            ws.init(_stream_ptr())
+        _native.check(rc, "cs_segment_centrality")
+        data[:, lo:hi] = out.cpu().numpy()
+    ns._progress = len(node_indices)
+    return CentralitySegmentResult(dists, ns.node_keys_py(), node_indices, data)
+
+
+# ---------------------------------------------------------------------------------------------
+# Trees (isochrones): dijkstra_tree_shortest (rust/src/centrality.rs:1141-1200, 1500-1508)
+# ---------------------------------------------------------------------------------------------
+def tree_shortest_raw(ns, sources: list[int], max_seconds: int, speed: float, row_cap: int | None = None):
+    """Batched trees on the GPU: returns (counts, nodes, agg_seconds, preds) numpy arrays, rows in
+    settle order, row_cap wide."""
+    csr = _primal_csr(ns)
+    dev = csr.device
+    nb = csr.n_bound
+    nq = len(sources)
+    if row_cap is None:
+        row_cap = nb
+    lib = _native.load()
+    g = csr.struct(speed)
+    ws = _workspace(ns, csr, 2, 1, speed)
+    src_t = torch.tensor(sources, dtype=torch.int32, device=dev)
+    count = torch.zeros(nq, dtype=torch.int32, device=dev)
+    node = torch.empty((nq, row_cap), dtype=torch.int32, device=dev)
+    agg = torch.empty((nq, row_cap), dtype=torch.float32, device=dev)
+    pred = torch.empty((nq, row_cap), dtype=torch.int32, device=dev)
+    rc = lib.cs_tree_shortest(C.byref(g), nq, src_t.data_ptr(), int(max_seconds), C.c_float(speed),
+                              C.byref(ws.plan), ws.ptr, ws.nbytes, row_cap, count.data_ptr(), node.data_ptr(),
+                              agg.data_ptr(), pred.data_ptr(), _stream_ptr())
+    if rc != _native.CS_OK:
+        ws.init(_stream_ptr())
+    _native.check(rc, "cs_tree_shortest")
+    return count.cpu().numpy(), node.cpu().numpy(), agg.cpu().numpy(), pred.cpu().numpy()
+
+
+def tree_shortest(ns, sources: list[int], max_seconds: int, speed: float):
+    """Per source: (visited_nodes, list[NodeVisit]) exactly as dijkstra_tree_shortest returns."""
+    counts, nodes, agg, preds = tree_shortest_raw(ns, sources, max_seconds, speed)
+    nb = ns.node_bound()
+    sp32 = np.float32(speed)
+    out = []
+    for q in range(len(sources)):
+        n = int(counts[q])
+        tree = [NodeVisit() for _ in range(nb)]
+        visited = nodes[q, :n].tolist()
+        for i in range(n):
+            v = int(nodes[q, i])
+            t = tree[v]
+            t.visited = True
+            t.discovered = True
+            t.agg_seconds = float(agg[q, i])
+            t.short_dist = float(np.float32(agg[q, i]) * sp32)
+            p = int(preds[q, i])
+            t.pred = None if p < 0 else p
+        out.append((visited, tree))
+    return out
+
+
+def tree_simplest(ns, sources: list[int], max_seconds: int, speed: float):
+    from . import dual
+
+    return dual.tree_simplest(ns, sources, max_seconds, speed)
+
+
+def last_counters() -> tuple[int, int, int, int]:
+    """(sources, edges relaxed, nodes settled, kernel launches) of the last native call on this
+    thread."""
+    lib = _native.load()
+    a, b, c, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+    lib.cs_last_counters(C.byref(a), C.byref(b), C.byref(c), C.byref(d))
+    return a.value, b.value, c.value, d.value
+
+
+_ = math

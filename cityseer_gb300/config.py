@@ -1,0 +1,58 @@
+"""Constants and helpers of pysrc/cityseer/config.py (column keys, thresholds, progress)."""
+from __future__ import annotations
+
+import os
+import threading
+import time
+from collections.abc import Callable
+from queue import Queue
+
+MIN_THRESH_WT: float = 0.01831563888873418
+SPEED_M_S = 1.33333
+ATOL: float = 0.01
+RTOL: float = 0.0001
+
+
+def prep_gdf_key(key: str, dist: int, angular: bool = False, weighted: bool | None = None) -> str:
+    """Column label, pysrc/cityseer/config.py:21-32."""
+    key = key.replace(".0", "")
+    key = key.replace(".0_", "_")
+    key = f"cc_{key}_{dist}"
+    if angular is True:
+        key += "_ang"
+    if weighted is True:
+        key += "_wt"
+    elif weighted is False:
+        key += "_nw"
+    return key
+
+
+def check_quiet() -> bool:
+    if "GCP_PROJECT" in os.environ:
+        return True
+    return os.environ.get("CITYSEER_QUIET_MODE", "").lower() in ("true", "1")
+
+
+QUIET_MODE = check_quiet()
+
+
+def wrap_progress(total: int, rust_struct, partial_func: Callable, desc: str | None = None):
+    """Runs partial_func on a worker thread and polls rust_struct.progress(), re-raising worker
+    exceptions (pysrc/cityseer/config.py:96-130).  Progress is reported when the call returns."""
+    q: Queue = Queue()
+
+    def worker():
+        try:
+            q.put(partial_func())
+        except Exception as e:  # noqa: BLE001
+            q.put(e)
+
+    th = threading.Thread(target=worker)
+    th.start()
+    while th.is_alive():
+        time.sleep(0.05)
+    th.join()
+    res = q.get()
+    if isinstance(res, Exception):
+        raise res
+    return res

@@ -1,0 +1,71 @@
+// cs_common.cuh -- shared device helpers for the cityseer_gb300 kernels (sm_103a).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/cityseer_gb300.h"
+
+namespace cs {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int INF_BITS = 0x7f800000;
+constexpr uint32_t NEAR_BIT = 1u << 30;
+constexpr uint32_t FAR_BIT = 1u << 31;
+// TIE_EPSILON and the f32 constants (1 + eps), (1 - eps) exactly as rust/src/centrality.rs:28,
+// 671-674 evaluates them (f32 arithmetic).
+constexpr float TIE_EPSILON = 1e-4f;
+constexpr float ANGULAR_TIE_BREAK = 1e-6f;
+constexpr int MAXK = CS_MAX_THRESHOLDS;
+constexpr int MAXDEG = CS_MAX_DEGREE;
+
+// Shared workspace header (first 256 bytes of every workspace).
+struct WsHeader {
+    unsigned long long work_next;     // persistent work counter
+    unsigned long long work_next2;    // second-phase counter (retries)
+    unsigned int n_failed;            // sources that overflowed their slot's capacity
+    unsigned int err;                 // first device-side error code (CS_ERR_*)
+    unsigned int err_where;           // diagnostic: where the error was raised
+    unsigned int pad0;
+    unsigned long long sources_done;
+    unsigned long long edges_relaxed;
+    unsigned long long nodes_settled;
+    unsigned long long pad[24];
+};
+static_assert(sizeof(WsHeader) <= 256, "header too large");
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+
+__device__ __forceinline__ int warp_max_i(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_min_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void raise_err(WsHeader *h, unsigned code, unsigned where) {
+    if (atomicCAS(&h->err, 0u, code) == 0u) h->err_where = where;
+}
+
+}  // namespace cs

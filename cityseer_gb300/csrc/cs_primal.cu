@@ -1,0 +1,1161 @@
+// cs_primal.cu -- GB300 kernels for shortest-path node centrality, segment centrality and
+// shortest-path trees (isochrones) on the primal graph.
+//
+// Reference behaviour (cityseer-api v4.24.0):
+//   centrality_shortest        rust/src/centrality.rs:1624-1874
+//   dijkstra_brandes_shortest  rust/src/centrality.rs:1344-1494
+//   circuit_ranks_from_traversal rust/src/centrality.rs:470-526
+//   brandes_backprop_with_beta rust/src/centrality.rs:823-873
+//   segment_centrality         rust/src/centrality.rs:2134-2407
+//   dijkstra_tree_segment      rust/src/centrality.rs:1524-1611
+//   dijkstra_tree_shortest_inner rust/src/centrality.rs:1141-1200
+//
+// Design (one warp per source, persistent warps pulling sources from a work counter):
+//  1. Bounded label-correcting search ("near-far" banded Bellman-Ford) from the source over
+//     reversed edges.  Every relaxation is fl(d[u] + w) with w >= 0, so the least fixpoint is
+//     unique and bit-identical to the reference's heap Dijkstra whatever the relaxation order.
+//  2. Warp LSD radix sort of the reached set by distance: the reference's settle order.
+//  3. Replay, per reached node and in parallel, of the exact sequence of candidate offers the
+//     heap Dijkstra would make to it (offering neighbours in settle order), through the
+//     reference's Phase-1 tie rules (and Phase 2 when tolerance > 1e-4).  This reproduces its
+//     multi-predecessor lists; sigma follows in settle order.
+//  4. Closeness into target rows and circuit ranks; one backward Brandes sweep carrying all K
+//     thresholds (a state beyond threshold k contributes nothing to lane k, so one sweep equals
+//     the reference's K sweeps).
+// Per-slot scratch: dense dist/aux arrays over node_bound (reset touched entries only) plus
+// compact per-reached-node arrays of capacity `cap`; sources that overflow `cap` are retried
+// with cap = node_bound inside the same API call.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <algorithm>
+#include <cmath>
+
+#include "cs_common.cuh"
+
+namespace cs {
+
+struct SlotPtrs {
+    float *dist;
+    uint32_t *aux;
+    int32_t *rl, *qa, *qb, *qf;
+    uint32_t *kb;
+    int32_t *vb;
+    int32_t *ord;
+    float *sd;
+    double *sig;
+    uint8_t *np;
+    int32_t *pr;
+    double *dl;
+    float *fa, *fb;
+    int32_t *eb;
+};
+
+__host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+__host__ __device__ inline size_t compact_bytes(size_t cap, int P, int L) {
+    size_t b = 0;
+    b += 7 * al256(cap * 4);      // rl qa qb qf kb vb ord
+    b += al256(cap * 4);          // sd
+    b += al256(cap * 8);          // sig
+    b += al256(cap);              // np
+    b += al256(cap * 4 * (size_t)P);  // pr
+    b += al256(cap * 8 * (size_t)L);  // dl
+    b += 3 * al256(cap * 4);      // fa fb eb
+    return b;
+}
+
+__host__ __device__ inline SlotPtrs slot_ptrs(char *dense, size_t dense_stride, char *compact, size_t cap, int P,
+                                              int L, int slot, int n_bound) {
+    SlotPtrs s;
+    char *d = dense + dense_stride * (size_t)slot;
+    s.dist = (float *)d;
+    s.aux = (uint32_t *)(d + al256((size_t)n_bound * 4));
+    char *c = compact + compact_bytes(cap, P, L) * (size_t)slot;
+    size_t o = 0;
+    s.rl = (int32_t *)(c + o); o += al256(cap * 4);
+    s.qa = (int32_t *)(c + o); o += al256(cap * 4);
+    s.qb = (int32_t *)(c + o); o += al256(cap * 4);
+    s.qf = (int32_t *)(c + o); o += al256(cap * 4);
+    s.kb = (uint32_t *)(c + o); o += al256(cap * 4);
+    s.vb = (int32_t *)(c + o); o += al256(cap * 4);
+    s.ord = (int32_t *)(c + o); o += al256(cap * 4);
+    s.sd = (float *)(c + o); o += al256(cap * 4);
+    s.sig = (double *)(c + o); o += al256(cap * 8);
+    s.np = (uint8_t *)(c + o); o += al256(cap);
+    s.pr = (int32_t *)(c + o); o += al256(cap * 4 * (size_t)P);
+    s.dl = (double *)(c + o); o += al256(cap * 8 * (size_t)L);
+    s.fa = (float *)(c + o); o += al256(cap * 4);
+    s.fb = (float *)(c + o); o += al256(cap * 4);
+    s.eb = (int32_t *)(c + o); o += al256(cap * 4);
+    return s;
+}
+
+enum Mode { MODE_SHORTEST = 0, MODE_SEGMENT = 1, MODE_TREE = 2 };
+
+struct PrimalParams {
+    cs_primal_graph g;
+    int32_t k;
+    float dk[MAXK];
+    float beta[MAXK];
+    float maxsec;
+    float speed;
+    float tol;
+    float delta;
+    int32_t closeness, betweenness, track_reach;
+    const int32_t *src_list;
+    int64_t n_src;
+    const float *src_wt;
+    const uint8_t *eligible;
+    double *out;
+    uint32_t *reach;
+    WsHeader *hdr;
+    int32_t *failed;  // [n_slots] source node indices that overflowed
+    char *dense;
+    size_t dense_stride;
+    char *compact;
+    int32_t cap, P, L;
+    int32_t n_slots;
+    int32_t rerun;
+    const int32_t *remap;  // rerun: indices into src_list of the sources to redo
+    int32_t mode;
+    int32_t row_cap;
+    int32_t *t_count, *t_node, *t_pred;
+    float *t_agg;
+};
+
+// ------------------------------------------------------------------------------------------
+// 1. Banded label-correcting search.  Returns R (reached count incl. source) or -1 on overflow.
+// ------------------------------------------------------------------------------------------
+__device__ int warp_search(const PrimalParams &p, const SlotPtrs &s, int src, long long &relaxed) {
+    const int lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    const int cap = p.cap;
+    const int32_t *__restrict__ in_ptr = p.g.in_ptr_dev;
+    const int32_t *__restrict__ in_nb = p.g.in_nb_dev;
+    const float *__restrict__ in_w = p.g.in_w_dev;
+    float *dist = s.dist;
+    uint32_t *aux = s.aux;
+    if (lane == 0) {
+        dist[src] = 0.0f;
+        s.rl[0] = src;
+        s.qa[0] = src;
+        aux[src] = NEAR_BIT;
+    }
+    __syncwarp();
+    int R = 1, nnear = 1, nfar = 0;
+    int32_t *cur = s.qa, *nxt = s.qb;
+    float T = p.delta;
+    bool overflow = false;
+    while (true) {
+        while (nnear > 0) {
+            int nnext = 0;
+            for (int base = 0; base < nnear; base += 32) {
+                const int i = base + lane;
+                const bool act = i < nnear;
+                const int u = act ? cur[i] : 0;
+                if (act) atomicAnd(&aux[u], ~NEAR_BIT);
+                __syncwarp();
+                const float du = act ? __ldcg(&dist[u]) : 0.0f;
+                const int beg = act ? __ldg(&in_ptr[u]) : 0;
+                const int end = act ? __ldg(&in_ptr[u + 1]) : 0;
+                relaxed += end - beg;
+                const int maxdeg = warp_max_i(end - beg);
+                for (int j = 0; j < maxdeg; j++) {
+                    const int e = beg + j;
+                    int v = 0;
+                    bool first = false;
+                    int route = 0;
+                    if (e < end) {
+                        v = __ldg(&in_nb[e]);
+                        if (v != u) {
+                            const float c = fadd(du, __ldg(&in_w[e]));
+                            if (c <= p.maxsec) {
+                                const int old = atomicMin((int *)&dist[v], __float_as_int(c));
+                                if (__float_as_int(c) < old) {
+                                    first = (old == INF_BITS);
+                                    if (c < T) {
+                                        const uint32_t o = atomicOr(&aux[v], NEAR_BIT);
+                                        route = (o & NEAR_BIT) ? 0 : 1;
+                                    } else {
+                                        const uint32_t o = atomicOr(&aux[v], FAR_BIT);
+                                        route = (o & FAR_BIT) ? 0 : 2;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    const unsigned mf = __ballot_sync(FULL, first);
+                    const unsigned mn = __ballot_sync(FULL, route == 1);
+                    const unsigned mr = __ballot_sync(FULL, route == 2);
+                    if (first) {
+                        const int q = R + __popc(mf & lt);
+                        if (q < cap) s.rl[q] = v;
+                    }
+                    if (route == 1) {
+                        const int q = nnext + __popc(mn & lt);
+                        if (q < cap) nxt[q] = v;
+                    }
+                    if (route == 2) {
+                        const int q = nfar + __popc(mr & lt);
+                        if (q < cap) s.qf[q] = v;
+                    }
+                    R += __popc(mf);
+                    nnext += __popc(mn);
+                    nfar += __popc(mr);
+                }
+            }
+            __syncwarp();
+            if (R > cap || nnext > cap || nfar > cap) { overflow = true; break; }
+            int32_t *t = cur; cur = nxt; nxt = t;
+            nnear = nnext;
+        }
+        if (overflow) break;
+        if (nfar == 0) break;
+        // Next band starts at the smallest pending distance.
+        float mn = __int_as_float(INF_BITS);
+        for (int i = lane; i < nfar; i += 32) {
+            const float d = __ldcg(&dist[s.qf[i]]);
+            if (d >= T) mn = fminf(mn, d);
+        }
+        mn = warp_min_f(mn);
+        const float Told = T;
+        // next band: [mn, mn + delta); strictly above mn even when delta is below mn's ulp
+        T = (mn == __int_as_float(INF_BITS)) ? Told
+                                             : fmaxf(fadd(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        int nn = 0, nf2 = 0;
+        for (int base = 0; base < nfar; base += 32) {
+            const int i = base + lane;
+            const bool act = i < nfar;
+            const int v = act ? s.qf[i] : 0;
+            const float d = act ? __ldcg(&dist[v]) : 0.0f;
+            const bool drop = act && d < Told;
+            bool tonear = act && !drop && d < T;
+            const bool keep = act && !drop && !tonear;
+            if (drop || tonear) atomicAnd(&aux[v], ~FAR_BIT);
+            if (tonear) {
+                const uint32_t o = atomicOr(&aux[v], NEAR_BIT);
+                tonear = !(o & NEAR_BIT);
+            }
+            const unsigned mt = __ballot_sync(FULL, tonear);
+            const unsigned mk = __ballot_sync(FULL, keep);
+            __syncwarp();
+            if (tonear) cur[nn + __popc(mt & lt)] = v;
+            if (keep) s.qf[nf2 + __popc(mk & lt)] = v;
+            nn += __popc(mt);
+            nf2 += __popc(mk);
+            __syncwarp();
+        }
+        nnear = nn;
+        nfar = nf2;
+    }
+    __syncwarp();
+    if (overflow) {
+        // Leave the slot dirty: the caller resets the whole slot before reuse.
+        return -1;
+    }
+    return R;
+}
+
+// ------------------------------------------------------------------------------------------
+// 2. Warp LSD radix sort of (dist bits, node) pairs.  Stable; input rl/dist, output ord/sd.
+// ------------------------------------------------------------------------------------------
+__device__ void warp_sort(const SlotPtrs &s, int R, uint32_t *hist) {
+    const int lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    // pass inputs/outputs: 0: (dist[rl], rl) -> (kb, vb); 1: (kb,vb)->(sd,ord); 2: ->(kb,vb); 3: ->(sd,ord)
+    for (int pass = 0; pass < 4; pass++) {
+        const int shift = pass * 8;
+        for (int b = lane; b < 256; b += 32) hist[b] = 0;
+        __syncwarp();
+        const uint32_t *kin = (pass == 0) ? nullptr : ((pass & 1) ? s.kb : (const uint32_t *)s.sd);
+        const int32_t *vin = (pass == 0) ? s.rl : ((pass & 1) ? s.vb : s.ord);
+        uint32_t *kout = (pass & 1) ? (uint32_t *)s.sd : s.kb;
+        int32_t *vout = (pass & 1) ? s.ord : s.vb;
+        for (int i = lane; i < R; i += 32) {
+            const uint32_t key = (pass == 0) ? (uint32_t)__float_as_int(__ldcg(&s.dist[vin[i]])) : kin[i];
+            atomicAdd(&hist[(key >> shift) & 255u], 1u);
+        }
+        __syncwarp();
+        // exclusive scan of 256 bins: each lane owns 8 consecutive bins
+        uint32_t loc[8];
+        uint32_t tot = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) { loc[q] = hist[lane * 8 + q]; tot += loc[q]; }
+        uint32_t inc = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += t;
+        }
+        uint32_t run = inc - tot;
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 8; q++) { hist[lane * 8 + q] = run; run += loc[q]; }
+        __syncwarp();
+        for (int base = 0; base < R; base += 32) {
+            const int i = base + lane;
+            const bool act = i < R;
+            uint32_t key = 0;
+            int32_t val = 0;
+            if (act) {
+                val = vin[i];
+                key = (pass == 0) ? (uint32_t)__float_as_int(__ldcg(&s.dist[val])) : kin[i];
+            }
+            const uint32_t dg = act ? ((key >> shift) & 255u) : (256u + (uint32_t)lane);
+            const unsigned peers = __match_any_sync(FULL, dg);
+            const int rank = __popc(peers & lt);
+            const int leader = __ffs(peers) - 1;
+            uint32_t off = 0;
+            if (act) off = hist[dg];
+            __syncwarp();
+            if (act) {
+                kout[off + rank] = key;
+                vout[off + rank] = val;
+            }
+            if (act && lane == leader) hist[dg] = off + __popc(peers);
+            __syncwarp();
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// 3. Offer replay for the node at sorted position i.
+// ------------------------------------------------------------------------------------------
+struct Offer {
+    int pos;
+    float c;
+    int e;
+};
+
+// Gathers the candidate offers to v (out-edges v->u with u settled before v), stably sorted by
+// the offering node's settle position.  Returns the count.
+__device__ __forceinline__ int gather_offers(const PrimalParams &p, const SlotPtrs &s, int v, int i, Offer *off) {
+    const int beg = __ldg(&p.g.out_ptr_dev[v]);
+    const int end = __ldg(&p.g.out_ptr_dev[v + 1]);
+    int n = 0;
+    for (int e = beg; e < end && n < MAXDEG; e++) {
+        const int u = __ldg(&p.g.out_to_dev[e]);
+        if (u == v) continue;
+        const uint32_t a = s.aux[u];
+        if (a == 0u) continue;
+        const int pu = (int)a - 1;
+        if (pu >= i) continue;
+        const float c = fadd(s.sd[pu], __ldg(&p.g.out_w_dev[e]));
+        // insertion keeping stability on equal positions (parallel edges keep list order)
+        int q = n;
+        while (q > 0 && off[q - 1].pos > pu) { off[q] = off[q - 1]; q--; }
+        off[q].pos = pu;
+        off[q].c = c;
+        off[q].e = e;
+        n++;
+    }
+    return n;
+}
+
+// Phase-1 (+ Phase-2) predecessor replay, rust/src/centrality.rs:1413-1437 and 1444-1483.
+// Returns the number of predecessors written to preds[], or -1 if the replayed distance does not
+// reproduce the searched one (internal inconsistency).
+__device__ __forceinline__ int replay_brandes(const PrimalParams &p, const Offer *off, int n, float dv, int *preds) {
+    const float one_plus = 1.0f + TIE_EPSILON;
+    const float one_minus = 1.0f - TIE_EPSILON;
+    float cur = __int_as_float(INF_BITS);
+    int np = 0;
+    for (int q = 0; q < n; q++) {
+        const float c = off[q].c;
+        if (c > p.maxsec) continue;
+        const bool improved = c < cur;
+        const bool tied = c <= fmul(cur, one_plus);
+        if (improved) {
+            if (c < fmul(cur, one_minus)) np = 0;
+            preds[np++] = off[q].pos;
+            cur = c;
+        } else if (tied) {
+            bool has = false;
+            for (int r = 0; r < np; r++) has |= (preds[r] == off[q].pos);
+            if (!has) preds[np++] = off[q].pos;
+        }
+    }
+    if (__float_as_int(cur) != __float_as_int(dv)) return -1;
+    if (p.tol > TIE_EPSILON) {
+        const float lim = fmul(dv, 1.0f + p.tol);
+        np = 0;
+        for (int q = 0; q < n; q++) {
+            if (off[q].c <= lim) {
+                bool has = false;
+                for (int r = 0; r < np; r++) has |= (preds[r] == off[q].pos);
+                if (!has) preds[np++] = off[q].pos;
+            }
+        }
+    }
+    return np;
+}
+
+// Strict-< single predecessor (dijkstra_tree_* / dijkstra_tree_segment): the first offer, in
+// settle order, that reaches the final distance.  Returns the offer index or -1.
+__device__ __forceinline__ int replay_first_min(const PrimalParams &p, const Offer *off, int n, float dv) {
+    float cur = __int_as_float(INF_BITS);
+    int best = -1;
+    for (int q = 0; q < n; q++) {
+        const float c = off[q].c;
+        if (c > p.maxsec) continue;
+        if (c < cur) { cur = c; best = q; }
+    }
+    if (__float_as_int(cur) != __float_as_int(dv)) return -2;
+    return best;
+}
+
+__device__ __forceinline__ float route_cost(float secs, float speed) { return fmul(secs, speed); }
+
+// ------------------------------------------------------------------------------------------
+// 4a. Shortest-path centrality for one source (after search and sort).
+// ------------------------------------------------------------------------------------------
+__device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R) {
+    const int lane = lane_id();
+    const int K = p.k;
+    const int P = p.P;
+    const int N = p.g.n_bound;
+    const float wt = __ldg(&p.src_wt[src]);
+    const float cycles_wt = wt / __ldg(&p.g.node_w_dev[src]);
+    // --- predecessor replay + circuit-rank edge counts
+    int ecount[MAXK];
+    int ncount[MAXK];
+#pragma unroll
+    for (int k = 0; k < MAXK; k++) { ecount[k] = 0; ncount[k] = 0; }
+    bool bad = false;
+    for (int i = lane; i < R; i += 32) {
+        const int v = s.ord[i];
+        const float dv = s.sd[i];
+        const float cv = route_cost(dv, p.speed);
+#pragma unroll
+        for (int k = 0; k < MAXK; k++) if (k < K && cv <= p.dk[k]) ncount[k]++;
+        if (p.closeness) {
+            const int beg = __ldg(&p.g.out_ptr_dev[v]);
+            const int end = __ldg(&p.g.out_ptr_dev[v + 1]);
+            for (int e = beg; e < end; e++) {
+                if (!__ldg(&p.g.out_cnt_dev[e])) continue;
+                const int u = __ldg(&p.g.out_to_dev[e]);
+                if (u == v) continue;
+                const uint32_t a = s.aux[u];
+                if (a == 0u) continue;
+                const float cu = route_cost(s.sd[a - 1], p.speed);
+                const float ec = fmaxf(cv, cu);
+#pragma unroll
+                for (int k = 0; k < MAXK; k++) if (k < K && ec <= p.dk[k]) ecount[k]++;
+            }
+        }
+        if (!p.betweenness) continue;
+        if (i == 0) { s.np[0] = 0; continue; }
+        Offer off[MAXDEG];
+        const int n = gather_offers(p, s, v, i, off);
+        int preds[MAXDEG];
+        const int np = replay_brandes(p, off, n, dv, preds);
+        if (np < 0 || np > P) { bad = true; s.np[i] = 0; continue; }
+        s.np[i] = (uint8_t)np;
+        for (int r = 0; r < np; r++) s.pr[(size_t)i * P + r] = preds[r];
+    }
+    if (__any_sync(FULL, bad)) {
+        if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 1);
+    }
+    __syncwarp();
+    // --- closeness (rust/src/centrality.rs:1733-1780)
+    if (p.closeness) {
+        float rank[MAXK];
+#pragma unroll
+        for (int k = 0; k < MAXK; k++) {
+            const long long nc = warp_sum_ll(ncount[k]);
+            const long long ec = warp_sum_ll(ecount[k]);
+            const long long r = ec - nc + 1;
+            rank[k] = (nc == 0) ? 0.0f : (float)(r > 0 ? r : 0);
+            if (p.track_reach && k < K && lane == 0 && nc > 1) atomicAdd(&p.reach[k], (unsigned)(nc - 1));
+        }
+        for (int i = 1 + lane; i < R; i += 32) {
+            const int t = s.ord[i];
+            const float c = route_cost(s.sd[i], p.speed);
+#pragma unroll
+            for (int k = 0; k < MAXK; k++) {
+                if (k < K && c <= p.dk[k]) {
+                    double *row = p.out + (size_t)k * N;
+                    const size_t MS = (size_t)K * N;
+                    atomicAdd(row + 0 * MS + t, (double)wt);
+                    atomicAdd(row + 1 * MS + t, (double)fmul(c, wt));
+                    atomicAdd(row + 2 * MS + t, (double)fmul(rank[k], cycles_wt));
+                    atomicAdd(row + 3 * MS + t, (double)fmul(__fdiv_rn(1.0f, c), wt));
+                    atomicAdd(row + 4 * MS + t, (double)fmul(expf(fmul(-p.beta[k], c)), wt));
+                }
+            }
+        }
+    }
+    if (!p.betweenness) return;
+    // --- sigma in settle order (chunked, ready when all in-chunk preds are done)
+    for (int base = 0; base < R; base += 32) {
+        const int i = base + lane;
+        const bool act = i < R;
+        int np = act ? s.np[i] : 0;
+        unsigned pm = 0;
+        int pl[MAXDEG];
+        for (int r = 0; r < np; r++) {
+            pl[r] = s.pr[(size_t)i * P + r];
+            if (pl[r] >= base) pm |= 1u << (pl[r] - base);
+        }
+        unsigned done = __ballot_sync(FULL, !act);
+        bool mine = !act;
+        int guard = 0;
+        while (done != FULL) {
+            const bool ready = !mine && ((pm & ~done) == 0u);
+            if (ready) {
+                double sg;
+                if (i == 0) sg = 1.0;
+                else {
+                    sg = 0.0;
+                    for (int r = 0; r < np; r++) sg += s.sig[pl[r]];
+                }
+                s.sig[i] = sg;
+                mine = true;
+            }
+            __syncwarp();
+            done |= __ballot_sync(FULL, ready);
+            if (++guard > 64) break;
+        }
+        if (done != FULL) {
+            if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 2);
+            return;
+        }
+    }
+    // --- backward Brandes sweep with 2K lanes (rust/src/centrality.rs:823-873, 1782-1835)
+    const int L = p.L;  // = 2K
+    for (int i = lane; i < R; i += 32) {
+        double *dl = s.dl + (size_t)i * L;
+        for (int q = 0; q < 2 * K; q++) dl[q] = 0.0;
+    }
+    __syncwarp();
+    const double wtd = (double)wt;
+    const int nchunks = (R + 31) / 32;
+    for (int ch = nchunks - 1; ch >= 0; ch--) {
+        const int base = ch * 32;
+        const int i = base + lane;
+        const bool act = i < R;
+        const int np = act ? s.np[i] : 0;
+        unsigned pm = 0;
+        int pl[MAXDEG];
+        for (int r = 0; r < np; r++) {
+            pl[r] = s.pr[(size_t)i * P + r];
+            if (pl[r] >= base) pm |= 1u << (pl[r] - base);
+        }
+        bool mine = !act;
+        unsigned done = __ballot_sync(FULL, mine);
+        int guard = 0;
+        while (done != FULL) {
+            const unsigned blocked = __reduce_or_sync(FULL, mine ? 0u : pm);
+            const bool ready = !mine && !((blocked >> lane) & 1u);
+            if (ready) {
+                const int v = s.ord[i];
+                const float cost = route_cost(s.sd[i], p.speed);
+                const double sw = s.sig[i];
+                const double pair = __ldg(&p.eligible[v]) ? 0.5 : 1.0;
+                double *dl = s.dl + (size_t)i * L;
+                for (int k = 0; k < K; k++) {
+                    if (!(cost <= p.dk[k])) continue;
+                    if (sw == 0.0) continue;
+                    const double seed = (i == 0) ? 0.0 : pair;
+                    const double seedb = (i == 0) ? 0.0 : pair * exp(-(double)p.beta[k] * (double)cost);
+                    const double dep = seed + __ldcg(&dl[k]);
+                    const double depb = seedb + __ldcg(&dl[K + k]);
+                    if (dep == 0.0 && depb == 0.0) continue;
+                    for (int r = 0; r < np; r++) {
+                        const double sv = s.sig[pl[r]];
+                        if (sv == 0.0) continue;
+                        const double f = sv / sw;
+                        double *pd = s.dl + (size_t)pl[r] * L;
+                        atomicAdd(&pd[k], f * dep);
+                        atomicAdd(&pd[K + k], f * depb);
+                    }
+                    if (v == src) continue;
+                    const double credit = dep - seed;
+                    const double creditb = depb - seedb;
+                    if (credit > 0.0) atomicAdd(p.out + ((size_t)5 * K + k) * N + v, credit * wtd);
+                    if (creditb > 0.0) atomicAdd(p.out + ((size_t)6 * K + k) * N + v, creditb * wtd);
+                }
+                mine = true;
+            }
+            __syncwarp();
+            done |= __ballot_sync(FULL, ready);
+            if (++guard > 64) break;
+        }
+        if (done != FULL) {
+            if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 3);
+            return;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// 4b. Segment centrality for one source.
+// ------------------------------------------------------------------------------------------
+__device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R) {
+    const int lane = lane_id();
+    const int K = p.k;
+    const int N = p.g.n_bound;
+    bool bad = false;
+    // single predecessor (strict <) with its last segment length; pred position in pr[i*P]
+    for (int i = lane; i < R; i += 32) {
+        if (i == 0) { s.pr[0] = -1; s.fa[0] = 0.0f; continue; }
+        const int v = s.ord[i];
+        Offer off[MAXDEG];
+        const int n = gather_offers(p, s, v, i, off);
+        const int q = replay_first_min(p, off, n, s.sd[i]);
+        if (q < 0) { bad = true; s.pr[(size_t)i * p.P] = -1; continue; }
+        s.pr[(size_t)i * p.P] = off[q].pos;
+        s.fa[i] = __ldg(&p.g.out_seglen_dev[off[q].e]);  // last segment length
+    }
+    if (__any_sync(FULL, bad)) {
+        if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 4);
+        return;
+    }
+    __syncwarp();
+    // origin segment length: inherited along the tree (settle order, chunked)
+    for (int base = 0; base < R; base += 32) {
+        const int i = base + lane;
+        const bool act = i < R;
+        const int pp = (act && i > 0) ? s.pr[(size_t)i * p.P] : -1;
+        const unsigned pm = (pp >= base) ? (1u << (pp - base)) : 0u;
+        bool mine = !act;
+        if (act && i == 0) { s.fb[0] = 0.0f; mine = true; }
+        unsigned done = __ballot_sync(FULL, mine);
+        int guard = 0;
+        while (done != FULL) {
+            const bool ready = !mine && ((pm & ~done) == 0u);
+            if (ready) {
+                s.fb[i] = (pp == 0) ? s.fa[i] : s.fb[pp];
+                mine = true;
+            }
+            __syncwarp();
+            done |= __ballot_sync(FULL, ready);
+            if (++guard > 64) break;
+        }
+        if (done != FULL) {
+            if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 5);
+            return;
+        }
+    }
+    // closeness integrals over visited edges (rust/src/centrality.rs:2201-2317), into the source
+    if (p.closeness) {
+        double acc[3 * MAXK];
+#pragma unroll
+        for (int q = 0; q < 3 * MAXK; q++) acc[q] = 0.0;
+        for (int i = lane; i < R; i += 32) {
+            const int u = s.ord[i];
+            const float au = route_cost(s.sd[i], p.speed);
+            const int beg = __ldg(&p.g.in_ptr_dev[u]);
+            const int end = __ldg(&p.g.in_ptr_dev[u + 1]);
+            for (int e = beg; e < end; e++) {
+                const int nb = __ldg(&p.g.in_nb_dev[e]);
+                float bm;
+                if (nb == u) {
+                    bm = au;
+                } else {
+                    const uint32_t a = s.aux[nb];
+                    if (a != 0u && (int)(a - 1) < i) continue;  // neighbour settled earlier
+                    bm = (a != 0u) ? route_cost(s.sd[a - 1], p.speed) : __int_as_float(INF_BITS);
+                }
+                const bool n_nearer = au <= bm;
+                const float A = n_nearer ? au : bm, Ai = A;
+                const float B = n_nearer ? bm : au, Bi = B;
+                const float elen = __ldg(&p.g.in_seglen_dev[e]);
+                const float imp = __ldg(&p.g.in_segimp_dev[e]);
+                const float C = __fdiv_rn(fadd(fadd(elen, A), B), 2.0f), D = C;
+                const float Ci = fadd(Ai, fmul(__fadd_rn(C, -A), imp)), Di = Ci;
+                for (int k = K - 1; k >= 0; k--) {
+                    const float df = p.dk[k];
+                    const float beta = p.beta[k], nbeta = -beta;
+                    const float inb = (beta != 0.0f) ? __fdiv_rn(1.0f, nbeta) : 0.0f;
+                    if (A < df) {
+                        float cc = C, cci = Ci;
+                        if (cc > df) { cc = df; cci = fadd(Ai, fmul(__fadd_rn(df, -A), imp)); }
+                        acc[k] += (double)__fadd_rn(cc, -A);
+                        const float sh = (Ai < 1.0f) ? logf(cci) : logf(fmaxf(__fdiv_rn(cci, Ai), 1.1920929e-07f));
+                        acc[MAXK + k] += (double)sh;
+                        const float bet = (beta == 0.0f) ? __fadd_rn(cci, -Ai)
+                                                         : fmul(__fadd_rn(expf(fmul(nbeta, cci)), -expf(fmul(nbeta, Ai))), inb);
+                        acc[2 * MAXK + k] += (double)bet;
+                    }
+                    if (B == D) continue;
+                    if (B <= df) {
+                        float cd = D, cdi = Di;
+                        if (cd > df) { cd = df; cdi = fadd(Bi, fmul(__fadd_rn(df, -B), imp)); }
+                        acc[k] += (double)__fadd_rn(cd, -B);
+                        const float sh = (Bi < 1.0f) ? logf(cdi) : logf(fmaxf(__fdiv_rn(cdi, Bi), 1.1920929e-07f));
+                        acc[MAXK + k] += (double)sh;
+                        const float bet = (beta == 0.0f) ? __fadd_rn(cdi, -Bi)
+                                                         : fmul(__fadd_rn(expf(fmul(nbeta, cdi)), -expf(fmul(nbeta, Bi))), inb);
+                        acc[2 * MAXK + k] += (double)bet;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < MAXK; k++) {
+            if (k >= K) break;
+            const double a0 = warp_sum_d(acc[k]);
+            const double a1 = warp_sum_d(acc[MAXK + k]);
+            const double a2 = warp_sum_d(acc[2 * MAXK + k]);
+            if (lane == 0) {
+                atomicAdd(p.out + ((size_t)0 * K + k) * N + src, a0);
+                atomicAdd(p.out + ((size_t)1 * K + k) * N + src, a1);
+                atomicAdd(p.out + ((size_t)2 * K + k) * N + src, a2);
+            }
+        }
+    }
+    if (!p.betweenness) return;
+    // betweenness: subtree sums of per-target auc (rust/src/centrality.rs:2319-2401)
+    double *acc = s.dl;  // [R][K]
+    for (int i = lane; i < R; i += 32)
+        for (int k = 0; k < K; k++) acc[(size_t)i * K + k] = 0.0;
+    __syncwarp();
+    const int nchunks = (R + 31) / 32;
+    for (int ch = nchunks - 1; ch >= 0; ch--) {
+        const int base = ch * 32;
+        const int i = base + lane;
+        const bool act = i < R;
+        const int pp = (act && i > 0) ? s.pr[(size_t)i * p.P] : -1;
+        const unsigned pm = (pp >= base) ? (1u << (pp - base)) : 0u;
+        bool mine = !act;
+        unsigned done = __ballot_sync(FULL, mine);
+        int guard = 0;
+        while (done != FULL) {
+            const unsigned blocked = __reduce_or_sync(FULL, mine ? 0u : pm);
+            const bool ready = !mine && !((blocked >> lane) & 1u);
+            if (ready) {
+                const int v = s.ord[i];
+                const float sdist = route_cost(s.sd[i], p.speed);
+                const float o_len = s.fb[i], l_len = s.fa[i];
+                const float min_span = __fadd_rn(__fadd_rn(sdist, -o_len), -l_len);
+                const float o_1 = min_span, o_2 = fadd(min_span, o_len);
+                const float l_1 = min_span, l_2 = fadd(min_span, l_len);
+                const bool own = (i > 0) && (v > src);
+                for (int k = 0; k < K; k++) {
+                    const double below = __ldcg(&acc[(size_t)i * K + k]);
+                    double total = below;
+                    if (own) {
+                        const float df = p.dk[k];
+                        const float beta = p.beta[k];
+                        if (min_span <= df) {
+                            const float o2s = fminf(o_2, df), l2s = fminf(l_2, df);
+                            float auc;
+                            if (beta == 0.0f) auc = fadd(__fadd_rn(o2s, -o_1), __fadd_rn(l2s, -l_1));
+                            else {
+                                const float nb = -beta, inb = __fdiv_rn(1.0f, nb);
+                                auc = fadd(fmul(__fadd_rn(expf(fmul(nb, o2s)), -expf(fmul(nb, o_1))), inb),
+                                           fmul(__fadd_rn(expf(fmul(nb, l2s)), -expf(fmul(nb, l_1))), inb));
+                            }
+                            if (isfinite(auc) && auc >= 0.0f) total += (double)auc;
+                        }
+                    }
+                    if (i > 0 && v != src && below > 0.0) atomicAdd(p.out + ((size_t)3 * K + k) * N + v, below);
+                    if (pp >= 0 && total != 0.0) atomicAdd(&acc[(size_t)pp * K + k], total);
+                }
+                mine = true;
+            }
+            __syncwarp();
+            done |= __ballot_sync(FULL, ready);
+            if (++guard > 64) break;
+        }
+        if (done != FULL) {
+            if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 6);
+            return;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// 4c. Shortest-path tree rows (isochrone query).
+// ------------------------------------------------------------------------------------------
+__device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, int R) {
+    const int lane = lane_id();
+    if (R > p.row_cap) {
+        if (lane == 0) p.t_count[qidx] = -1;
+        return;
+    }
+    bool bad = false;
+    for (int i = lane; i < R; i += 32) {
+        const int v = s.ord[i];
+        int pred = -1;
+        if (i > 0) {
+            Offer off[MAXDEG];
+            const int n = gather_offers(p, s, v, i, off);
+            const int q = replay_first_min(p, off, n, s.sd[i]);
+            if (q < 0) bad = true;
+            else pred = s.ord[off[q].pos];
+        }
+        const size_t o = (size_t)qidx * p.row_cap + i;
+        p.t_node[o] = v;
+        p.t_agg[o] = s.sd[i];
+        p.t_pred[o] = pred;
+    }
+    if (__any_sync(FULL, bad) && lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 7);
+    if (lane == 0) p.t_count[qidx] = R;
+}
+
+// ------------------------------------------------------------------------------------------
+// Persistent kernel: each warp owns one scratch slot and pulls sources until the list is empty.
+// ------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) primal_kernel(const PrimalParams p) {
+    __shared__ uint32_t hist_all[8][256];
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
+    if (slot >= p.n_slots) return;
+    uint32_t *hist = hist_all[wib];
+    const SlotPtrs s = slot_ptrs(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.P, p.L, slot, p.g.n_bound);
+    long long relaxed = 0, settled = 0, done_src = 0;
+    while (true) {
+        unsigned long long idx = 0;
+        if (lane == 0) idx = atomicAdd(p.rerun ? &p.hdr->work_next2 : &p.hdr->work_next, 1ull);
+        idx = __shfl_sync(FULL, idx, 0);
+        if (idx >= (unsigned long long)p.n_src) break;
+        if (__ldcg(&p.hdr->err) != 0u) break;
+        const int li = p.remap ? p.remap[idx] : (int)idx;
+        const int src = p.src_list[li];
+        const int R = warp_search(p, s, src, relaxed);
+        if (R < 0) {
+            if (lane == 0) {
+                const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
+                if (f < (unsigned)p.n_slots) p.failed[f] = li;
+            }
+            break;  // slot is dirty; the host resets it
+        }
+        warp_sort(s, R, hist);
+        __syncwarp();
+        for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+        __syncwarp();
+        if (p.mode == MODE_SHORTEST) shortest_accumulate(p, s, src, R);
+        else if (p.mode == MODE_SEGMENT) segment_accumulate(p, s, src, R);
+        else tree_rows(p, s, li, R);
+        __syncwarp();
+        for (int i = lane; i < R; i += 32) {
+            const int v = s.ord[i];
+            s.dist[v] = __int_as_float(INF_BITS);
+            s.aux[v] = 0u;
+        }
+        __syncwarp();
+        settled += R;
+        done_src += 1;
+    }
+    const long long rsum = warp_sum_ll(relaxed);
+    if (lane == 0) {
+        atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
+        atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
+        atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
+    }
+}
+
+__global__ void fill_dense_kernel(char *dense, size_t dense_stride, int n_bound, const int32_t *slots, int n_list,
+                                  int all_slots) {
+    // Resets dist (=inf) and aux (=0) of the listed slots (or of slots [0, all_slots)).
+    const int n_sl = slots ? n_list : all_slots;
+    const size_t per = (size_t)n_bound;
+    const size_t total = per * (size_t)n_sl;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int si = (int)(t / per);
+        const size_t j = t % per;
+        const int slot = slots ? slots[si] : si;
+        char *d = dense + dense_stride * (size_t)slot;
+        ((float *)d)[j] = __int_as_float(INF_BITS);
+        ((uint32_t *)(d + al256(per * 4)))[j] = 0u;
+    }
+}
+
+}  // namespace cs
+
+
+// ==========================================================================================
+// Host side (C-ABI).
+// ==========================================================================================
+namespace cs_host {
+thread_local std::string g_last_error;
+thread_local long long g_counters[4] = {0, 0, 0, 0};
+}
+
+extern "C" void cs_set_error_internal(const char *msg) { cs_host::g_last_error = msg ? msg : ""; }
+
+namespace {
+using cs_host::g_counters;
+
+cs_status fail(cs_status code, const std::string &msg) {
+    cs_host::g_last_error = msg;
+    return code;
+}
+cs_status cuda_fail(cudaError_t e, const char *what) {
+    return fail(CS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int sm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return n;
+}
+
+struct Layout {
+    size_t hdr_off, failed_off, dense_off, compact_off, compact_total, total;
+    size_t dense_stride;
+};
+
+Layout layout(int n_bound, int n_slots, int cap, int P, int L) {
+    Layout l;
+    l.hdr_off = 0;
+    l.failed_off = 256;
+    l.dense_off = cs::al256(l.failed_off + sizeof(int32_t) * (size_t)n_slots);
+    l.dense_stride = cs::al256((size_t)n_bound * 4) * 2;
+    l.compact_off = l.dense_off + l.dense_stride * (size_t)n_slots;
+    l.compact_total = cs::compact_bytes((size_t)cap, P, L) * (size_t)n_slots;
+    // the in-call retry runs at cap = n_bound on the same compact region: keep room for one slot
+    l.compact_total = std::max(l.compact_total, cs::compact_bytes((size_t)n_bound, P, L));
+    l.total = l.compact_off + l.compact_total;
+    return l;
+}
+
+int lanes_for(int mode, int k) { return mode == cs::MODE_SHORTEST ? 2 * k : (mode == cs::MODE_SEGMENT ? k : 1); }
+
+cs_status validate_primal(const cs_primal_graph *g) {
+    if (!g) return fail(CS_ERR_ARG, "graph is NULL");
+    if (g->n_bound <= 0) return fail(CS_ERR_ARG, "NetworkStructure contains no nodes.");
+    if (g->max_out_degree > CS_MAX_DEGREE)
+        return fail(CS_ERR_ARG, "node out-degree " + std::to_string(g->max_out_degree) + " exceeds CS_MAX_DEGREE");
+    return CS_OK;
+}
+
+cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, cudaStream_t stream) {
+    const int tpb = 256;
+    const int wpb = tpb / 32;
+    const int blocks = (n_slots + wpb - 1) / wpb;
+    p.n_slots = n_slots;
+    cs::primal_kernel<<<blocks, tpb, 0, stream>>>(p);
+    g_counters[3]++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "primal_kernel launch");
+    return CS_OK;
+}
+
+cs_status reset_dense(char *dense, size_t stride, int n_bound, int n_slots, cudaStream_t stream) {
+    const size_t total = (size_t)n_bound * (size_t)n_slots;
+    int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)sm_count() * 16);
+    if (blocks < 1) blocks = 1;
+    cs::fill_dense_kernel<<<blocks, 256, 0, stream>>>(dense, stride, n_bound, nullptr, 0, n_slots);
+    g_counters[3]++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "fill_dense_kernel launch");
+    return CS_OK;
+}
+
+cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan, void *ws, size_t ws_bytes,
+                     cs_outputs out, void *stream_v, int mode, int32_t row_cap, int32_t *t_count, int32_t *t_node,
+                     float *t_agg, int32_t *t_pred, const int32_t *tree_src, int32_t n_tree, uint32_t tree_maxsec,
+                     float tree_speed) {
+    cs_status st = validate_primal(g);
+    if (st != CS_OK) return st;
+    if (!plan || !ws) return fail(CS_ERR_ARG, "plan/workspace is NULL");
+    const int P = std::max(1, g->max_out_degree);
+    const int K = (mode == cs::MODE_TREE) ? 1 : q->k;
+    if (K < 1 || K > CS_MAX_THRESHOLDS) return fail(CS_ERR_ARG, "threshold count out of range");
+    const int L = lanes_for(mode, K);
+    if (plan->lanes < L) return fail(CS_ERR_ARG, "plan was made for fewer thresholds");
+    Layout lay = layout(g->n_bound, plan->n_slots, plan->cap, P, plan->lanes);
+    if (ws_bytes < lay.total) return fail(CS_ERR_ARG, "workspace too small for this plan");
+    cudaStream_t stream = (cudaStream_t)stream_v;
+    char *base = (char *)ws;
+    cs::PrimalParams p;
+    memset(&p, 0, sizeof(p));
+    p.g = *g;
+    p.k = K;
+    uint32_t maxs = 0;
+    if (mode == cs::MODE_TREE) {
+        maxs = tree_maxsec;
+        p.speed = tree_speed;
+        p.tol = cs::TIE_EPSILON;
+        p.src_list = tree_src;
+        p.n_src = n_tree;
+    } else {
+        if (!q) return fail(CS_ERR_ARG, "query is NULL");
+        for (int i = 0; i < K; i++) {
+            p.dk[i] = (float)q->distances[i];
+            p.beta[i] = q->betas[i];
+            maxs = std::max(maxs, q->seconds[i]);
+        }
+        p.speed = q->speed_m_s;
+        p.tol = q->tolerance;
+        p.closeness = q->compute_closeness;
+        p.betweenness = q->compute_betweenness;
+        p.track_reach = q->track_reach;
+        p.src_list = q->sources_dev;
+        p.n_src = q->n_sources;
+        p.src_wt = q->src_wt_dev;
+        p.eligible = q->eligible_dev;
+        if (p.track_reach && !out.reach_dev) return fail(CS_ERR_ARG, "reach_dev required when track_reach");
+        if (!out.out_dev) return fail(CS_ERR_ARG, "out_dev is NULL");
+    }
+    if (!(p.speed > 0.0f) || !std::isfinite(p.speed)) return fail(CS_ERR_ARG, "speed_m_s must be finite and positive");
+    p.maxsec = (float)maxs;
+    p.delta = plan->delta_seconds > 0.0f ? plan->delta_seconds : std::max(1.0f, p.maxsec / 48.0f);
+    p.out = out.out_dev;
+    p.reach = out.reach_dev;
+    p.hdr = (cs::WsHeader *)(base + lay.hdr_off);
+    p.failed = (int32_t *)(base + lay.failed_off);
+    p.dense = base + lay.dense_off;
+    p.dense_stride = lay.dense_stride;
+    p.compact = base + lay.compact_off;
+    p.cap = plan->cap;
+    p.P = P;
+    p.L = plan->lanes;
+    p.mode = mode;
+    p.row_cap = row_cap;
+    p.t_count = t_count;
+    p.t_node = t_node;
+    p.t_agg = t_agg;
+    p.t_pred = t_pred;
+    g_counters[0] = g_counters[1] = g_counters[2] = g_counters[3] = 0;
+    if (p.n_src <= 0) return CS_OK;
+    cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "workspace header reset");
+    st = launch_primal(p, plan, plan->n_slots, stream);
+    if (st != CS_OK) return st;
+    cs::WsHeader h;
+    e = cudaMemcpyAsync(&h, p.hdr, sizeof(h), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_fail(e, "centrality kernel");
+    if (h.err != 0u)
+        return fail((cs_status)h.err, "device-side check failed (code " + std::to_string(h.err) + " at " +
+                                          std::to_string(h.err_where) + ")");
+    long long done = (long long)h.sources_done, rel = (long long)h.edges_relaxed, set = (long long)h.nodes_settled;
+    if (h.n_failed > 0u) {
+        // Sources whose reach overflowed `cap`: reset every slot's dense scratch, then redo them at
+        // cap = n_bound on as many slots as the compact region holds.
+        const int nf = (int)std::min<unsigned>(h.n_failed, (unsigned)plan->n_slots);
+        st = reset_dense(p.dense, p.dense_stride, g->n_bound, plan->n_slots, stream);
+        if (st != CS_OK) return st;
+        const size_t per = cs::compact_bytes((size_t)g->n_bound, P, plan->lanes);
+        int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
+        slots2 = std::max(1, std::min(slots2, nf));
+        cs::PrimalParams p2 = p;
+        p2.cap = g->n_bound;
+        p2.rerun = 1;
+        p2.remap = p.failed;
+        p2.n_src = nf;
+        st = launch_primal(p2, plan, slots2, stream);
+        if (st != CS_OK) return st;
+        e = cudaMemcpyAsync(&h, p.hdr, sizeof(h), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_fail(e, "centrality retry kernel");
+        if (h.err != 0u)
+            return fail((cs_status)h.err, "device-side check failed in retry (code " + std::to_string(h.err) + ")");
+        done = (long long)h.sources_done;
+        rel = (long long)h.edges_relaxed;
+        set = (long long)h.nodes_settled;
+    }
+    g_counters[0] = done;
+    g_counters[1] = rel;
+    g_counters[2] = set;
+    return CS_OK;
+}
+
+cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t budget, cs_plan *plan) {
+    if (!plan) return fail(CS_ERR_ARG, "plan is NULL");
+    int sms = sm_count();
+    if (sms <= 0) return fail(CS_ERR_CUDA, "no CUDA device");
+    int bpsm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, cs::primal_kernel, 256, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
+    if (bpsm < 1) bpsm = 1;
+    int slots = sms * bpsm * 8;
+    if (max_slots > 0) slots = std::min(slots, max_slots);
+    if (cap <= 0) cap = std::min(n_bound, 16384);
+    cap = std::max(32, std::min(cap, n_bound));
+    auto total_for = [&](int ns) { return layout(n_bound, ns, cap, P, L).total; };
+    if (budget > 0) {
+        while (slots > 8 && (int64_t)total_for(slots) > budget) slots = (slots * 7) / 8;
+    }
+    slots = std::max(1, slots);
+    plan->n_slots = slots;
+    plan->cap = cap;
+    plan->threads_per_block = 256;
+    plan->blocks = (slots + 7) / 8;
+    if (plan->delta_seconds != plan->delta_seconds) plan->delta_seconds = 0.0f;
+    plan->lanes = L;
+    plan->workspace_bytes = total_for(slots);
+    return CS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t cs_last_error(char *buf, size_t len) {
+    const std::string &m = cs_host::g_last_error;
+    const size_t n = m.size();
+    if (buf && len) {
+        const size_t c = std::min(n, len - 1);
+        memcpy(buf, m.data(), c);
+        buf[c] = 0;
+    }
+    return n;
+}
+
+int32_t cs_device_sm_count(void) { return sm_count(); }
+
+cs_status cs_last_counters(int64_t *sources, int64_t *edges_relaxed, int64_t *nodes_settled, int64_t *launches) {
+    if (sources) *sources = g_counters[0];
+    if (edges_relaxed) *edges_relaxed = g_counters[1];
+    if (nodes_settled) *nodes_settled = g_counters[2];
+    if (launches) *launches = g_counters[3];
+    return CS_OK;
+}
+
+cs_status cs_plan_primal(const cs_primal_graph *g, int32_t mode, int32_t k, int32_t cap, int32_t max_slots,
+                         int64_t mem_budget_bytes, cs_plan *plan) {
+    cs_status st = validate_primal(g);
+    if (st != CS_OK) return st;
+    if (mode < 0 || mode > 2) return fail(CS_ERR_ARG, "unknown mode");
+    if (mode != cs::MODE_TREE && (k < 1 || k > CS_MAX_THRESHOLDS)) return fail(CS_ERR_ARG, "threshold count out of range");
+    const int P = std::max(1, g->max_out_degree);
+    const float keep_delta = plan ? plan->delta_seconds : 0.0f;
+    if (plan) plan->delta_seconds = keep_delta;
+    return plan_common(g->n_bound, P, lanes_for(mode, mode == cs::MODE_TREE ? 1 : k), cap, max_slots,
+                       mem_budget_bytes, plan);
+}
+
+cs_status cs_workspace_init(const cs_plan *plan, int32_t n_bound, void *workspace_dev, size_t workspace_bytes,
+                            void *stream) {
+    if (!plan || !workspace_dev) return fail(CS_ERR_ARG, "plan/workspace is NULL");
+    if (workspace_bytes < plan->workspace_bytes) return fail(CS_ERR_ARG, "workspace smaller than plan");
+    Layout lay = layout(n_bound, plan->n_slots, 32, 1, 1);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(workspace_dev, 0, 256, s);
+    if (e != cudaSuccess) return cuda_fail(e, "workspace init");
+    return reset_dense((char *)workspace_dev + lay.dense_off, lay.dense_stride, n_bound, plan->n_slots, s);
+}
+
+cs_status cs_centrality_shortest(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan,
+                                 void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream) {
+    return run_primal(g, q, plan, workspace_dev, workspace_bytes, out, stream, cs::MODE_SHORTEST, 0, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, 0, 0, 0.0f);
+}
+
+cs_status cs_segment_centrality(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan,
+                                void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream) {
+    return run_primal(g, q, plan, workspace_dev, workspace_bytes, out, stream, cs::MODE_SEGMENT, 0, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, 0, 0, 0.0f);
+}
+
+cs_status cs_tree_shortest(const cs_primal_graph *g, int32_t n_queries, const int32_t *src_dev, uint32_t max_seconds,
+                           float speed_m_s, const cs_plan *plan, void *workspace_dev, size_t workspace_bytes,
+                           int32_t row_cap, int32_t *count_dev, int32_t *node_dev, float *agg_seconds_dev,
+                           int32_t *pred_dev, void *stream) {
+    if (!count_dev || !node_dev || !agg_seconds_dev || !pred_dev || row_cap <= 0)
+        return fail(CS_ERR_ARG, "tree outputs missing");
+    cs_outputs o{nullptr, nullptr};
+    return run_primal(g, nullptr, plan, workspace_dev, workspace_bytes, o, stream, cs::MODE_TREE, row_cap, count_dev,
+                      node_dev, agg_seconds_dev, pred_dev, src_dev, n_queries, max_seconds, speed_m_s);
+}
+
+}  // extern "C"

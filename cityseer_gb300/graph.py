@@ -1,0 +1,618 @@
+"""Host-side NetworkStructure: the reference's graph store, restated over numpy columns.
+
+Mirrors ``rustalgos.graph.NetworkStructure`` (rust/src/graph.rs:381-1341): the same builder
+methods, getters, validation messages and index semantics (StableGraph indices with gaps after
+removals; petgraph reverse-insertion edge order).  The centrality methods hand the graph to the
+GPU through ``cityseer_gb300.device`` (a device-resident CSR) and libcsgpu.so.
+"""
+from __future__ import annotations
+
+import math
+import re
+from collections.abc import Sequence
+from typing import Any
+
+import numpy as np
+
+_LS_RE = re.compile(r"^\s*LINESTRING\s*(Z|M|ZM)?\s*\((.*)\)\s*$", re.IGNORECASE | re.DOTALL)
+
+
+def parse_linestring_wkt(wkt: str) -> list[tuple[float, ...]]:
+    m = _LS_RE.match(wkt)
+    if not m:
+        raise ValueError(f"Failed to parse WKT: {wkt[:200]}")
+    coords = []
+    for part in m.group(2).split(","):
+        vals = part.split()
+        if len(vals) < 2:
+            raise ValueError(f"Failed to parse WKT coordinate '{part}'")
+        coords.append(tuple(float(v) for v in vals))
+    return coords
+
+
+def _bearing(a, b) -> float:
+    """measure_bearing (rust/src/graph.rs:326-332): degrees, 0 for coincident points."""
+    if a[0] == b[0] and a[1] == b[1]:
+        return 0.0
+    return math.degrees(math.atan2(b[1] - a[1], b[0] - a[0]))
+
+
+def _coords_angle(a, b, c) -> float:
+    """measure_coords_angle (rust/src/graph.rs:336-346)."""
+    if (a[0] == b[0] and a[1] == b[1]) or (b[0] == c[0] and b[1] == c[1]):
+        return 0.0
+    a1 = _bearing(b, a)
+    a2 = _bearing(c, b)
+    diff = a2 - a1
+    r = math.fmod(diff + 180.0, 360.0)
+    if r < 0.0:
+        r += 360.0
+    return abs(r - 180.0)
+
+
+def cumulative_angle(coords: Sequence[Sequence[float]]) -> float:
+    """measure_cumulative_angle (rust/src/graph.rs:367-379), f64."""
+    if len(coords) < 3:
+        return 0.0
+    s = 0.0
+    for i in range(1, len(coords) - 1):
+        s += _coords_angle(coords[i - 1], coords[i], coords[i + 1])
+    return s
+
+
+def linestring_length(coords: Sequence[Sequence[float]]) -> float:
+    """Euclidean length of the 2D polyline in f64 (geo Euclidean.length, rust/src/graph.rs:774)."""
+    s = 0.0
+    for i in range(len(coords) - 1):
+        s += float(np.hypot(coords[i + 1][0] - coords[i][0], coords[i + 1][1] - coords[i][1]))
+    return s
+
+
+class _Col:
+    """Growable numpy column with amortised appends."""
+
+    __slots__ = ("a", "n")
+
+    def __init__(self, dtype, data=None):
+        if data is None:
+            self.a = np.zeros(16, dtype=dtype)
+            self.n = 0
+        else:
+            self.a = np.ascontiguousarray(data, dtype=dtype)
+            self.n = len(self.a)
+
+    def append(self, v):
+        if self.n == len(self.a):
+            b = np.zeros(max(16, 2 * len(self.a)), dtype=self.a.dtype)
+            b[: self.n] = self.a[: self.n]
+            self.a = b
+        self.a[self.n] = v
+        self.n += 1
+
+    def view(self) -> np.ndarray:
+        return self.a[: self.n]
+
+
+class NodeVisit:
+    """Per-node traversal state (rust/src/graph.rs:251-288)."""
+
+    __slots__ = ("visited", "discovered", "pred", "short_dist", "simpl_dist", "origin_seg", "last_seg", "agg_seconds")
+
+    def __init__(self):
+        self.visited = False
+        self.discovered = False
+        self.pred = None
+        self.short_dist = math.inf
+        self.simpl_dist = math.inf
+        self.origin_seg = None
+        self.last_seg = None
+        self.agg_seconds = math.inf
+
+    def __repr__(self):
+        return (
+            f"NodeVisit(visited={self.visited}, pred={self.pred}, short_dist={self.short_dist}, "
+            f"simpl_dist={self.simpl_dist}, agg_seconds={self.agg_seconds})"
+        )
+
+
+class EdgeVisit:
+    """Per-edge traversal state (rust/src/graph.rs:290-315)."""
+
+    __slots__ = ("visited", "start_nd_idx", "end_nd_idx", "edge_idx")
+
+    def __init__(self):
+        self.visited = False
+        self.start_nd_idx = None
+        self.end_nd_idx = None
+        self.edge_idx = None
+
+
+class NetworkStructure:
+    """Graph store with the reference's builder API; centralities run on the GPU."""
+
+    def __init__(self):
+        self._keys: list[Any] | None = []
+        self._x = _Col(np.float64)
+        self._y = _Col(np.float64)
+        self._z = _Col(np.float64)
+        self._has_z = _Col(np.uint8)
+        self._live = _Col(np.uint8)
+        self._weight = _Col(np.float32)
+        self._exists = _Col(np.uint8)
+        self._transport = _Col(np.uint8)
+        self._e_src = _Col(np.int32)
+        self._e_dst = _Col(np.int32)
+        self._e_idx = _Col(np.int64)
+        self._e_len = _Col(np.float32)
+        self._e_ang = _Col(np.float32)
+        self._e_imp = _Col(np.float32)
+        self._e_sec = _Col(np.float32)
+        self._e_inb = _Col(np.float32)
+        self._e_outb = _Col(np.float32)
+        self._e_exists = _Col(np.uint8)
+        self._e_transport = _Col(np.uint8)
+        self._e_shared: list[str | None] = []
+        self._e_keys: list[tuple[Any, Any] | None] | None = []
+        self._is_dual = False
+        self._progress = 0
+        self._version = 0
+        self._cache: dict[str, Any] = {}
+
+    # ------------------------------------------------------------------ bulk construction
+    @classmethod
+    def from_arrays(
+        cls,
+        x: np.ndarray,
+        y: np.ndarray,
+        edge_src: np.ndarray,
+        edge_dst: np.ndarray,
+        edge_length: np.ndarray,
+        *,
+        edge_idx: np.ndarray | None = None,
+        edge_angle_sum: np.ndarray | None = None,
+        edge_imp: np.ndarray | None = None,
+        edge_shared_key: Sequence[str | None] | np.ndarray | None = None,
+        live: np.ndarray | None = None,
+        weight: np.ndarray | None = None,
+        z: np.ndarray | None = None,
+        is_dual: bool = False,
+        node_keys: Sequence[Any] | None = None,
+    ) -> "NetworkStructure":
+        """Builds a structure from columns: nodes 0..n-1, directed edges in insertion order.
+
+        Equivalent to calling add_street_node / add_street_edge in order, with the edge lengths
+        and angle sums already computed (f32) as add_street_edge would from the geometry.
+        """
+        ns = cls()
+        n = len(x)
+        m = len(edge_src)
+        ns._keys = None if node_keys is None else list(node_keys)
+        ns._x = _Col(np.float64, x)
+        ns._y = _Col(np.float64, y)
+        if z is None:
+            ns._z = _Col(np.float64, np.full(n, np.nan))
+            ns._has_z = _Col(np.uint8, np.zeros(n))
+        else:
+            z = np.asarray(z, dtype=np.float64)
+            ns._z = _Col(np.float64, z)
+            ns._has_z = _Col(np.uint8, ~np.isnan(z))
+        ns._live = _Col(np.uint8, np.ones(n) if live is None else live)
+        w = np.ones(n, np.float32) if weight is None else np.asarray(weight, np.float32)
+        if not np.all(np.isfinite(w)) or np.any(w < 0):
+            raise ValueError("Invalid street node payload: weight must be finite and non-negative (>= 0.0).")
+        ns._weight = _Col(np.float32, w)
+        ns._exists = _Col(np.uint8, np.ones(n))
+        ns._transport = _Col(np.uint8, np.zeros(n))
+        es = np.asarray(edge_src, np.int64)
+        ed = np.asarray(edge_dst, np.int64)
+        if m and (es.min() < 0 or ed.min() < 0 or es.max() >= n or ed.max() >= n):
+            raise ValueError("edge endpoint does not exist in the graph.")
+        ns._e_src = _Col(np.int32, es)
+        ns._e_dst = _Col(np.int32, ed)
+        ns._e_idx = _Col(np.int64, np.zeros(m) if edge_idx is None else edge_idx)
+        ns._e_len = _Col(np.float32, edge_length)
+        ns._e_ang = _Col(np.float32, np.zeros(m) if edge_angle_sum is None else edge_angle_sum)
+        imp = np.ones(m, np.float32) if edge_imp is None else np.asarray(edge_imp, np.float32)
+        if np.any(~np.isfinite(imp)) or np.any(imp <= 0):
+            raise ValueError("Invalid edge payload : imp_factor must be finite and positive (> 0.0).")
+        ns._e_imp = _Col(np.float32, imp)
+        ns._e_sec = _Col(np.float32, np.full(m, np.nan))
+        ns._e_inb = _Col(np.float32, np.zeros(m))
+        ns._e_outb = _Col(np.float32, np.zeros(m))
+        ns._e_exists = _Col(np.uint8, np.ones(m))
+        ns._e_transport = _Col(np.uint8, np.zeros(m))
+        if edge_shared_key is None:
+            ns._e_shared = [None] * m
+        else:
+            ns._e_shared = [None if k is None else str(k) for k in edge_shared_key]
+        ns._e_keys = None
+        ns._is_dual = bool(is_dual)
+        return ns
+
+    # ------------------------------------------------------------------ basic state
+    def _touch(self):
+        self._version += 1
+        self._cache.clear()
+
+    def progress_init(self) -> None:
+        self._progress = 0
+
+    def progress(self) -> int:
+        return self._progress
+
+    @property
+    def is_dual(self) -> bool:
+        return self._is_dual
+
+    def set_is_dual(self, is_dual: bool) -> None:
+        self._is_dual = bool(is_dual)
+        self._touch()
+
+    # ------------------------------------------------------------------ builders
+    def add_street_node(self, node_key: Any, x: float, y: float, live: bool, weight: float, z: float | None = None) -> int:
+        """add_street_node (rust/src/graph.rs:426-452)."""
+        w = np.float32(weight)
+        if not np.isfinite(w) or w < 0:
+            raise ValueError(
+                f"Invalid street node payload: weight must be finite and non-negative (>= 0.0). Found {weight}. "
+                f"Node key: {node_key!r}"
+            )
+        return self._add_node(node_key, x, y, z, bool(live), w, False)
+
+    def add_transport_node(self, node_key: Any, x: float, y: float, linking_radius: float | None = None,
+                           z: float | None = None) -> int:
+        """Transport nodes are never live and carry zero weight (rust/src/graph.rs:454-555)."""
+        return self._add_node(node_key, x, y, z, False, np.float32(0.0), True)
+
+    def _add_node(self, key, x, y, z, live, w, transport) -> int:
+        idx = self._x.n
+        if self._keys is None:
+            self._keys = list(range(idx))
+        self._keys.append(key)
+        self._x.append(float(x))
+        self._y.append(float(y))
+        self._z.append(np.nan if z is None else float(z))
+        self._has_z.append(0 if z is None else 1)
+        self._live.append(1 if live else 0)
+        self._weight.append(w)
+        self._exists.append(1)
+        self._transport.append(1 if transport else 0)
+        self._touch()
+        return idx
+
+    def _require_node(self, idx: int, name: str) -> None:
+        if idx < 0 or idx >= self._x.n or not self._exists.view()[idx]:
+            raise ValueError(f"{name} {idx} does not exist in the graph.")
+
+    def add_street_edge(
+        self,
+        start_nd_idx: int,
+        end_nd_idx: int,
+        edge_idx: int,
+        start_nd_key_py: Any,
+        end_nd_key_py: Any,
+        geom_wkt: str,
+        imp_factor: float | None = None,
+        shared_primal_node_key: str | None = None,
+    ) -> int:
+        """add_street_edge (rust/src/graph.rs:727-889): length, bearings, angle_sum from WKT."""
+        coords = parse_linestring_wkt(geom_wkt)
+        if len(coords) < 2:
+            raise ValueError(
+                f"Street edge geometry (idx {edge_idx}) between nodes {start_nd_idx} and {end_nd_idx} must have "
+                f"at least 2 coordinates. Found {len(coords)}."
+            )
+        return self.add_street_edge_coords(start_nd_idx, end_nd_idx, edge_idx, start_nd_key_py, end_nd_key_py,
+                                           coords, imp_factor, shared_primal_node_key)
+
+    def add_street_edge_coords(self, start_nd_idx, end_nd_idx, edge_idx, start_key, end_key, coords,
+                               imp_factor=None, shared_primal_node_key=None) -> int:
+        """add_street_edge with an already parsed coordinate list."""
+        length = np.float32(linestring_length(coords))
+        first, last = coords[0], coords[-1]
+        inb = 0.0
+        for c in coords[1:]:
+            if c[0] != first[0] or c[1] != first[1]:
+                inb = _bearing(first, c)
+                break
+        outb = 0.0
+        for c in reversed(coords[:-1]):
+            if c[0] != last[0] or c[1] != last[1]:
+                outb = _bearing(c, last)
+                break
+        angle_sum = np.float32(cumulative_angle(coords))
+        imp = np.float32(1.0 if imp_factor is None else imp_factor)
+        if not np.isfinite(imp) or imp <= 0:
+            raise ValueError(
+                f"Invalid impedance factor ({imp_factor}) for edge (idx {edge_idx}) between nodes {start_nd_idx} "
+                f"and {end_nd_idx}.\nImpedance must be finite and positive (> 0.0)."
+            )
+        self._require_node(start_nd_idx, "start_nd_idx")
+        self._require_node(end_nd_idx, "end_nd_idx")
+        if not np.isfinite(length):
+            raise ValueError("Invalid street edge payload : length must be finite.")
+        return self._add_edge(start_nd_idx, end_nd_idx, edge_idx, length, angle_sum, imp, np.float32(np.nan),
+                              np.float32(inb), np.float32(outb), shared_primal_node_key, (start_key, end_key), False)
+
+    def add_transport_edge(self, start_nd_idx, end_nd_idx, edge_idx, start_nd_key_py, end_nd_key_py, seconds,
+                           imp_factor=None) -> int:
+        """add_transport_edge (rust/src/graph.rs:946-985): a travel-time edge without geometry."""
+        s = np.float32(seconds)
+        if not np.isfinite(s) or s < 0:
+            raise ValueError(
+                f"Invalid seconds value ({seconds}) for transport edge (idx {edge_idx}) between nodes "
+                f"{start_nd_idx} and {end_nd_idx}."
+            )
+        self._require_node(start_nd_idx, "start_nd_idx")
+        self._require_node(end_nd_idx, "end_nd_idx")
+        imp = np.float32(1.0 if imp_factor is None else imp_factor)
+        return self._add_edge(start_nd_idx, end_nd_idx, edge_idx, np.float32(np.nan), np.float32(np.nan), imp, s,
+                              np.float32(np.nan), np.float32(np.nan), None, (start_nd_key_py, end_nd_key_py), True)
+
+    def _add_edge(self, s, d, eidx, length, ang, imp, sec, inb, outb, shared, keys, transport) -> int:
+        idx = self._e_src.n
+        self._e_src.append(int(s))
+        self._e_dst.append(int(d))
+        self._e_idx.append(int(eidx))
+        self._e_len.append(length)
+        self._e_ang.append(ang)
+        self._e_imp.append(imp)
+        self._e_sec.append(sec)
+        self._e_inb.append(inb)
+        self._e_outb.append(outb)
+        self._e_exists.append(1)
+        self._e_transport.append(1 if transport else 0)
+        self._e_shared.append(None if shared is None else str(shared))
+        if self._e_keys is None:
+            self._e_keys = [None] * idx
+        self._e_keys.append(keys)
+        self._touch()
+        return idx
+
+    def remove_street_node(self, node_idx: int) -> None:
+        """remove_street_node (rust/src/graph.rs:891-916): removes the node and its edges."""
+        if node_idx < 0 or node_idx >= self._x.n or not self._exists.view()[node_idx]:
+            raise ValueError(f"Node index {node_idx} does not exist in the graph.")
+        if self._transport.view()[node_idx]:
+            raise ValueError(
+                f"Node index {node_idx} is a transport node and cannot be removed with remove_street_node."
+            )
+        self._exists.view()[node_idx] = 0
+        es, ed, ex = self._e_src.view(), self._e_dst.view(), self._e_exists.view()
+        ex[(es == node_idx) | (ed == node_idx)] = 0
+        self._touch()
+
+    def remove_street_edge(self, start_nd_idx: int, end_nd_idx: int, edge_idx: int) -> None:
+        """remove_street_edge (rust/src/graph.rs:918-944): the newest matching directed edge."""
+        self._require_node(start_nd_idx, "start_nd_idx")
+        self._require_node(end_nd_idx, "end_nd_idx")
+        e = self._find_edge(start_nd_idx, end_nd_idx, edge_idx)
+        if e < 0:
+            raise ValueError(f"No edge with edge_idx {edge_idx} found from node {start_nd_idx} to node {end_nd_idx}.")
+        self._e_exists.view()[e] = 0
+        self._touch()
+
+    def _find_edge(self, start, end, edge_idx) -> int:
+        es, ed, ei, ex = self._e_src.view(), self._e_dst.view(), self._e_idx.view(), self._e_exists.view()
+        hits = np.nonzero((es == start) & (ed == end) & (ei == edge_idx) & (ex == 1))[0]
+        return int(hits[-1]) if len(hits) else -1
+
+    # ------------------------------------------------------------------ getters
+    def node_count(self) -> int:
+        return int(self._exists.view().sum())
+
+    def node_bound(self) -> int:
+        ex = self._exists.view()
+        nz = np.nonzero(ex)[0]
+        return int(nz[-1]) + 1 if len(nz) else 0
+
+    def edge_bound(self) -> int:
+        ex = self._e_exists.view()
+        nz = np.nonzero(ex)[0]
+        return int(nz[-1]) + 1 if len(nz) else 0
+
+    @property
+    def edge_count(self) -> int:
+        return int(self._e_exists.view().sum())
+
+    def street_node_count(self) -> int:
+        return int(((self._exists.view() == 1) & (self._transport.view() == 0)).sum())
+
+    def node_indices(self) -> list[int]:
+        return np.nonzero(self._exists.view())[0].tolist()
+
+    def street_node_indices(self) -> list[int]:
+        return np.nonzero((self._exists.view() == 1) & (self._transport.view() == 0))[0].tolist()
+
+    def node_keys_py(self) -> list[Any]:
+        idx = np.nonzero(self._exists.view())[0]
+        if self._keys is None:
+            return idx.tolist()
+        return [self._keys[i] for i in idx]
+
+    @property
+    def node_xs(self) -> list[float]:
+        return self._x.view()[self._exists.view() == 1].tolist()
+
+    @property
+    def node_ys(self) -> list[float]:
+        return self._y.view()[self._exists.view() == 1].tolist()
+
+    @property
+    def node_xys(self) -> list[tuple[float, float]]:
+        m = self._exists.view() == 1
+        return list(zip(self._x.view()[m].tolist(), self._y.view()[m].tolist()))
+
+    @property
+    def node_lives(self) -> list[bool]:
+        return [bool(v) for v in self._live.view()[self._exists.view() == 1]]
+
+    def _node_checked(self, node_idx: int) -> None:
+        self._require_node(node_idx, "node_idx")
+
+    def get_node_weight(self, node_idx: int) -> float:
+        self._node_checked(node_idx)
+        return float(self._weight.view()[node_idx])
+
+    def is_node_live(self, node_idx: int) -> bool:
+        self._node_checked(node_idx)
+        return bool(self._live.view()[node_idx])
+
+    def set_node_live(self, node_idx: int, live: bool) -> None:
+        if node_idx < 0 or node_idx >= self._x.n or not self._exists.view()[node_idx]:
+            raise ValueError(f"Node index {node_idx} does not exist in the graph.")
+        self._live.view()[node_idx] = 1 if live else 0
+        self._touch()
+
+    def edge_references(self) -> list[tuple[int, int, int]]:
+        ex = np.nonzero(self._e_exists.view())[0]
+        es, ed, ei = self._e_src.view(), self._e_dst.view(), self._e_idx.view()
+        return [(int(es[e]), int(ed[e]), int(ei[e])) for e in ex]
+
+    def get_edge_length(self, start_nd_idx: int, end_nd_idx: int, edge_idx: int) -> float:
+        self._require_node(start_nd_idx, "start_nd_idx")
+        self._require_node(end_nd_idx, "end_nd_idx")
+        e = self._find_edge(start_nd_idx, end_nd_idx, edge_idx)
+        if e < 0:
+            raise ValueError("Edge not found")
+        return float(self._e_len.view()[e])
+
+    def get_edge_impedance(self, start_nd_idx: int, end_nd_idx: int, edge_idx: int) -> float:
+        self._require_node(start_nd_idx, "start_nd_idx")
+        self._require_node(end_nd_idx, "end_nd_idx")
+        e = self._find_edge(start_nd_idx, end_nd_idx, edge_idx)
+        if e < 0:
+            raise ValueError("Edge not found")
+        return float(self._e_imp.view()[e])
+
+    def validate(self) -> None:
+        """validate (rust/src/graph.rs:1035-1058)."""
+        if self.node_count() == 0:
+            raise ValueError("NetworkStructure contains no nodes.")
+        ex = self._e_exists.view() == 1
+        street = ex & (self._e_transport.view() == 0)
+        if np.any(~np.isfinite(self._e_len.view()[street])):
+            raise ValueError("Invalid street edge payload : length must be finite.")
+        if np.any(~np.isfinite(self._e_ang.view()[street])):
+            raise ValueError("Invalid street edge payload : angle_sum must be finite.")
+        imp = self._e_imp.view()[ex]
+        if np.any(~np.isfinite(imp)) or np.any(imp <= 0):
+            raise ValueError("Invalid edge payload : imp_factor must be finite and positive (> 0.0).")
+
+    def validate_dual_for_angular(self, context: str) -> None:
+        """validate_dual_for_angular (rust/src/graph.rs:1333-1341)."""
+        if not self._is_dual:
+            raise ValueError(
+                f"{context} requires a dual graph for angular analysis. Convert the graph with "
+                "cityseer.tools.graphs.nx_to_dual(...) before ingesting it into NetworkStructure."
+            )
+
+    # ------------------------------------------------------------------ arrays for the device / oracle
+    def arrays(self) -> dict[str, np.ndarray]:
+        """Column view of the graph (node slots and edge slots, with existence flags)."""
+        c = self._cache.get("arrays")
+        if c is not None:
+            return c
+        nb = self._x.n
+        shared = self._e_shared
+        uniq: dict[str, int] = {}
+        sid = np.full(self._e_src.n, -1, np.int32)
+        for i, k in enumerate(shared):
+            if k is not None:
+                sid[i] = uniq.setdefault(k, len(uniq))
+        c = {
+            "n_slots": nb,
+            "node_exists": self._exists.view().copy(),
+            "live": (self._live.view() & self._exists.view()).astype(np.uint8),
+            "weight": self._weight.view().copy(),
+            "has_z": self._has_z.view().copy(),
+            "z": self._z.view().copy(),
+            "e_src": self._e_src.view().copy(),
+            "e_dst": self._e_dst.view().copy(),
+            "e_exists": self._e_exists.view().copy(),
+            "e_idx": self._e_idx.view().copy(),
+            "e_len": self._e_len.view().copy(),
+            "e_ang": self._e_ang.view().copy(),
+            "e_imp": self._e_imp.view().copy(),
+            "e_sec": self._e_sec.view().copy(),
+            "e_shared": sid,
+        }
+        self._cache["arrays"] = c
+        return c
+
+    # ------------------------------------------------------------------ traversals and centrality
+    def _validate_src(self, src_idx: int, speed_m_s: float) -> None:
+        """validate_dijkstra_inputs (rust/src/centrality.rs:1009-1030)."""
+        nb = self.node_bound()
+        if src_idx < 0 or src_idx >= nb:
+            raise ValueError(f"src_idx {src_idx} out of range for network with node_bound {nb}")
+        if not self._exists.view()[src_idx]:
+            raise ValueError(f"src_idx {src_idx} does not exist in the graph")
+        if not math.isfinite(speed_m_s) or speed_m_s <= 0:
+            raise ValueError(f"speed_m_s must be finite and positive, got {speed_m_s}")
+
+    def dijkstra_tree_shortest(self, src_idx: int, max_seconds: int, speed_m_s: float):
+        from . import centrality
+
+        self._validate_src(src_idx, speed_m_s)
+        return centrality.tree_shortest(self, [src_idx], max_seconds, speed_m_s)[0]
+
+    def dijkstra_tree_shortest_batch(self, src_indices: Sequence[int], max_seconds: int, speed_m_s: float):
+        """Many isochrone queries in one launch (one warp per query)."""
+        from . import centrality
+
+        for s in src_indices:
+            self._validate_src(int(s), speed_m_s)
+        return centrality.tree_shortest(self, list(src_indices), max_seconds, speed_m_s)
+
+    def dijkstra_tree_simplest(self, src_idx: int, max_seconds: int, speed_m_s: float):
+        from . import centrality
+
+        self.validate_dual_for_angular("dijkstra_tree_simplest")
+        self._validate_src(src_idx, speed_m_s)
+        return centrality.tree_simplest(self, [src_idx], max_seconds, speed_m_s)[0]
+
+    def centrality_shortest(self, distances=None, betas=None, minutes=None, compute_closeness=None,
+                            compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, tolerance=None,
+                            sample_probability=None, sampling_weights=None, random_seed=None, source_indices=None,
+                            pbar_disabled=None):
+        from . import centrality
+
+        return centrality.centrality_shortest(
+            self, distances=distances, betas=betas, minutes=minutes, compute_closeness=compute_closeness,
+            compute_betweenness=compute_betweenness, min_threshold_wt=min_threshold_wt, speed_m_s=speed_m_s,
+            tolerance=tolerance, sample_probability=sample_probability, sampling_weights=sampling_weights,
+            random_seed=random_seed, source_indices=source_indices, pbar_disabled=pbar_disabled)
+
+    def centrality_simplest(self, distances=None, betas=None, minutes=None, compute_closeness=None,
+                            compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, tolerance=None,
+                            angular_scaling_unit=None, farness_scaling_offset=None, sample_probability=None,
+                            sampling_weights=None, random_seed=None, source_indices=None, pbar_disabled=None):
+        from . import centrality
+
+        return centrality.centrality_simplest(
+            self, distances=distances, betas=betas, minutes=minutes, compute_closeness=compute_closeness,
+            compute_betweenness=compute_betweenness, min_threshold_wt=min_threshold_wt, speed_m_s=speed_m_s,
+            tolerance=tolerance, angular_scaling_unit=angular_scaling_unit,
+            farness_scaling_offset=farness_scaling_offset, sample_probability=sample_probability,
+            sampling_weights=sampling_weights, random_seed=random_seed, source_indices=source_indices,
+            pbar_disabled=pbar_disabled)
+
+    def segment_centrality(self, distances=None, betas=None, minutes=None, compute_closeness=None,
+                           compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, pbar_disabled=None):
+        from . import centrality
+
+        return centrality.segment_centrality(
+            self, distances=distances, betas=betas, minutes=minutes, compute_closeness=compute_closeness,
+            compute_betweenness=compute_betweenness, min_threshold_wt=min_threshold_wt, speed_m_s=speed_m_s,
+            pbar_disabled=pbar_disabled)
+
+    # aliases under the names of earlier cityseer releases
+    def local_node_centrality_shortest(self, *args, **kwargs):
+        return self.centrality_shortest(*args, **kwargs)
+
+    def local_node_centrality_simplest(self, *args, **kwargs):
+        return self.centrality_simplest(*args, **kwargs)
+
+    def local_segment_centrality(self, *args, **kwargs):
+        return self.segment_centrality(*args, **kwargs)

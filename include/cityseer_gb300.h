@@ -1,0 +1,186 @@
+/*
+ * cityseer_gb300.h -- C-ABI of libcsgpu.so, the GB300 (sm_103a) implementation of cityseer's
+ * localised network centrality (cityseer-api v4.24.0, rust/src/centrality.rs).
+ *
+ * Conventions
+ *  - Plain C types only.  Pointers named *_dev are CUDA device pointers owned by the caller; the
+ *    library never frees them.  `stream` is a cudaStream_t passed as void* (NULL = legacy stream).
+ *  - Every entry point returns a cs_status; cs_last_error() gives the message of the last failure
+ *    on the calling thread.  No C++ exception crosses this boundary.
+ *  - Node indices are the reference's StableGraph indices in [0, n_bound); removed nodes simply
+ *    have no edges and are never sources.
+ *  - Output accumulators are caller-zeroed f64 arrays laid out [metric][threshold][n_bound], the
+ *    reference's MetricResult rows (rust/src/common.rs:18-35) stacked per metric.
+ */
+#ifndef CITYSEER_GB300_H
+#define CITYSEER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t cs_status;
+#define CS_OK 0
+#define CS_ERR_ARG 1        /* invalid argument (mirrors the reference's PyValueError paths) */
+#define CS_ERR_CAPACITY 2   /* workspace too small for a source's reach; retried internally */
+#define CS_ERR_CUDA 3       /* CUDA runtime error (no device, launch failure, ...) */
+#define CS_ERR_TIMEOUT 4    /* a bounded device-side wait gave up */
+#define CS_ERR_INTERNAL 5   /* a device-side consistency check failed */
+
+#define CS_MAX_THRESHOLDS 16  /* thresholds per launch; the host layer splits longer lists */
+#define CS_MAX_DEGREE 32      /* max out-degree of a node supported by the replay kernels */
+
+/* Device-resident primal CSR.  Built by cityseer_gb300.device from a NetworkStructure.
+ * in_*  : per node u, the edges v->u in petgraph Incoming order (newest first); searches relax
+ *         these (rust/src/centrality.rs:1389-1405).
+ * out_* : per node v, the edges v->u sorted by (u, newest first); used to replay the order in
+ *         which the reference offers candidates to v (rust/src/centrality.rs:1413-1437).
+ * *_seglen / *_segimp: length / imp_factor of the edge looked up by get_edge_length_unchecked
+ *         (rust/src/graph.rs:1278-1314) for that edge's reverse direction. */
+typedef struct {
+    int32_t n_bound;
+    int32_t n_edges;            /* directed edges in each CSR */
+    int32_t max_out_degree;
+    const int32_t *in_ptr_dev;  /* [n_bound + 1] */
+    const int32_t *in_nb_dev;   /* [n_edges] edge source v of v->u */
+    const float *in_w_dev;      /* [n_edges] travel seconds of v->u (impedance applied) */
+    const float *in_seglen_dev; /* [n_edges] */
+    const float *in_segimp_dev; /* [n_edges] */
+    const int32_t *out_ptr_dev; /* [n_bound + 1] */
+    const int32_t *out_to_dev;  /* [n_edges] edge target u of v->u */
+    const float *out_w_dev;     /* [n_edges] travel seconds of v->u (impedance applied) */
+    const uint8_t *out_cnt_dev; /* [n_edges] 1 = counts once for the circuit rank's edge set */
+    const float *out_seglen_dev;/* [n_edges] */
+    const float *node_w_dev;    /* [n_bound] node weight */
+} cs_primal_graph;
+
+/* Device-resident dual CSR for simplest (angular) routing (rust/src/centrality.rs:533-775):
+ * per dual node, its outgoing dual edges in petgraph Outgoing order (newest first). */
+typedef struct {
+    int32_t n_bound;
+    int32_t n_edges;
+    int32_t max_out_degree;
+    const int32_t *ptr_dev;     /* [n_bound + 1] */
+    const int32_t *to_dev;      /* [n_edges] */
+    const float *w_dev;         /* [n_edges] travel seconds, no impedance */
+    const float *ang_dev;       /* [n_edges] angle_sum */
+    const float *len_dev;       /* [n_edges] length */
+    const uint8_t *exit_slot_dev;  /* [n_edges] slot of the shared primal node at the edge source */
+    const uint8_t *entry_slot_dev; /* [n_edges] slot of the shared primal node at the edge target */
+    const int32_t *rptr_dev;    /* [n_bound + 1] incoming edges (reverse CSR of the same edges) */
+    const int32_t *rfrom_dev;   /* [n_edges] source node of each incoming edge */
+    const int32_t *rid_dev;     /* [n_edges] index of that edge in the forward arrays */
+} cs_dual_graph;
+
+/* One centrality call.  Thresholds are the reference's resolved (distances, betas, seconds)
+ * triple from pair_distances_betas_time (rust/src/common.rs:239-270). */
+typedef struct {
+    int32_t k;                               /* number of thresholds, 1..CS_MAX_THRESHOLDS */
+    uint32_t distances[CS_MAX_THRESHOLDS];   /* metres */
+    float betas[CS_MAX_THRESHOLDS];
+    uint32_t seconds[CS_MAX_THRESHOLDS];
+    float speed_m_s;
+    float tolerance;              /* validated decimal tolerance, >= 1e-4 */
+    float angular_scaling_unit;   /* simplest only */
+    float farness_scaling_offset; /* simplest only */
+    int32_t compute_closeness;
+    int32_t compute_betweenness;
+    int32_t track_reach;          /* count reachability_totals (sampling / source subset) */
+    int64_t n_sources;
+    const int32_t *sources_dev;   /* [n_sources] node indices to process, in order */
+    const float *src_wt_dev;      /* [n_bound] per-source weight (node weight / sampling p) */
+    const uint8_t *eligible_dev;  /* [n_bound] source_eligible (pair weights 0.5 vs 1.0) */
+} cs_query;
+
+/* Launch plan: how many concurrent per-source searches and how much workspace they need. */
+typedef struct {
+    int32_t n_slots;      /* concurrent searches (one warp each) */
+    int32_t cap;          /* reached-set capacity per search */
+    int32_t threads_per_block;
+    int32_t blocks;
+    float delta_seconds;  /* band width of the label-correcting search; <= 0 picks a default */
+    int32_t lanes;        /* f64 accumulator lanes per reached node */
+    size_t workspace_bytes;
+} cs_plan;
+
+/* Outputs: f64 rows [metric][k][n_bound]; reach_dev: u32[k] (may be NULL when !track_reach). */
+typedef struct {
+    double *out_dev;
+    uint32_t *reach_dev;
+} cs_outputs;
+
+/* Thread-local message of the last failing call. */
+size_t cs_last_error(char *buf, size_t len);
+
+/* Host-side threshold conversions, f32-exact restatements of rust/src/common.rs:99-270.
+ * mode: 0 = distances given, 1 = betas given, 2 = minutes given.  On success fills all three
+ * output arrays (length k).  min_threshold_wt < 0 selects the default MIN_THRESH_WT. */
+cs_status cs_pair_distances_betas_time(float speed_m_s, int32_t mode, int32_t k, const uint32_t *distances,
+                                       const float *betas, const float *minutes, float min_threshold_wt,
+                                       uint32_t *out_distances, float *out_betas, uint32_t *out_seconds);
+
+/* Host-side per-edge travel seconds, rust/src/centrality.rs:961-1007 (edge_travel_seconds with the
+ * Tobler slope penalty).  has_z/z per node may be NULL.  seconds: NaN for street edges. */
+cs_status cs_edge_travel_seconds(int64_t n_edges, const int32_t *src, const int32_t *dst, const float *length,
+                                 const float *imp_factor, const float *seconds, const uint8_t *has_z,
+                                 const double *z, float speed_m_s, int32_t use_impedance, float *out);
+
+/* Plans a call: n_slots/cap/threads/blocks and the workspace size.  cap <= 0 picks a default;
+ * max_slots <= 0 uses every resident warp; mem_budget_bytes <= 0 means no budget.
+ * mode: 0 = centrality_shortest, 1 = segment_centrality, 2 = trees (isochrones). */
+cs_status cs_plan_primal(const cs_primal_graph *g, int32_t mode, int32_t k, int32_t cap, int32_t max_slots,
+                         int64_t mem_budget_bytes, cs_plan *plan);
+cs_status cs_plan_dual(const cs_dual_graph *g, int32_t mode, int32_t k, int32_t cap, int32_t max_slots,
+                       int64_t mem_budget_bytes, cs_plan *plan);
+
+/* Puts a freshly allocated workspace into the clean state every call expects (and leaves).
+ * Call once after allocating it, and again after any call that returned an error. */
+cs_status cs_workspace_init(const cs_plan *plan, int32_t n_bound, void *workspace_dev, size_t workspace_bytes,
+                            void *stream);
+
+/* Replaces NetworkStructure.centrality_shortest (rust/src/centrality.rs:1624-1874).
+ * out rows: 0 density, 1 farness, 2 cycles, 3 harmonic, 4 beta, 5 betweenness, 6 betweenness_beta.
+ * Sources whose reach exceeds plan->cap are re-run with a larger capacity inside the call. */
+cs_status cs_centrality_shortest(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan,
+                                 void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream);
+
+/* Replaces NetworkStructure.centrality_simplest (rust/src/centrality.rs:1880-2132) on a dual graph.
+ * out rows: 0 density, 1 farness, 2 harmonic, 3 betweenness. */
+cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, const cs_plan *plan,
+                                 void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream);
+
+/* Replaces NetworkStructure.segment_centrality (rust/src/centrality.rs:2134-2407).
+ * out rows: 0 segment_density, 1 segment_harmonic, 2 segment_beta, 3 segment_betweenness.
+ * q->sources_dev lists the live sources (segment centrality has no sampling). */
+cs_status cs_segment_centrality(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan,
+                                void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream);
+
+/* Replaces NetworkStructure.dijkstra_tree_shortest (rust/src/centrality.rs:1141-1200, 1500-1508)
+ * for a batch of sources: per query q, visited nodes in settle order with their agg_seconds and
+ * predecessor.  count_dev[q] = number visited (or -1 if it exceeds row_cap); rows are row_cap wide. */
+cs_status cs_tree_shortest(const cs_primal_graph *g, int32_t n_queries, const int32_t *src_dev, uint32_t max_seconds,
+                           float speed_m_s, const cs_plan *plan, void *workspace_dev, size_t workspace_bytes,
+                           int32_t row_cap, int32_t *count_dev, int32_t *node_dev, float *agg_seconds_dev,
+                           int32_t *pred_dev, void *stream);
+
+/* Same for dijkstra_tree_simplest (rust/src/centrality.rs:1202-1332, 1510-1521) on a dual graph:
+ * per query, reached dual nodes with simpl_dist, agg_seconds and node-level predecessor. */
+cs_status cs_tree_simplest(const cs_dual_graph *g, int32_t n_queries, const int32_t *src_dev, uint32_t max_seconds,
+                           float speed_m_s, const cs_plan *plan, void *workspace_dev, size_t workspace_bytes,
+                           int32_t row_cap, int32_t *count_dev, int32_t *node_dev, float *simpl_dev,
+                           float *agg_seconds_dev, int32_t *pred_dev, void *stream);
+
+/* Device counters of the last call on this thread: sources done, edges relaxed, nodes settled
+ * (used for throughput and roofline accounting) and the number of kernels it launched. */
+cs_status cs_last_counters(int64_t *sources, int64_t *edges_relaxed, int64_t *nodes_settled, int64_t *launches);
+
+/* Number of SMs of the current device (0 on failure). */
+int32_t cs_device_sm_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CITYSEER_GB300_H */
