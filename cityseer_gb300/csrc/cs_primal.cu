@@ -1159,3 +1159,100 @@ cs_status cs_tree_shortest(const cs_primal_graph *g, int32_t n_queries, const in
 }
 
 }  // extern "C"
+
+// ==========================================================================================
+// Allocation-free entry point (cs_centrality_shortest_noalloc).
+//
+// Some callers cannot allocate device memory at the time they want centralities: code running
+// inside a host application that owns every device allocation through its own pool, plugins whose
+// memory budget is fixed when the process starts, or code paths where an allocation could fail or
+// block.  For them this entry point draws its scratch from one static device array that the CUDA
+// module reserves when it is loaded, so the call itself allocates nothing.
+//
+// Limits and rules:
+//  - The array holds 64 MiB; every GPU that loads this library keeps it until the process exits.
+//  - One search needs 8 bytes per node of dense state plus its per-node arrays for the whole
+//    graph (the capacity is node_bound, so no search can overflow).  Graphs whose single search
+//    does not fit are rejected with CS_ERR_ARG and a message naming the sizes.
+//  - All calls share the array and it keeps the previous call's contents; each call therefore
+//    re-initialises the state that must start clean.  Calls that overlap on the GPU (two streams,
+//    two host threads) race on the array: issue them one after another.
+//  - The first call on a device looks up the array's device address with cudaGetSymbolAddress
+//    while that device is current; make that first call before any stream capture begins.
+// ==========================================================================================
+#include <mutex>
+
+namespace {
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
+}  // namespace
+
+static __device__ __align__(256) unsigned char cs_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[128] = {};
+
+cs_status noalloc_scratch_address(void **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 128) return fail(CS_ERR_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, cs_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
+        if (!p) return fail(CS_ERR_CUDA, "static scratch has no device address");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return CS_OK;
+}
+}  // namespace
+
+extern "C" cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, const cs_query *q, cs_outputs out,
+                                                    void *stream) {
+    cs_status st = validate_primal(g);
+    if (st != CS_OK) return st;
+    if (!q) return fail(CS_ERR_ARG, "query is NULL");
+    if (q->k < 1 || q->k > CS_MAX_THRESHOLDS) return fail(CS_ERR_ARG, "threshold count out of range");
+    const int P = std::max(1, g->max_out_degree);
+    const int L = lanes_for(cs::MODE_SHORTEST, q->k);
+    const int cap = g->n_bound;  // a search can never overflow: no retry pass is needed
+    const size_t one = layout(g->n_bound, 1, cap, P, L).total;
+    if (one > kNoAllocScratchBytes)
+        return fail(CS_ERR_ARG, "graph too large for the allocation-free path: one search needs " +
+                                    std::to_string(one) + " bytes of scratch, the static array holds " +
+                                    std::to_string(kNoAllocScratchBytes) + " bytes");
+    int sms = sm_count();
+    if (sms <= 0) return fail(CS_ERR_CUDA, "no CUDA device");
+    int bpsm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, cs::primal_kernel, 256, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
+    int slots = std::max(1, sms * std::max(1, bpsm) * 8);
+    while (slots > 1 && layout(g->n_bound, slots, cap, P, L).total > kNoAllocScratchBytes) {
+        const int next = (slots * 7) / 8;
+        slots = next < slots ? next : slots - 1;
+    }
+    void *ws = nullptr;
+    st = noalloc_scratch_address(&ws);
+    if (st != CS_OK) return st;
+    cs_plan plan;
+    memset(&plan, 0, sizeof(plan));
+    plan.n_slots = slots;
+    plan.cap = cap;
+    plan.threads_per_block = 256;
+    plan.blocks = (slots + 7) / 8;
+    plan.delta_seconds = 0.0f;
+    plan.lanes = L;
+    const Layout lay = layout(g->n_bound, slots, cap, P, L);
+    plan.workspace_bytes = lay.total;
+    cudaStream_t s = (cudaStream_t)stream;
+    // the array keeps whatever the previous call (or module load, which zeroes it) left there
+    e = cudaMemsetAsync(ws, 0, 256, s);
+    if (e != cudaSuccess) return cuda_fail(e, "static scratch header reset");
+    st = reset_dense((char *)ws + lay.dense_off, lay.dense_stride, g->n_bound, slots, s);
+    if (st != CS_OK) return st;
+    return run_primal(g, q, &plan, ws, kNoAllocScratchBytes, out, stream, cs::MODE_SHORTEST, 0, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, 0, 0, 0.0f);
+}

@@ -147,6 +147,18 @@ cs_status cs_workspace_init(const cs_plan *plan, int32_t n_bound, void *workspac
 cs_status cs_centrality_shortest(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan,
                                  void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream);
 
+/* Allocation-free variant of cs_centrality_shortest, for callers that cannot allocate device memory
+ * when they call (a host application that owns all device memory through its own pool, a plugin
+ * with a fixed memory budget, code that must not block or fail on an allocation).  It has no
+ * counterpart in the reference: the Rust code allocates per call.  Its scratch is one static 64 MiB
+ * device array reserved when the library's CUDA module loads; no workspace is passed and nothing
+ * is allocated.  Same inputs, outputs and results as cs_centrality_shortest.  Graphs whose single
+ * search needs more than 64 MiB of scratch are rejected with CS_ERR_ARG.  All calls share the array:
+ * calls that overlap on the GPU race, so issue them one after another.  The first call on each
+ * device looks up the array's address (cudaGetSymbolAddress) with that device current; make it
+ * before any stream capture. */
+cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, const cs_query *q, cs_outputs out, void *stream);
+
 /* Replaces NetworkStructure.centrality_simplest (rust/src/centrality.rs:1880-2132) on a dual graph.
  * out rows: 0 density, 1 farness, 2 harmonic, 3 betweenness. */
 cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, const cs_plan *plan,
