@@ -215,7 +215,7 @@ def run_gpu(args):
     # ---- resident state (as the public API leaves it after a first call)
     first = ns.centrality_shortest(distances=dists)
     csr = centrality._primal_csr(ns)
-    wsp = centrality._workspace(ns, csr, 0, K, speed)
+    wsp = centrality._workspace(ns, csr, 0, K, speed, max(s))
     sp = centrality.prepare_source_sampling(ns, None, None, None, None)
     proc_t = torch.from_numpy(sp.process).to(dev)
     wt_t = torch.from_numpy(sp.src_wt).to(dev)
@@ -260,6 +260,9 @@ def run_gpu(args):
         c = centrality.last_counters()
         counters.append(c)
         launches += c[3]
+    ph = (C.c_int64 * 8)()
+    lib.cs_last_phase_cycles(ph, 8)
+    ph = [int(x) for x in ph][:7]
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
@@ -301,7 +304,7 @@ def run_gpu(args):
     h2d = host.nbytes(speed) + sp.process.nbytes + sp.src_wt.nbytes + sp.eligible.nbytes
     d2h = 7 * K * nb * 8 + K * 4
     e2e_times = []
-    for i in range(args.e2e_steps + 1):
+    for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         centrality.drop_device_state(ns)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -310,7 +313,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         if i > 0:
             e2e_times.append(time.perf_counter() - t0)
-    e2e_v = ws * n_src / float(np.mean(e2e_times))
+    e2e_v = ws * n_src / float(np.mean(e2e_times)) if e2e_times else None
     line = {
         "metric": METRIC,
         "value": value,
@@ -339,6 +342,8 @@ def run_gpu(args):
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": roofline,
         "gpu_launches": int(launches),
+        "phase_share": {nm: round(v / max(1, sum(ph)), 4) for nm, v in
+                        zip(("search", "sort", "replay", "closeness", "sigma", "backward", "reset"), ph)},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu:

@@ -145,6 +145,11 @@ SIGNATURES = {
     ),
     "cs_last_counters": (C.c_int32, [C.POINTER(C.c_int64)] * 4),
     "cs_device_sm_count": (C.c_int32, []),
+    "cs_last_phase_cycles": (C.c_int32, [_ptr, C.c_int32]),
+    "cs_centrality_shortest_noalloc": (
+        C.c_int32,
+        [C.POINTER(PrimalGraph), C.POINTER(Query), Outputs, _ptr],
+    ),
 }
 
 _lib = None

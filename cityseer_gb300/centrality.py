@@ -196,15 +196,53 @@ def drop_device_state(ns, keep_workspace: bool = True) -> None:
             del ns._cache[k]
 
 
-def _workspace(ns, csr, mode: int, k: int, speed: float, key_extra=()) -> device.Workspace:
-    key = ("ws", mode, k) + tuple(key_extra)
+def estimate_reach(ns, csr, speed: float, max_seconds: int, n_samples: int = 48) -> int:
+    """Largest reach (nodes settled) over an even sample of sources, from the tree kernel run with
+    one-wide rows (it then reports only the count)."""
+    key = ("reach", float(np.float32(speed)), int(max_seconds))
+    hit = ns._cache.get(key)
+    if hit is not None:
+        return hit
+    idx = np.asarray(ns.node_indices(), np.int64)
+    if len(idx) == 0:
+        return 1
+    pick = idx[np.linspace(0, len(idx) - 1, min(n_samples, len(idx))).astype(np.int64)]
+    lib = _native.load()
+    plan = device.plan_primal(csr, 2, 1, speed, cap=csr.n_bound, max_slots=len(pick))
+    ws = device.Workspace(plan, csr.n_bound, csr.device)
+    dev = csr.device
+    src_t = torch.from_numpy(pick.astype(np.int32)).to(dev)
+    count = torch.zeros(len(pick), dtype=torch.int32, device=dev)
+    scratch = torch.zeros(len(pick), dtype=torch.int32, device=dev)
+    aggs = torch.zeros(len(pick), dtype=torch.float32, device=dev)
+    rc = lib.cs_tree_shortest(C.byref(csr.struct(speed)), len(pick), src_t.data_ptr(), int(max_seconds),
+                              C.c_float(speed), C.byref(plan), ws.ptr, ws.nbytes, 1, count.data_ptr(),
+                              scratch.data_ptr(), aggs.data_ptr(), scratch.data_ptr(), _stream_ptr())
+    _native.check(rc, "reach estimate")
+    r = int(np.abs(count.cpu().numpy()).max())
+    del ws
+    ns._cache[key] = r
+    return r
+
+
+def _mem_budget(device_: torch.device) -> int:
+    free, total = torch.cuda.mem_get_info(device_)
+    return int(min(free * 0.6, 96 << 30))
+
+
+def _workspace(ns, csr, mode: int, k: int, speed: float, max_seconds: int | None = None) -> device.Workspace:
+    cap = 0
+    if max_seconds is not None and mode != 2:
+        r = estimate_reach(ns, csr, speed, max_seconds)
+        cap = int(min(csr.n_bound, max(1024, -(-int(r * 1.3) // 256) * 256)))
+    key = ("ws", mode, k, cap)
     ws = ns._cache.get(key)
     if ws is None:
         # free other workspaces of this graph first: they can be large
         for kk in [kk for kk in ns._cache if isinstance(kk, tuple) and kk and kk[0] == "ws"]:
             del ns._cache[kk]
         torch.cuda.empty_cache()
-        plan = device.plan_primal(csr, mode, k, speed)
+        plan = device.plan_primal(csr, mode, k, speed, cap=cap, mem_budget=_mem_budget(csr.device))
         ws = device.Workspace(plan, csr.n_bound, csr.device)
         ns._cache[key] = ws
     return ws
@@ -235,6 +273,7 @@ def _make_query(dists, betas, secs, speed, tol, closeness, betweenness, track_re
     q.sources = proc_t.data_ptr() if proc_t.numel() else None
     q.src_wt = wt_t.data_ptr()
     q.eligible = el_t.data_ptr()
+    q._keep = (proc_t, wt_t, el_t)  # the device arrays must outlive every launch using q
     return q
 
 
@@ -273,7 +312,7 @@ def centrality_shortest(ns, distances=None, betas=None, minutes=None, compute_cl
     lib = _native.load()
     for lo, hi in _groups(K):
         k = hi - lo
-        ws = _workspace(ns, csr, 0, k, speed)
+        ws = _workspace(ns, csr, 0, k, speed, max(secs[lo:hi]))
         out = torch.zeros((7, k, nb), dtype=torch.float64, device=dev)
         reach = torch.zeros(k, dtype=torch.int32, device=dev)
         q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, tol, closeness, betweenness, track,
@@ -356,7 +395,7 @@ def segment_centrality(ns, distances=None, betas=None, minutes=None, compute_clo
     lib = _native.load()
     for lo, hi in _groups(K):
         k = hi - lo
-        ws = _workspace(ns, csr, 1, k, speed)
+        ws = _workspace(ns, csr, 1, k, speed, max(secs[lo:hi]))
         out = torch.zeros((4, k, nb), dtype=torch.float64, device=dev)
         q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, float(TIE_EPSILON), closeness, betweenness,
                         False, proc_t, wt_t, el_t)

@@ -108,9 +108,11 @@ struct PrimalParams {
     const float *src_wt;
     const uint8_t *eligible;
     double *out;
+    double *bucket;  // [3][K][N] threshold-bucketed closeness terms (density, farness, harmonic)
     uint32_t *reach;
     WsHeader *hdr;
-    int32_t *failed;  // [n_slots] source node indices that overflowed
+    int32_t *failed;  // [fail_cap] indices (into src_list) of sources that overflowed
+    int32_t fail_cap;
     char *dense;
     size_t dense_stride;
     char *compact;
@@ -331,7 +333,8 @@ struct Offer {
 
 // Gathers the candidate offers to v (out-edges v->u with u settled before v), stably sorted by
 // the offering node's settle position.  Returns the count.
-__device__ __forceinline__ int gather_offers(const PrimalParams &p, const SlotPtrs &s, int v, int i, Offer *off) {
+__device__ __forceinline__ int gather_offers(const PrimalParams &p, const SlotPtrs &s, int v, int i, int R, Offer *off,
+                                             bool &bad) {
     const int beg = __ldg(&p.g.out_ptr_dev[v]);
     const int end = __ldg(&p.g.out_ptr_dev[v + 1]);
     int n = 0;
@@ -340,6 +343,7 @@ __device__ __forceinline__ int gather_offers(const PrimalParams &p, const SlotPt
         if (u == v) continue;
         const uint32_t a = s.aux[u];
         if (a == 0u) continue;
+        if (a > (uint32_t)R) { bad = true; continue; }
         const int pu = (int)a - 1;
         if (pu >= i) continue;
         const float c = fadd(s.sd[pu], __ldg(&p.g.out_w_dev[e]));
@@ -411,44 +415,79 @@ __device__ __forceinline__ float route_cost(float secs, float speed) { return fm
 // ------------------------------------------------------------------------------------------
 // 4a. Shortest-path centrality for one source (after search and sort).
 // ------------------------------------------------------------------------------------------
-__device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R) {
+__device__ __forceinline__ void phase_mark(long long *ph, int idx, long long &t) {
+    const long long now = clock64();
+    ph[idx] += now - t;
+    t = now;
+}
+
+// f32 -> f64 by integer ops: keeps the conversion off GB300's narrow FP64 pipe.  Exact for
+// every finite f32; zeros, subnormals, infinities and NaN take the hardware conversion.
+__device__ __forceinline__ double f2d(float x) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    const uint32_t lo = b << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// first threshold index k with c <= dk[k] (thresholds strictly increasing), K if none
+__device__ __forceinline__ int first_k(const PrimalParams &p, float c) {
+    int k = 0;
+    while (k < p.k && !(c <= p.dk[k])) k++;
+    return k;
+}
+
+__device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R, long long *ph,
+                                    int *cnt) {
     const int lane = lane_id();
+    long long tph = clock64();
     const int K = p.k;
     const int P = p.P;
     const int N = p.g.n_bound;
     const float wt = __ldg(&p.src_wt[src]);
     const float cycles_wt = wt / __ldg(&p.g.node_w_dev[src]);
-    // --- predecessor replay + circuit-rank edge counts
-    int ecount[MAXK];
-    int ncount[MAXK];
-#pragma unroll
-    for (int k = 0; k < MAXK; k++) { ecount[k] = 0; ncount[k] = 0; }
+    // cnt[0..K): nodes whose first qualifying threshold is k; cnt[MAXK..MAXK+K): same for edges
+    for (int q = lane; q < 2 * MAXK; q += 32) cnt[q] = 0;
+    __syncwarp();
+    // --- one pass over out-edges: circuit-rank counts and predecessor replay
     bool bad = false;
     for (int i = lane; i < R; i += 32) {
         const int v = s.ord[i];
         const float dv = s.sd[i];
         const float cv = route_cost(dv, p.speed);
-#pragma unroll
-        for (int k = 0; k < MAXK; k++) if (k < K && cv <= p.dk[k]) ncount[k]++;
-        if (p.closeness) {
-            const int beg = __ldg(&p.g.out_ptr_dev[v]);
-            const int end = __ldg(&p.g.out_ptr_dev[v + 1]);
-            for (int e = beg; e < end; e++) {
-                if (!__ldg(&p.g.out_cnt_dev[e])) continue;
-                const int u = __ldg(&p.g.out_to_dev[e]);
-                if (u == v) continue;
-                const uint32_t a = s.aux[u];
-                if (a == 0u) continue;
-                const float cu = route_cost(s.sd[a - 1], p.speed);
-                const float ec = fmaxf(cv, cu);
-#pragma unroll
-                for (int k = 0; k < MAXK; k++) if (k < K && ec <= p.dk[k]) ecount[k]++;
+        const int k0v = first_k(p, cv);
+        if (k0v < K) atomicAdd(&cnt[k0v], 1);
+        const int beg = __ldg(&p.g.out_ptr_dev[v]);
+        const int end = __ldg(&p.g.out_ptr_dev[v + 1]);
+        Offer off[MAXDEG];
+        int n = 0;
+        for (int e = beg; e < end; e++) {
+            const int u = __ldg(&p.g.out_to_dev[e]);
+            if (u == v) continue;
+            const uint32_t a = s.aux[u];
+            if (a == 0u) continue;
+            if (a > (uint32_t)R) { bad = true; continue; }  // scratch not clean: refuse to index
+            const int pu = (int)a - 1;
+            const float du = s.sd[pu];
+            if (p.closeness && __ldg(&p.g.out_cnt_dev[e])) {
+                const float ec = fmaxf(cv, route_cost(du, p.speed));
+                const int k0e = first_k(p, ec);
+                if (k0e < K) atomicAdd(&cnt[MAXK + k0e], 1);
+            }
+            if (p.betweenness && pu < i && n < MAXDEG) {
+                const float c = fadd(du, __ldg(&p.g.out_w_dev[e]));
+                int q = n;
+                while (q > 0 && off[q - 1].pos > pu) { off[q] = off[q - 1]; q--; }
+                off[q].pos = pu;
+                off[q].c = c;
+                off[q].e = e;
+                n++;
             }
         }
         if (!p.betweenness) continue;
         if (i == 0) { s.np[0] = 0; continue; }
-        Offer off[MAXDEG];
-        const int n = gather_offers(p, s, v, i, off);
         int preds[MAXDEG];
         const int np = replay_brandes(p, off, n, dv, preds);
         if (np < 0 || np > P) { bad = true; s.np[i] = 0; continue; }
@@ -459,36 +498,44 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
         if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 1);
     }
     __syncwarp();
-    // --- closeness (rust/src/centrality.rs:1733-1780)
+    phase_mark(ph, 2, tph);
+    // --- closeness (rust/src/centrality.rs:1733-1780).  Density, farness and harmonic terms do not
+    // depend on the threshold: they go once into the bucket of the first qualifying threshold and a
+    // prefix over thresholds after the launch completes them.  Cycles and beta terms are per k.
     if (p.closeness) {
-        float rank[MAXK];
+        float rankw[MAXK];
+        long long nc = 0, ec = 0;
 #pragma unroll
         for (int k = 0; k < MAXK; k++) {
-            const long long nc = warp_sum_ll(ncount[k]);
-            const long long ec = warp_sum_ll(ecount[k]);
+            nc += cnt[k];
+            ec += cnt[MAXK + k];
             const long long r = ec - nc + 1;
-            rank[k] = (nc == 0) ? 0.0f : (float)(r > 0 ? r : 0);
+            const float rank = (nc == 0) ? 0.0f : (float)(r > 0 ? r : 0);
+            rankw[k] = fmul(rank, cycles_wt);
             if (p.track_reach && k < K && lane == 0 && nc > 1) atomicAdd(&p.reach[k], (unsigned)(nc - 1));
         }
+        const double wt_d = f2d(wt);
+        const size_t KN = (size_t)K * N;
         for (int i = 1 + lane; i < R; i += 32) {
             const int t = s.ord[i];
             const float c = route_cost(s.sd[i], p.speed);
-#pragma unroll
-            for (int k = 0; k < MAXK; k++) {
-                if (k < K && c <= p.dk[k]) {
-                    double *row = p.out + (size_t)k * N;
-                    const size_t MS = (size_t)K * N;
-                    atomicAdd(row + 0 * MS + t, (double)wt);
-                    atomicAdd(row + 1 * MS + t, (double)fmul(c, wt));
-                    atomicAdd(row + 2 * MS + t, (double)fmul(rank[k], cycles_wt));
-                    atomicAdd(row + 3 * MS + t, (double)fmul(__fdiv_rn(1.0f, c), wt));
-                    atomicAdd(row + 4 * MS + t, (double)fmul(expf(fmul(-p.beta[k], c)), wt));
-                }
+            const int k0 = first_k(p, c);
+            if (k0 >= K) continue;
+            double *bk = p.bucket + (size_t)k0 * N + t;
+            atomicAdd(bk, wt_d);
+            atomicAdd(bk + KN, f2d(fmul(c, wt)));
+            atomicAdd(bk + 2 * KN, f2d(fmul(__fdiv_rn(1.0f, c), wt)));
+            for (int k = k0; k < K; k++) {
+                double *row = p.out + (size_t)k * N + t;
+                atomicAdd(row + 2 * KN, f2d(rankw[k]));
+                atomicAdd(row + 4 * KN, f2d(fmul(expf(fmul(-p.beta[k], c)), wt)));
             }
         }
     }
+    phase_mark(ph, 3, tph);
     if (!p.betweenness) return;
-    // --- sigma in settle order (chunked, ready when all in-chunk preds are done)
+    // --- sigma (f32 path counts) in settle order, chunked: ready once in-chunk preds are done
+    float *sig = (float *)s.sig;
     for (int base = 0; base < R; base += 32) {
         const int i = base + lane;
         const bool act = i < R;
@@ -505,13 +552,13 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
         while (done != FULL) {
             const bool ready = !mine && ((pm & ~done) == 0u);
             if (ready) {
-                double sg;
-                if (i == 0) sg = 1.0;
+                float sg;
+                if (i == 0) sg = 1.0f;
                 else {
-                    sg = 0.0;
-                    for (int r = 0; r < np; r++) sg += s.sig[pl[r]];
+                    sg = 0.0f;
+                    for (int r = 0; r < np; r++) sg = fadd(sg, sig[pl[r]]);
                 }
-                s.sig[i] = sg;
+                sig[i] = sg;
                 mine = true;
             }
             __syncwarp();
@@ -523,13 +570,16 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
             return;
         }
     }
-    // --- backward Brandes sweep with 2K lanes (rust/src/centrality.rs:823-873, 1782-1835)
-    const int L = p.L;  // = 2K
-    for (int i = lane; i < R; i += 32) {
-        double *dl = s.dl + (size_t)i * L;
-        for (int q = 0; q < 2 * K; q++) dl[q] = 0.0;
-    }
+    phase_mark(ph, 4, tph);
+    // --- backward Brandes sweep, all K thresholds in one pass (rust/src/centrality.rs:823-873,
+    // 1782-1835).  Dependencies accumulate in f32: for sources whose paths are unique (sigma == 1)
+    // they are half-integers and exact; otherwise they carry f32 rounding (well inside 1e-5).
+    const int L = p.L;  // 2K floats per node: [0,K) plain, [K,2K) beta-weighted
+    float *dl = (float *)s.dl;
+    for (int i = lane; i < R; i += 32)
+        for (int q = 0; q < 2 * K; q++) dl[(size_t)i * L + q] = 0.0f;
     __syncwarp();
+    const bool unit_wt = (wt == 1.0f);
     const double wtd = (double)wt;
     const int nchunks = (R + 31) / 32;
     for (int ch = nchunks - 1; ch >= 0; ch--) {
@@ -552,30 +602,35 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
             if (ready) {
                 const int v = s.ord[i];
                 const float cost = route_cost(s.sd[i], p.speed);
-                const double sw = s.sig[i];
-                const double pair = __ldg(&p.eligible[v]) ? 0.5 : 1.0;
-                double *dl = s.dl + (size_t)i * L;
-                for (int k = 0; k < K; k++) {
-                    if (!(cost <= p.dk[k])) continue;
-                    if (sw == 0.0) continue;
-                    const double seed = (i == 0) ? 0.0 : pair;
-                    const double seedb = (i == 0) ? 0.0 : pair * exp(-(double)p.beta[k] * (double)cost);
-                    const double dep = seed + __ldcg(&dl[k]);
-                    const double depb = seedb + __ldcg(&dl[K + k]);
-                    if (dep == 0.0 && depb == 0.0) continue;
+                const float sw = sig[i];
+                const float pair = __ldg(&p.eligible[v]) ? 0.5f : 1.0f;
+                float fr[MAXDEG];
+                for (int r = 0; r < np; r++) {
+                    const float sv = sig[pl[r]];
+                    fr[r] = (sv == sw) ? 1.0f : __fdiv_rn(sv, sw);
+                }
+                float *dli = dl + (size_t)i * L;
+                const int k0 = first_k(p, cost);
+                for (int k = k0; k < K; k++) {
+                    if (sw == 0.0f) break;
+                    const float seed = (i == 0) ? 0.0f : pair;
+                    const float seedb = (i == 0) ? 0.0f : fmul(pair, expf(fmul(-p.beta[k], cost)));
+                    const float dep = fadd(seed, __ldcg(&dli[k]));
+                    const float depb = fadd(seedb, __ldcg(&dli[K + k]));
+                    if (dep == 0.0f && depb == 0.0f) continue;
                     for (int r = 0; r < np; r++) {
-                        const double sv = s.sig[pl[r]];
-                        if (sv == 0.0) continue;
-                        const double f = sv / sw;
-                        double *pd = s.dl + (size_t)pl[r] * L;
-                        atomicAdd(&pd[k], f * dep);
-                        atomicAdd(&pd[K + k], f * depb);
+                        if (fr[r] == 0.0f) continue;
+                        float *pd = dl + (size_t)pl[r] * L;
+                        atomicAdd(&pd[k], fmul(fr[r], dep));
+                        atomicAdd(&pd[K + k], fmul(fr[r], depb));
                     }
                     if (v == src) continue;
-                    const double credit = dep - seed;
-                    const double creditb = depb - seedb;
-                    if (credit > 0.0) atomicAdd(p.out + ((size_t)5 * K + k) * N + v, credit * wtd);
-                    if (creditb > 0.0) atomicAdd(p.out + ((size_t)6 * K + k) * N + v, creditb * wtd);
+                    const float credit = __fadd_rn(dep, -seed);
+                    const float creditb = __fadd_rn(depb, -seedb);
+                    if (credit > 0.0f)
+                        atomicAdd(p.out + ((size_t)5 * K + k) * N + v, unit_wt ? f2d(credit) : f2d(credit) * wtd);
+                    if (creditb > 0.0f)
+                        atomicAdd(p.out + ((size_t)6 * K + k) * N + v, unit_wt ? f2d(creditb) : f2d(creditb) * wtd);
                 }
                 mine = true;
             }
@@ -586,6 +641,23 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
         if (done != FULL) {
             if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 3);
             return;
+        }
+    }
+    phase_mark(ph, 5, tph);
+}
+
+// Completes the bucketed closeness rows: out[m][k] += sum_{j<=k} bucket[m][j] for density,
+// farness and harmonic (rows 0, 1, 3).
+__global__ void bucket_prefix_kernel(const double *bucket, double *out, int K, int N) {
+    const size_t KN = (size_t)K * N;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+        const int rows[3] = {0, 1, 3};
+        for (int m = 0; m < 3; m++) {
+            double acc = 0.0;
+            for (int k = 0; k < K; k++) {
+                acc += bucket[(size_t)m * KN + (size_t)k * N + t];
+                out[(size_t)rows[m] * KN + (size_t)k * N + t] += acc;
+            }
         }
     }
 }
@@ -603,7 +675,7 @@ __device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int
         if (i == 0) { s.pr[0] = -1; s.fa[0] = 0.0f; continue; }
         const int v = s.ord[i];
         Offer off[MAXDEG];
-        const int n = gather_offers(p, s, v, i, off);
+        const int n = gather_offers(p, s, v, i, R, off, bad);
         const int q = replay_first_min(p, off, n, s.sd[i]);
         if (q < 0) { bad = true; s.pr[(size_t)i * p.P] = -1; continue; }
         s.pr[(size_t)i * p.P] = off[q].pos;
@@ -656,6 +728,7 @@ __device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int
                     bm = au;
                 } else {
                     const uint32_t a = s.aux[nb];
+                    if (a > (uint32_t)R) continue;  // cannot happen on clean scratch
                     if (a != 0u && (int)(a - 1) < i) continue;  // neighbour settled earlier
                     bm = (a != 0u) ? route_cost(s.sd[a - 1], p.speed) : __int_as_float(INF_BITS);
                 }
@@ -774,7 +847,7 @@ __device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int
 __device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, int R) {
     const int lane = lane_id();
     if (R > p.row_cap) {
-        if (lane == 0) p.t_count[qidx] = -1;
+        if (lane == 0) p.t_count[qidx] = -R;  // rows too narrow: report the reach only
         return;
     }
     bool bad = false;
@@ -783,7 +856,7 @@ __device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, in
         int pred = -1;
         if (i > 0) {
             Offer off[MAXDEG];
-            const int n = gather_offers(p, s, v, i, off);
+            const int n = gather_offers(p, s, v, i, R, off, bad);
             const int q = replay_first_min(p, off, n, s.sd[i]);
             if (q < 0) bad = true;
             else pred = s.ord[off[q].pos];
@@ -802,6 +875,7 @@ __device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, in
 // ------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) primal_kernel(const PrimalParams p) {
     __shared__ uint32_t hist_all[8][256];
+    __shared__ int cnt_all[8][2 * MAXK];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
@@ -809,6 +883,7 @@ __global__ void __launch_bounds__(256) primal_kernel(const PrimalParams p) {
     uint32_t *hist = hist_all[wib];
     const SlotPtrs s = slot_ptrs(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.P, p.L, slot, p.g.n_bound);
     long long relaxed = 0, settled = 0, done_src = 0;
+    long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     while (true) {
         unsigned long long idx = 0;
         if (lane == 0) idx = atomicAdd(p.rerun ? &p.hdr->work_next2 : &p.hdr->work_next, 1ull);
@@ -817,33 +892,48 @@ __global__ void __launch_bounds__(256) primal_kernel(const PrimalParams p) {
         if (__ldcg(&p.hdr->err) != 0u) break;
         const int li = p.remap ? p.remap[idx] : (int)idx;
         const int src = p.src_list[li];
+        long long t0 = clock64();
         const int R = warp_search(p, s, src, relaxed);
+        phase_mark(ph, 0, t0);
         if (R < 0) {
+            // Reach exceeded this slot's capacity: the reached list lost track of touched entries,
+            // so reset the slot's whole dense state, record the source for the full-capacity retry
+            // and carry on with the next source.
+            for (int j = lane; j < p.g.n_bound; j += 32) {
+                s.dist[j] = __int_as_float(INF_BITS);
+                s.aux[j] = 0u;
+            }
             if (lane == 0) {
                 const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
-                if (f < (unsigned)p.n_slots) p.failed[f] = li;
+                if (f < (unsigned)p.fail_cap) p.failed[f] = li;
+                else raise_err(p.hdr, CS_ERR_CAPACITY, 8);
             }
-            break;  // slot is dirty; the host resets it
+            __syncwarp();
+            continue;
         }
         warp_sort(s, R, hist);
         __syncwarp();
         for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
         __syncwarp();
-        if (p.mode == MODE_SHORTEST) shortest_accumulate(p, s, src, R);
+        phase_mark(ph, 1, t0);
+        if (p.mode == MODE_SHORTEST) shortest_accumulate(p, s, src, R, ph, cnt_all[wib]);
         else if (p.mode == MODE_SEGMENT) segment_accumulate(p, s, src, R);
         else tree_rows(p, s, li, R);
         __syncwarp();
+        t0 = clock64();
         for (int i = lane; i < R; i += 32) {
             const int v = s.ord[i];
             s.dist[v] = __int_as_float(INF_BITS);
             s.aux[v] = 0u;
         }
         __syncwarp();
+        phase_mark(ph, 6, t0);
         settled += R;
         done_src += 1;
     }
     const long long rsum = warp_sum_ll(relaxed);
     if (lane == 0) {
+        for (int q = 0; q < 8; q++) atomicAdd(&p.hdr->pad[q], (unsigned long long)ph[q]);
         atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
         atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
         atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
@@ -875,12 +965,14 @@ __global__ void fill_dense_kernel(char *dense, size_t dense_stride, int n_bound,
 namespace cs_host {
 thread_local std::string g_last_error;
 thread_local long long g_counters[4] = {0, 0, 0, 0};
+thread_local long long g_phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 }
 
 extern "C" void cs_set_error_internal(const char *msg) { cs_host::g_last_error = msg ? msg : ""; }
 
 namespace {
 using cs_host::g_counters;
+using cs_host::g_phase;
 
 cs_status fail(cs_status code, const std::string &msg) {
     cs_host::g_last_error = msg;
@@ -898,15 +990,22 @@ int sm_count() {
 }
 
 struct Layout {
-    size_t hdr_off, failed_off, dense_off, compact_off, compact_total, total;
+    size_t hdr_off, failed_off, bucket_off, dense_off, compact_off, compact_total, total;
     size_t dense_stride;
+    int fail_cap;
 };
+
+// sources that overflow their slot are listed for the in-call retry; beyond this many the call
+// reports CS_ERR_CAPACITY (plan a larger cap)
+int fail_capacity(int n_slots) { return std::max(n_slots, 1 << 18); }
 
 Layout layout(int n_bound, int n_slots, int cap, int P, int L) {
     Layout l;
     l.hdr_off = 0;
     l.failed_off = 256;
-    l.dense_off = cs::al256(l.failed_off + sizeof(int32_t) * (size_t)n_slots);
+    l.fail_cap = fail_capacity(n_slots);
+    l.bucket_off = cs::al256(l.failed_off + sizeof(int32_t) * (size_t)l.fail_cap);
+    l.dense_off = cs::al256(l.bucket_off + sizeof(double) * 3 * (size_t)L * (size_t)n_bound);
     l.dense_stride = cs::al256((size_t)n_bound * 4) * 2;
     l.compact_off = l.dense_off + l.dense_stride * (size_t)n_slots;
     l.compact_total = cs::compact_bytes((size_t)cap, P, L) * (size_t)n_slots;
@@ -999,9 +1098,11 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     p.maxsec = (float)maxs;
     p.delta = plan->delta_seconds > 0.0f ? plan->delta_seconds : std::max(1.0f, p.maxsec / 48.0f);
     p.out = out.out_dev;
+    p.bucket = (double *)(base + lay.bucket_off);
     p.reach = out.reach_dev;
     p.hdr = (cs::WsHeader *)(base + lay.hdr_off);
     p.failed = (int32_t *)(base + lay.failed_off);
+    p.fail_cap = lay.fail_cap;
     p.dense = base + lay.dense_off;
     p.dense_stride = lay.dense_stride;
     p.compact = base + lay.compact_off;
@@ -1018,6 +1119,11 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     if (p.n_src <= 0) return CS_OK;
     cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), stream);
     if (e != cudaSuccess) return cuda_fail(e, "workspace header reset");
+    const bool bucketed = (mode == cs::MODE_SHORTEST) && p.closeness;
+    if (bucketed) {
+        e = cudaMemsetAsync(p.bucket, 0, sizeof(double) * 3 * (size_t)K * (size_t)g->n_bound, stream);
+        if (e != cudaSuccess) return cuda_fail(e, "bucket reset");
+    }
     st = launch_primal(p, plan, plan->n_slots, stream);
     if (st != CS_OK) return st;
     cs::WsHeader h;
@@ -1029,11 +1135,9 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
                                           std::to_string(h.err_where) + ")");
     long long done = (long long)h.sources_done, rel = (long long)h.edges_relaxed, set = (long long)h.nodes_settled;
     if (h.n_failed > 0u) {
-        // Sources whose reach overflowed `cap`: reset every slot's dense scratch, then redo them at
+        // Sources whose reach overflowed `cap` (their slots already reset themselves): redo them at
         // cap = n_bound on as many slots as the compact region holds.
-        const int nf = (int)std::min<unsigned>(h.n_failed, (unsigned)plan->n_slots);
-        st = reset_dense(p.dense, p.dense_stride, g->n_bound, plan->n_slots, stream);
-        if (st != CS_OK) return st;
+        const int nf = (int)std::min<unsigned>(h.n_failed, (unsigned)lay.fail_cap);
         const size_t per = cs::compact_bytes((size_t)g->n_bound, P, plan->lanes);
         int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
         slots2 = std::max(1, std::min(slots2, nf));
@@ -1053,9 +1157,17 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
         rel = (long long)h.edges_relaxed;
         set = (long long)h.nodes_settled;
     }
+    if (bucketed) {
+        int blocks = std::max(1, std::min((g->n_bound + 255) / 256, sm_count() * 8));
+        cs::bucket_prefix_kernel<<<blocks, 256, 0, stream>>>(p.bucket, p.out, K, g->n_bound);
+        g_counters[3]++;
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "bucket_prefix_kernel launch");
+    }
     g_counters[0] = done;
     g_counters[1] = rel;
     g_counters[2] = set;
+    for (int i = 0; i < 8; i++) cs_host::g_phase[i] = (long long)h.pad[i];
     return CS_OK;
 }
 
@@ -1103,6 +1215,12 @@ size_t cs_last_error(char *buf, size_t len) {
 
 int32_t cs_device_sm_count(void) { return sm_count(); }
 
+cs_status cs_last_phase_cycles(int64_t *cycles, int32_t n) {
+    if (!cycles || n < 0) return fail(CS_ERR_ARG, "cycles is NULL");
+    for (int i = 0; i < n && i < 8; i++) cycles[i] = cs_host::g_phase[i];
+    return CS_OK;
+}
+
 cs_status cs_last_counters(int64_t *sources, int64_t *edges_relaxed, int64_t *nodes_settled, int64_t *launches) {
     if (sources) *sources = g_counters[0];
     if (edges_relaxed) *edges_relaxed = g_counters[1];
@@ -1128,7 +1246,9 @@ cs_status cs_workspace_init(const cs_plan *plan, int32_t n_bound, void *workspac
                             void *stream) {
     if (!plan || !workspace_dev) return fail(CS_ERR_ARG, "plan/workspace is NULL");
     if (workspace_bytes < plan->workspace_bytes) return fail(CS_ERR_ARG, "workspace smaller than plan");
-    Layout lay = layout(n_bound, plan->n_slots, 32, 1, 1);
+    if (plan->lanes < 1) return fail(CS_ERR_ARG, "plan has no lanes");
+    // the dense region's offset depends only on (n_bound, n_slots, lanes): same as every call
+    Layout lay = layout(n_bound, plan->n_slots, plan->cap, 1, plan->lanes);
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaMemsetAsync(workspace_dev, 0, 256, s);
     if (e != cudaSuccess) return cuda_fail(e, "workspace init");

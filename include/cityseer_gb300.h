@@ -172,7 +172,8 @@ cs_status cs_segment_centrality(const cs_primal_graph *g, const cs_query *q, con
 
 /* Replaces NetworkStructure.dijkstra_tree_shortest (rust/src/centrality.rs:1141-1200, 1500-1508)
  * for a batch of sources: per query q, visited nodes in settle order with their agg_seconds and
- * predecessor.  count_dev[q] = number visited (or -1 if it exceeds row_cap); rows are row_cap wide. */
+ * predecessor.  count_dev[q] = number visited, or minus that number when it exceeds row_cap (the
+ * rows are then not written); rows are row_cap wide. */
 cs_status cs_tree_shortest(const cs_primal_graph *g, int32_t n_queries, const int32_t *src_dev, uint32_t max_seconds,
                            float speed_m_s, const cs_plan *plan, void *workspace_dev, size_t workspace_bytes,
                            int32_t row_cap, int32_t *count_dev, int32_t *node_dev, float *agg_seconds_dev,
@@ -188,6 +189,10 @@ cs_status cs_tree_simplest(const cs_dual_graph *g, int32_t n_queries, const int3
 /* Device counters of the last call on this thread: sources done, edges relaxed, nodes settled
  * (used for throughput and roofline accounting) and the number of kernels it launched. */
 cs_status cs_last_counters(int64_t *sources, int64_t *edges_relaxed, int64_t *nodes_settled, int64_t *launches);
+
+/* Per-phase SM cycles of the last call on this thread, summed over warps: 0 search, 1 sort,
+ * 2 predecessor replay, 3 closeness, 4 sigma, 5 backward sweep, 6 scratch reset (n <= 8). */
+cs_status cs_last_phase_cycles(int64_t *cycles, int32_t n);
 
 /* Number of SMs of the current device (0 on failure). */
 int32_t cs_device_sm_count(void);

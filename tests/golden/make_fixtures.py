@@ -98,12 +98,35 @@ def centrality_golden(ref: Path) -> dict:
     return {"source": "tests/rustalgos/test_centrality.py", "local_centrality_all": gold, "dual_paths": paths}
 
 
+def helper_graphs(ref: Path) -> dict:
+    """Coordinates/edges of make_angular_plateau_graph and make_tolerance_drift_graph."""
+    tree = ast.parse((ref / "tests/rustalgos/test_centrality.py").read_text())
+    out = {}
+    for fn in tree.body:
+        if not (isinstance(fn, ast.FunctionDef) and fn.name in ("make_angular_plateau_graph",
+                                                                  "make_tolerance_drift_graph")):
+            continue
+        coords = edges = None
+        for st in ast.walk(fn):
+            if isinstance(st, ast.Assign) and isinstance(st.targets[0], ast.Name) and st.targets[0].id == "coords":
+                coords = _literal(st.value)
+            if isinstance(st, ast.For) and isinstance(st.iter, ast.List):
+                edges = _literal(st.iter)
+        out[fn.name] = {
+            "source": f"tests/rustalgos/test_centrality.py:{fn.name}",
+            "nodes": [[k, float(x), float(y)] for k, (x, y) in coords.items()],
+            "edges": [list(e) for e in edges],
+        }
+    return out
+
+
 def main(ref: Path) -> None:
     data = {
         "reference": "cityseer-api v4.24.0",
         "mock_graph": mock_graph(ref),
         "conftest": conftest_graphs(ref),
         "centrality": centrality_golden(ref),
+        "helpers": helper_graphs(ref),
     }
     (HERE / "reference_fixtures.json").write_text(json.dumps(data, indent=1))
     print("wrote", HERE / "reference_fixtures.json")
