@@ -30,6 +30,7 @@
 #include <string>
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "cs_common.cuh"
 
@@ -38,7 +39,8 @@ namespace cs {
 struct SlotPtrs {
     float *dist;
     uint32_t *aux;
-    int32_t *rl, *qa, *qb, *qf;
+    int32_t *rl;
+    uint2 *qa, *qb, *qf;  // (node, dist bits) entries, capacity 2 * cap
     uint32_t *kb;
     int32_t *vb;
     int32_t *ord;
@@ -55,7 +57,8 @@ __host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~size_t(2
 
 __host__ __device__ inline size_t compact_bytes(size_t cap, int P, int L) {
     size_t b = 0;
-    b += 7 * al256(cap * 4);      // rl qa qb qf kb vb ord
+    b += 4 * al256(cap * 4);      // rl kb vb ord
+    b += 3 * al256(cap * 16);     // qa qb qf: 2 * cap entries of 8 bytes
     b += al256(cap * 4);          // sd
     b += al256(cap * 8);          // sig
     b += al256(cap);              // np
@@ -74,9 +77,9 @@ __host__ __device__ inline SlotPtrs slot_ptrs(char *dense, size_t dense_stride, 
     char *c = compact + compact_bytes(cap, P, L) * (size_t)slot;
     size_t o = 0;
     s.rl = (int32_t *)(c + o); o += al256(cap * 4);
-    s.qa = (int32_t *)(c + o); o += al256(cap * 4);
-    s.qb = (int32_t *)(c + o); o += al256(cap * 4);
-    s.qf = (int32_t *)(c + o); o += al256(cap * 4);
+    s.qa = (uint2 *)(c + o); o += al256(cap * 16);
+    s.qb = (uint2 *)(c + o); o += al256(cap * 16);
+    s.qf = (uint2 *)(c + o); o += al256(cap * 16);
     s.kb = (uint32_t *)(c + o); o += al256(cap * 4);
     s.vb = (int32_t *)(c + o); o += al256(cap * 4);
     s.ord = (int32_t *)(c + o); o += al256(cap * 4);
@@ -128,25 +131,50 @@ struct PrimalParams {
 
 // ------------------------------------------------------------------------------------------
 // 1. Banded label-correcting search.  Returns R (reached count incl. source) or -1 on overflow.
+//    Queues hold (node, distance-at-push) entries with lazy deletion: an entry is live only while
+//    its distance still equals the node's, so no flag atomics are needed to de-duplicate.
 // ------------------------------------------------------------------------------------------
+constexpr int DEG_FAST = 8;  // edges per node loaded together; higher degrees loop
+
+__device__ __forceinline__ void push_entries(bool first, int route, int v, float c, int &R, int &nnext, int &nfar,
+                                             int cap, int qcap, const SlotPtrs &s, uint2 *nxt, unsigned lt) {
+    const unsigned mf = __ballot_sync(FULL, first);
+    const unsigned mn = __ballot_sync(FULL, route == 1);
+    const unsigned mr = __ballot_sync(FULL, route == 2);
+    if (first) {
+        const int q = R + __popc(mf & lt);
+        if (q < cap) s.rl[q] = v;
+    }
+    if (route == 1) {
+        const int q = nnext + __popc(mn & lt);
+        if (q < qcap) nxt[q] = make_uint2((unsigned)v, __float_as_uint(c));
+    }
+    if (route == 2) {
+        const int q = nfar + __popc(mr & lt);
+        if (q < qcap) s.qf[q] = make_uint2((unsigned)v, __float_as_uint(c));
+    }
+    R += __popc(mf);
+    nnext += __popc(mn);
+    nfar += __popc(mr);
+}
+
 __device__ int warp_search(const PrimalParams &p, const SlotPtrs &s, int src, long long &relaxed) {
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
     const int cap = p.cap;
+    const int qcap = 2 * cap;
     const int32_t *__restrict__ in_ptr = p.g.in_ptr_dev;
     const int32_t *__restrict__ in_nb = p.g.in_nb_dev;
     const float *__restrict__ in_w = p.g.in_w_dev;
     float *dist = s.dist;
-    uint32_t *aux = s.aux;
     if (lane == 0) {
         dist[src] = 0.0f;
         s.rl[0] = src;
-        s.qa[0] = src;
-        aux[src] = NEAR_BIT;
+        s.qa[0] = make_uint2((unsigned)src, 0u);
     }
     __syncwarp();
     int R = 1, nnear = 1, nfar = 0;
-    int32_t *cur = s.qa, *nxt = s.qb;
+    uint2 *cur = s.qa, *nxt = s.qb;
     float T = p.delta;
     bool overflow = false;
     while (true) {
@@ -154,71 +182,72 @@ __device__ int warp_search(const PrimalParams &p, const SlotPtrs &s, int src, lo
             int nnext = 0;
             for (int base = 0; base < nnear; base += 32) {
                 const int i = base + lane;
-                const bool act = i < nnear;
-                const int u = act ? cur[i] : 0;
-                if (act) atomicAnd(&aux[u], ~NEAR_BIT);
-                __syncwarp();
-                const float du = act ? __ldcg(&dist[u]) : 0.0f;
-                const int beg = act ? __ldg(&in_ptr[u]) : 0;
-                const int end = act ? __ldg(&in_ptr[u + 1]) : 0;
-                relaxed += end - beg;
-                const int maxdeg = warp_max_i(end - beg);
-                for (int j = 0; j < maxdeg; j++) {
-                    const int e = beg + j;
-                    int v = 0;
-                    bool first = false;
-                    int route = 0;
-                    if (e < end) {
-                        v = __ldg(&in_nb[e]);
-                        if (v != u) {
-                            const float c = fadd(du, __ldg(&in_w[e]));
-                            if (c <= p.maxsec) {
-                                const int old = atomicMin((int *)&dist[v], __float_as_int(c));
-                                if (__float_as_int(c) < old) {
-                                    first = (old == INF_BITS);
-                                    if (c < T) {
-                                        const uint32_t o = atomicOr(&aux[v], NEAR_BIT);
-                                        route = (o & NEAR_BIT) ? 0 : 1;
-                                    } else {
-                                        const uint32_t o = atomicOr(&aux[v], FAR_BIT);
-                                        route = (o & FAR_BIT) ? 0 : 2;
-                                    }
-                                }
-                            }
+                uint2 ent = make_uint2(0u, 0u);
+                if (i < nnear) ent = cur[i];
+                const int u = (int)ent.x;
+                const float du = (i < nnear) ? __ldcg(&dist[u]) : 0.0f;
+                const bool live = (i < nnear) && (__float_as_uint(du) == ent.y);
+                const int beg = live ? __ldg(&in_ptr[u]) : 0;
+                const int deg = live ? __ldg(&in_ptr[u + 1]) - beg : 0;
+                relaxed += deg;
+                // load this node's first DEG_FAST edges together, then issue their atomics together
+                int vv[DEG_FAST];
+                float cc[DEG_FAST];
+                int old[DEG_FAST];
+#pragma unroll
+                for (int j = 0; j < DEG_FAST; j++) {
+                    vv[j] = u;
+                    cc[j] = 0.0f;
+                    if (j < deg) {
+                        vv[j] = __ldg(&in_nb[beg + j]);
+                        cc[j] = fadd(du, __ldg(&in_w[beg + j]));
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < DEG_FAST; j++) {
+                    old[j] = 0;
+                    if (j < deg && vv[j] != u && cc[j] <= p.maxsec)
+                        old[j] = atomicMin((int *)&dist[vv[j]], __float_as_int(cc[j]));
+                }
+                const int maxdeg = warp_max_i(deg);
+#pragma unroll
+                for (int j = 0; j < DEG_FAST; j++) {
+                    if (j >= maxdeg) break;
+                    const bool imp = (j < deg) && vv[j] != u && cc[j] <= p.maxsec && __float_as_int(cc[j]) < old[j];
+                    const int route = imp ? (cc[j] < T ? 1 : 2) : 0;
+                    push_entries(imp && old[j] == INF_BITS, route, vv[j], cc[j], R, nnext, nfar, cap, qcap, s, nxt,
+                                 lt);
+                }
+                // rare high-degree nodes: remaining edges one at a time
+                for (int j = DEG_FAST; j < maxdeg; j++) {
+                    int v = u;
+                    float c = 0.0f;
+                    bool imp = false, first = false;
+                    if (j < deg) {
+                        v = __ldg(&in_nb[beg + j]);
+                        c = fadd(du, __ldg(&in_w[beg + j]));
+                        if (v != u && c <= p.maxsec) {
+                            const int o = atomicMin((int *)&dist[v], __float_as_int(c));
+                            imp = __float_as_int(c) < o;
+                            first = imp && o == INF_BITS;
                         }
                     }
-                    const unsigned mf = __ballot_sync(FULL, first);
-                    const unsigned mn = __ballot_sync(FULL, route == 1);
-                    const unsigned mr = __ballot_sync(FULL, route == 2);
-                    if (first) {
-                        const int q = R + __popc(mf & lt);
-                        if (q < cap) s.rl[q] = v;
-                    }
-                    if (route == 1) {
-                        const int q = nnext + __popc(mn & lt);
-                        if (q < cap) nxt[q] = v;
-                    }
-                    if (route == 2) {
-                        const int q = nfar + __popc(mr & lt);
-                        if (q < cap) s.qf[q] = v;
-                    }
-                    R += __popc(mf);
-                    nnext += __popc(mn);
-                    nfar += __popc(mr);
+                    push_entries(first, imp ? (c < T ? 1 : 2) : 0, v, c, R, nnext, nfar, cap, qcap, s, nxt, lt);
                 }
             }
             __syncwarp();
-            if (R > cap || nnext > cap || nfar > cap) { overflow = true; break; }
-            int32_t *t = cur; cur = nxt; nxt = t;
+            if (R > cap || nnext > qcap || nfar > qcap) { overflow = true; break; }
+            uint2 *t = cur; cur = nxt; nxt = t;
             nnear = nnext;
         }
         if (overflow) break;
         if (nfar == 0) break;
-        // Next band starts at the smallest pending distance.
+        // Next band starts at the smallest live pending distance.
         float mn = __int_as_float(INF_BITS);
         for (int i = lane; i < nfar; i += 32) {
-            const float d = __ldcg(&dist[s.qf[i]]);
-            if (d >= T) mn = fminf(mn, d);
+            const uint2 ent = s.qf[i];
+            const float d = __ldcg(&dist[ent.x]);
+            if (__float_as_uint(d) == ent.y) mn = fminf(mn, d);
         }
         mn = warp_min_f(mn);
         const float Told = T;
@@ -229,21 +258,16 @@ __device__ int warp_search(const PrimalParams &p, const SlotPtrs &s, int src, lo
         for (int base = 0; base < nfar; base += 32) {
             const int i = base + lane;
             const bool act = i < nfar;
-            const int v = act ? s.qf[i] : 0;
-            const float d = act ? __ldcg(&dist[v]) : 0.0f;
-            const bool drop = act && d < Told;
-            bool tonear = act && !drop && d < T;
-            const bool keep = act && !drop && !tonear;
-            if (drop || tonear) atomicAnd(&aux[v], ~FAR_BIT);
-            if (tonear) {
-                const uint32_t o = atomicOr(&aux[v], NEAR_BIT);
-                tonear = !(o & NEAR_BIT);
-            }
+            const uint2 ent = act ? s.qf[i] : make_uint2(0u, 0u);
+            const float d = act ? __ldcg(&dist[ent.x]) : 0.0f;
+            const bool live = act && __float_as_uint(d) == ent.y;
+            const bool tonear = live && d < T;
+            const bool keep = live && !tonear;
             const unsigned mt = __ballot_sync(FULL, tonear);
             const unsigned mk = __ballot_sync(FULL, keep);
             __syncwarp();
-            if (tonear) cur[nn + __popc(mt & lt)] = v;
-            if (keep) s.qf[nf2 + __popc(mk & lt)] = v;
+            if (tonear) cur[nn + __popc(mt & lt)] = ent;
+            if (keep) s.qf[nf2 + __popc(mk & lt)] = ent;
             nn += __popc(mt);
             nf2 += __popc(mk);
             __syncwarp();
@@ -252,10 +276,7 @@ __device__ int warp_search(const PrimalParams &p, const SlotPtrs &s, int src, lo
         nfar = nf2;
     }
     __syncwarp();
-    if (overflow) {
-        // Leave the slot dirty: the caller resets the whole slot before reuse.
-        return -1;
-    }
+    if (overflow) return -1;  // the slot's dense state is dirty: the caller resets it
     return R;
 }
 
@@ -274,6 +295,7 @@ __device__ void warp_sort(const SlotPtrs &s, int R, uint32_t *hist) {
         const int32_t *vin = (pass == 0) ? s.rl : ((pass & 1) ? s.vb : s.ord);
         uint32_t *kout = (pass & 1) ? (uint32_t *)s.sd : s.kb;
         int32_t *vout = (pass & 1) ? s.ord : s.vb;
+#pragma unroll 4
         for (int i = lane; i < R; i += 32) {
             const uint32_t key = (pass == 0) ? (uint32_t)__float_as_int(__ldcg(&s.dist[vin[i]])) : kin[i];
             atomicAdd(&hist[(key >> shift) & 255u], 1u);
@@ -295,14 +317,22 @@ __device__ void warp_sort(const SlotPtrs &s, int R, uint32_t *hist) {
 #pragma unroll
         for (int q = 0; q < 8; q++) { hist[lane * 8 + q] = run; run += loc[q]; }
         __syncwarp();
+        // software-pipelined: the next chunk's key/value loads are in flight while this one scatters
+        int32_t val_n = 0;
+        uint32_t key_n = 0;
+        if (lane < R) {
+            val_n = vin[lane];
+            key_n = (pass == 0) ? (uint32_t)__float_as_int(__ldcg(&s.dist[val_n])) : kin[lane];
+        }
         for (int base = 0; base < R; base += 32) {
             const int i = base + lane;
             const bool act = i < R;
-            uint32_t key = 0;
-            int32_t val = 0;
-            if (act) {
-                val = vin[i];
-                key = (pass == 0) ? (uint32_t)__float_as_int(__ldcg(&s.dist[val])) : kin[i];
+            const uint32_t key = key_n;
+            const int32_t val = val_n;
+            const int inext = i + 32;
+            if (inext < R) {
+                val_n = vin[inext];
+                key_n = (pass == 0) ? (uint32_t)__float_as_int(__ldcg(&s.dist[val_n])) : kin[inext];
             }
             const uint32_t dg = act ? ((key >> shift) & 255u) : (256u + (uint32_t)lane);
             const unsigned peers = __match_any_sync(FULL, dg);
@@ -323,94 +353,145 @@ __device__ void warp_sort(const SlotPtrs &s, int R, uint32_t *hist) {
 }
 
 // ------------------------------------------------------------------------------------------
-// 3. Offer replay for the node at sorted position i.
+// 3. Offer replay for the node at sorted position i.  Everything per node stays in registers:
+//    the kernel is instantiated for a maximum out-degree PM (8 for street graphs, 32 otherwise)
+//    and all per-edge arrays are fixed-size and fully unrolled.
 // ------------------------------------------------------------------------------------------
-struct Offer {
-    int pos;
-    float c;
-    int e;
+__device__ __forceinline__ float route_cost(float secs, float speed) { return fmul(secs, speed); }
+
+// Reached out-neighbours of v: slot j holds out-CSR edge beg + j (pos -1: unreached or self loop).
+template <int PM>
+struct Nb {
+    int pos[PM];
+    float d[PM];
+    int beg, deg;
 };
 
-// Gathers the candidate offers to v (out-edges v->u with u settled before v), stably sorted by
-// the offering node's settle position.  Returns the count.
-__device__ __forceinline__ int gather_offers(const PrimalParams &p, const SlotPtrs &s, int v, int i, int R, Offer *off,
-                                             bool &bad) {
-    const int beg = __ldg(&p.g.out_ptr_dev[v]);
-    const int end = __ldg(&p.g.out_ptr_dev[v + 1]);
-    int n = 0;
-    for (int e = beg; e < end && n < MAXDEG; e++) {
-        const int u = __ldg(&p.g.out_to_dev[e]);
-        if (u == v) continue;
-        const uint32_t a = s.aux[u];
-        if (a == 0u) continue;
-        if (a > (uint32_t)R) { bad = true; continue; }
-        const int pu = (int)a - 1;
-        if (pu >= i) continue;
-        const float c = fadd(s.sd[pu], __ldg(&p.g.out_w_dev[e]));
-        // insertion keeping stability on equal positions (parallel edges keep list order)
-        int q = n;
-        while (q > 0 && off[q - 1].pos > pu) { off[q] = off[q - 1]; q--; }
-        off[q].pos = pu;
-        off[q].c = c;
-        off[q].e = e;
-        n++;
+template <int PM>
+__device__ __forceinline__ void load_nb(const PrimalParams &p, const SlotPtrs &s, int v, int R, Nb<PM> &nb,
+                                        bool &bad) {
+    nb.beg = __ldg(&p.g.out_ptr_dev[v]);
+    nb.deg = min(__ldg(&p.g.out_ptr_dev[v + 1]) - nb.beg, PM);
+    int uu[PM];
+    uint32_t aa[PM];
+#pragma unroll
+    for (int j = 0; j < PM; j++) uu[j] = (j < nb.deg) ? __ldg(&p.g.out_to_dev[nb.beg + j]) : v;
+#pragma unroll
+    for (int j = 0; j < PM; j++) aa[j] = (uu[j] != v) ? s.aux[uu[j]] : 0u;
+#pragma unroll
+    for (int j = 0; j < PM; j++) {
+        const bool ok = aa[j] != 0u && aa[j] <= (uint32_t)R;
+        if (aa[j] > (uint32_t)R) bad = true;  // scratch not clean: refuse to index
+        nb.pos[j] = ok ? (int)aa[j] - 1 : -1;
+        nb.d[j] = ok ? s.sd[aa[j] - 1] : 0.0f;
     }
-    return n;
 }
 
-// Phase-1 (+ Phase-2) predecessor replay, rust/src/centrality.rs:1413-1437 and 1444-1483.
-// Returns the number of predecessors written to preds[], or -1 if the replayed distance does not
-// reproduce the searched one (internal inconsistency).
-__device__ __forceinline__ int replay_brandes(const PrimalParams &p, const Offer *off, int n, float dv, int *preds) {
-    const float one_plus = 1.0f + TIE_EPSILON;
-    const float one_minus = 1.0f - TIE_EPSILON;
-    float cur = __int_as_float(INF_BITS);
-    int np = 0;
-    for (int q = 0; q < n; q++) {
-        const float c = off[q].c;
-        if (c > p.maxsec) continue;
-        const bool improved = c < cur;
-        const bool tied = c <= fmul(cur, one_plus);
-        if (improved) {
-            if (c < fmul(cur, one_minus)) np = 0;
-            preds[np++] = off[q].pos;
-            cur = c;
-        } else if (tied) {
-            bool has = false;
-            for (int r = 0; r < np; r++) has |= (preds[r] == off[q].pos);
-            if (!has) preds[np++] = off[q].pos;
-        }
+// Offers to the node at position i are the reached neighbours settled before it, taken in order of
+// the offering node's position (parallel edges keep list order).  Candidate seconds per slot:
+template <int PM>
+__device__ __forceinline__ unsigned offer_cands(const PrimalParams &p, const Nb<PM> &nb, int i, float *c) {
+    unsigned todo = 0;
+#pragma unroll
+    for (int j = 0; j < PM; j++) {
+        const bool off = nb.pos[j] >= 0 && nb.pos[j] < i;
+        c[j] = off ? fadd(nb.d[j], __ldg(&p.g.out_w_dev[nb.beg + j])) : 0.0f;
+        if (off) todo |= 1u << j;
     }
-    if (__float_as_int(cur) != __float_as_int(dv)) return -1;
-    if (p.tol > TIE_EPSILON) {
-        const float lim = fmul(dv, 1.0f + p.tol);
-        np = 0;
-        for (int q = 0; q < n; q++) {
-            if (off[q].c <= lim) {
-                bool has = false;
-                for (int r = 0; r < np; r++) has |= (preds[r] == off[q].pos);
-                if (!has) preds[np++] = off[q].pos;
-            }
-        }
-    }
-    return np;
+    return todo;
 }
 
-// Strict-< single predecessor (dijkstra_tree_* / dijkstra_tree_segment): the first offer, in
-// settle order, that reaches the final distance.  Returns the offer index or -1.
-__device__ __forceinline__ int replay_first_min(const PrimalParams &p, const Offer *off, int n, float dv) {
-    float cur = __int_as_float(INF_BITS);
+// next offer in settle order: lowest position, then lowest slot
+template <int PM>
+__device__ __forceinline__ int next_offer(const Nb<PM> &nb, unsigned todo, const float *c, int &bp, float &bc) {
     int best = -1;
-    for (int q = 0; q < n; q++) {
-        const float c = off[q].c;
-        if (c > p.maxsec) continue;
-        if (c < cur) { cur = c; best = q; }
+    bp = 0x7fffffff;
+    bc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < PM; j++) {
+        if (((todo >> j) & 1u) && nb.pos[j] < bp) {
+            bp = nb.pos[j];
+            best = j;
+            bc = c[j];
+        }
     }
-    if (__float_as_int(cur) != __float_as_int(dv)) return -2;
     return best;
 }
 
-__device__ __forceinline__ float route_cost(float secs, float speed) { return fmul(secs, speed); }
+template <int PM>
+__device__ __forceinline__ bool pos_in(const Nb<PM> &nb, unsigned mask, int pos) {
+    bool has = false;
+#pragma unroll
+    for (int j = 0; j < PM; j++) has |= ((mask >> j) & 1u) && nb.pos[j] == pos;
+    return has;
+}
+
+// Phase-1 (+ Phase-2) predecessor replay, rust/src/centrality.rs:1413-1437 and 1444-1483.
+// Returns the predecessor slots as a bit mask; ok = false if the replayed distance does not
+// reproduce the searched one (internal inconsistency).
+template <int PM>
+__device__ __forceinline__ unsigned replay_brandes(const PrimalParams &p, const Nb<PM> &nb, int i, float dv,
+                                                   bool &ok) {
+    const float one_plus = 1.0f + TIE_EPSILON;
+    const float one_minus = 1.0f - TIE_EPSILON;
+    float c[PM];
+    const unsigned todo = offer_cands<PM>(p, nb, i, c);
+    unsigned t = todo, pm = 0u;
+    float cur = __int_as_float(INF_BITS);
+    while (t) {
+        int bp;
+        float bc;
+        const int best = next_offer<PM>(nb, t, c, bp, bc);
+        t &= ~(1u << best);
+        if (bc > p.maxsec) continue;
+        const bool improved = bc < cur;
+        const bool tied = bc <= fmul(cur, one_plus);
+        if (improved) {
+            if (bc < fmul(cur, one_minus)) pm = 0u;
+            pm |= 1u << best;
+            cur = bc;
+        } else if (tied && !pos_in<PM>(nb, pm, bp)) {
+            pm |= 1u << best;
+        }
+    }
+    ok = __float_as_int(cur) == __float_as_int(dv);
+    if (p.tol > TIE_EPSILON) {
+        const float lim = fmul(dv, 1.0f + p.tol);
+        pm = 0u;
+        t = todo;
+        while (t) {
+            int bp;
+            float bc;
+            const int best = next_offer<PM>(nb, t, c, bp, bc);
+            t &= ~(1u << best);
+            if (bc <= lim && !pos_in<PM>(nb, pm, bp)) pm |= 1u << best;
+        }
+    }
+    return pm;
+}
+
+// Strict-< single predecessor (dijkstra_tree_* / dijkstra_tree_segment): the first offer in settle
+// order that reaches the final distance.  Returns its slot or -1; ok as above.
+template <int PM>
+__device__ __forceinline__ int replay_first_min(const PrimalParams &p, const Nb<PM> &nb, int i, float dv, bool &ok) {
+    float c[PM];
+    unsigned t = offer_cands<PM>(p, nb, i, c);
+    float cur = __int_as_float(INF_BITS);
+    int pick = -1;
+    while (t) {
+        int bp;
+        float bc;
+        const int best = next_offer<PM>(nb, t, c, bp, bc);
+        t &= ~(1u << best);
+        if (bc > p.maxsec) continue;
+        if (bc < cur) {
+            cur = bc;
+            pick = best;
+        }
+    }
+    ok = __float_as_int(cur) == __float_as_int(dv);
+    return pick;
+}
 
 // ------------------------------------------------------------------------------------------
 // 4a. Shortest-path centrality for one source (after search and sort).
@@ -439,6 +520,16 @@ __device__ __forceinline__ int first_k(const PrimalParams &p, float c) {
     return k;
 }
 
+// predecessor positions of the node at position i, in registers
+template <int PM>
+__device__ __forceinline__ int load_preds(const SlotPtrs &s, int i, int P, int *pl) {
+    const int np = s.np[i];
+#pragma unroll
+    for (int r = 0; r < PM; r++) pl[r] = (r < np) ? s.pr[(size_t)i * P + r] : 0;
+    return np;
+}
+
+template <int PM>
 __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R, long long *ph,
                                     int *cnt) {
     const int lane = lane_id();
@@ -459,40 +550,27 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
         const float cv = route_cost(dv, p.speed);
         const int k0v = first_k(p, cv);
         if (k0v < K) atomicAdd(&cnt[k0v], 1);
-        const int beg = __ldg(&p.g.out_ptr_dev[v]);
-        const int end = __ldg(&p.g.out_ptr_dev[v + 1]);
-        Offer off[MAXDEG];
-        int n = 0;
-        for (int e = beg; e < end; e++) {
-            const int u = __ldg(&p.g.out_to_dev[e]);
-            if (u == v) continue;
-            const uint32_t a = s.aux[u];
-            if (a == 0u) continue;
-            if (a > (uint32_t)R) { bad = true; continue; }  // scratch not clean: refuse to index
-            const int pu = (int)a - 1;
-            const float du = s.sd[pu];
-            if (p.closeness && __ldg(&p.g.out_cnt_dev[e])) {
-                const float ec = fmaxf(cv, route_cost(du, p.speed));
+        Nb<PM> nb;
+        load_nb<PM>(p, s, v, R, nb, bad);
+        if (p.closeness) {
+#pragma unroll
+            for (int j = 0; j < PM; j++) {
+                if (nb.pos[j] < 0 || !__ldg(&p.g.out_cnt_dev[nb.beg + j])) continue;
+                const float ec = fmaxf(cv, route_cost(nb.d[j], p.speed));
                 const int k0e = first_k(p, ec);
                 if (k0e < K) atomicAdd(&cnt[MAXK + k0e], 1);
-            }
-            if (p.betweenness && pu < i && n < MAXDEG) {
-                const float c = fadd(du, __ldg(&p.g.out_w_dev[e]));
-                int q = n;
-                while (q > 0 && off[q - 1].pos > pu) { off[q] = off[q - 1]; q--; }
-                off[q].pos = pu;
-                off[q].c = c;
-                off[q].e = e;
-                n++;
             }
         }
         if (!p.betweenness) continue;
         if (i == 0) { s.np[0] = 0; continue; }
-        int preds[MAXDEG];
-        const int np = replay_brandes(p, off, n, dv, preds);
-        if (np < 0 || np > P) { bad = true; s.np[i] = 0; continue; }
-        s.np[i] = (uint8_t)np;
-        for (int r = 0; r < np; r++) s.pr[(size_t)i * P + r] = preds[r];
+        bool ok = true;
+        const unsigned pm = replay_brandes<PM>(p, nb, i, dv, ok);
+        if (!ok) { bad = true; s.np[i] = 0; continue; }
+        int r = 0;
+#pragma unroll
+        for (int j = 0; j < PM; j++)
+            if ((pm >> j) & 1u) s.pr[(size_t)i * P + r++] = nb.pos[j];
+        s.np[i] = (uint8_t)r;
     }
     if (__any_sync(FULL, bad)) {
         if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 1);
@@ -525,7 +603,9 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
             atomicAdd(bk, wt_d);
             atomicAdd(bk + KN, f2d(fmul(c, wt)));
             atomicAdd(bk + 2 * KN, f2d(fmul(__fdiv_rn(1.0f, c), wt)));
-            for (int k = k0; k < K; k++) {
+#pragma unroll
+            for (int k = 0; k < MAXK; k++) {
+                if (k < k0 || k >= K) continue;
                 double *row = p.out + (size_t)k * N + t;
                 atomicAdd(row + 2 * KN, f2d(rankw[k]));
                 atomicAdd(row + 4 * KN, f2d(fmul(expf(fmul(-p.beta[k], c)), wt)));
@@ -539,25 +619,22 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
     for (int base = 0; base < R; base += 32) {
         const int i = base + lane;
         const bool act = i < R;
-        int np = act ? s.np[i] : 0;
+        int pl[PM];
+        const int np = act ? load_preds<PM>(s, i, P, pl) : 0;
         unsigned pm = 0;
-        int pl[MAXDEG];
-        for (int r = 0; r < np; r++) {
-            pl[r] = s.pr[(size_t)i * P + r];
-            if (pl[r] >= base) pm |= 1u << (pl[r] - base);
-        }
+#pragma unroll
+        for (int r = 0; r < PM; r++)
+            if (r < np && pl[r] >= base) pm |= 1u << (pl[r] - base);
         unsigned done = __ballot_sync(FULL, !act);
         bool mine = !act;
         int guard = 0;
         while (done != FULL) {
             const bool ready = !mine && ((pm & ~done) == 0u);
             if (ready) {
-                float sg;
-                if (i == 0) sg = 1.0f;
-                else {
-                    sg = 0.0f;
-                    for (int r = 0; r < np; r++) sg = fadd(sg, sig[pl[r]]);
-                }
+                float sg = (i == 0) ? 1.0f : 0.0f;
+#pragma unroll
+                for (int r = 0; r < PM; r++)
+                    if (r < np) sg = fadd(sg, sig[pl[r]]);
                 sig[i] = sg;
                 mine = true;
             }
@@ -586,13 +663,12 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
         const int base = ch * 32;
         const int i = base + lane;
         const bool act = i < R;
-        const int np = act ? s.np[i] : 0;
+        int pl[PM];
+        const int np = act ? load_preds<PM>(s, i, P, pl) : 0;
         unsigned pm = 0;
-        int pl[MAXDEG];
-        for (int r = 0; r < np; r++) {
-            pl[r] = s.pr[(size_t)i * P + r];
-            if (pl[r] >= base) pm |= 1u << (pl[r] - base);
-        }
+#pragma unroll
+        for (int r = 0; r < PM; r++)
+            if (r < np && pl[r] >= base) pm |= 1u << (pl[r] - base);
         bool mine = !act;
         unsigned done = __ballot_sync(FULL, mine);
         int guard = 0;
@@ -604,10 +680,14 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
                 const float cost = route_cost(s.sd[i], p.speed);
                 const float sw = sig[i];
                 const float pair = __ldg(&p.eligible[v]) ? 0.5f : 1.0f;
-                float fr[MAXDEG];
-                for (int r = 0; r < np; r++) {
-                    const float sv = sig[pl[r]];
-                    fr[r] = (sv == sw) ? 1.0f : __fdiv_rn(sv, sw);
+                float fr[PM];
+#pragma unroll
+                for (int r = 0; r < PM; r++) {
+                    fr[r] = 0.0f;
+                    if (r < np) {
+                        const float sv = sig[pl[r]];
+                        fr[r] = (sv == sw) ? 1.0f : __fdiv_rn(sv, sw);
+                    }
                 }
                 float *dli = dl + (size_t)i * L;
                 const int k0 = first_k(p, cost);
@@ -618,8 +698,9 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
                     const float dep = fadd(seed, __ldcg(&dli[k]));
                     const float depb = fadd(seedb, __ldcg(&dli[K + k]));
                     if (dep == 0.0f && depb == 0.0f) continue;
-                    for (int r = 0; r < np; r++) {
-                        if (fr[r] == 0.0f) continue;
+#pragma unroll
+                    for (int r = 0; r < PM; r++) {
+                        if (r >= np || fr[r] == 0.0f) continue;
                         float *pd = dl + (size_t)pl[r] * L;
                         atomicAdd(&pd[k], fmul(fr[r], dep));
                         atomicAdd(&pd[K + k], fmul(fr[r], depb));
@@ -665,6 +746,7 @@ __global__ void bucket_prefix_kernel(const double *bucket, double *out, int K, i
 // ------------------------------------------------------------------------------------------
 // 4b. Segment centrality for one source.
 // ------------------------------------------------------------------------------------------
+template <int PM>
 __device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R) {
     const int lane = lane_id();
     const int K = p.k;
@@ -674,12 +756,18 @@ __device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int
     for (int i = lane; i < R; i += 32) {
         if (i == 0) { s.pr[0] = -1; s.fa[0] = 0.0f; continue; }
         const int v = s.ord[i];
-        Offer off[MAXDEG];
-        const int n = gather_offers(p, s, v, i, R, off, bad);
-        const int q = replay_first_min(p, off, n, s.sd[i]);
-        if (q < 0) { bad = true; s.pr[(size_t)i * p.P] = -1; continue; }
-        s.pr[(size_t)i * p.P] = off[q].pos;
-        s.fa[i] = __ldg(&p.g.out_seglen_dev[off[q].e]);  // last segment length
+        Nb<PM> nb;
+        load_nb<PM>(p, s, v, R, nb, bad);
+        bool ok = true;
+        const int q = replay_first_min<PM>(p, nb, i, s.sd[i], ok);
+        if (!ok || q < 0) { bad = true; s.pr[(size_t)i * p.P] = -1; continue; }
+        int pos = 0;
+        float last = 0.0f;
+#pragma unroll
+        for (int j = 0; j < PM; j++)
+            if (j == q) { pos = nb.pos[j]; last = __ldg(&p.g.out_seglen_dev[nb.beg + j]); }
+        s.pr[(size_t)i * p.P] = pos;
+        s.fa[i] = last;  // last segment length
     }
     if (__any_sync(FULL, bad)) {
         if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 4);
@@ -739,7 +827,9 @@ __device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int
                 const float imp = __ldg(&p.g.in_segimp_dev[e]);
                 const float C = __fdiv_rn(fadd(fadd(elen, A), B), 2.0f), D = C;
                 const float Ci = fadd(Ai, fmul(__fadd_rn(C, -A), imp)), Di = Ci;
-                for (int k = K - 1; k >= 0; k--) {
+#pragma unroll
+                for (int k = MAXK - 1; k >= 0; k--) {
+                    if (k >= K) continue;
                     const float df = p.dk[k];
                     const float beta = p.beta[k], nbeta = -beta;
                     const float inb = (beta != 0.0f) ? __fdiv_rn(1.0f, nbeta) : 0.0f;
@@ -844,6 +934,7 @@ __device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int
 // ------------------------------------------------------------------------------------------
 // 4c. Shortest-path tree rows (isochrone query).
 // ------------------------------------------------------------------------------------------
+template <int PM>
 __device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, int R) {
     const int lane = lane_id();
     if (R > p.row_cap) {
@@ -855,11 +946,16 @@ __device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, in
         const int v = s.ord[i];
         int pred = -1;
         if (i > 0) {
-            Offer off[MAXDEG];
-            const int n = gather_offers(p, s, v, i, R, off, bad);
-            const int q = replay_first_min(p, off, n, s.sd[i]);
-            if (q < 0) bad = true;
-            else pred = s.ord[off[q].pos];
+            Nb<PM> nb;
+            load_nb<PM>(p, s, v, R, nb, bad);
+            bool ok = true;
+            const int q = replay_first_min<PM>(p, nb, i, s.sd[i], ok);
+            if (!ok || q < 0) bad = true;
+            else {
+#pragma unroll
+                for (int j = 0; j < PM; j++)
+                    if (j == q) pred = s.ord[nb.pos[j]];
+            }
         }
         const size_t o = (size_t)qidx * p.row_cap + i;
         p.t_node[o] = v;
@@ -873,7 +969,8 @@ __device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, in
 // ------------------------------------------------------------------------------------------
 // Persistent kernel: each warp owns one scratch slot and pulls sources until the list is empty.
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) primal_kernel(const PrimalParams p) {
+template <int PM, int MINB>
+__global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][2 * MAXK];
     const int lane = lane_id();
@@ -916,9 +1013,9 @@ __global__ void __launch_bounds__(256) primal_kernel(const PrimalParams p) {
         for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
         __syncwarp();
         phase_mark(ph, 1, t0);
-        if (p.mode == MODE_SHORTEST) shortest_accumulate(p, s, src, R, ph, cnt_all[wib]);
-        else if (p.mode == MODE_SEGMENT) segment_accumulate(p, s, src, R);
-        else tree_rows(p, s, li, R);
+        if (p.mode == MODE_SHORTEST) shortest_accumulate<PM>(p, s, src, R, ph, cnt_all[wib]);
+        else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
+        else tree_rows<PM>(p, s, li, R);
         __syncwarp();
         t0 = clock64();
         for (int i = lane; i < R; i += 32) {
@@ -1025,12 +1122,31 @@ cs_status validate_primal(const cs_primal_graph *g) {
     return CS_OK;
 }
 
+// register budget of the P <= 8 kernel: 3 (default, 80 registers) or 2 (128 registers) resident
+// 256-thread blocks per SM; CS_MIN_BLOCKS_PER_SM=2 selects the larger budget
+int min_blocks_variant() {
+    const char *e = getenv("CS_MIN_BLOCKS_PER_SM");
+    return (e && e[0] == '2') ? 2 : 3;
+}
+
+cudaError_t occupancy_blocks(int P, int *bpsm) {
+    if (P > 8) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<CS_MAX_DEGREE, 2>, 256, 0);
+    if (min_blocks_variant() == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 3>, 256, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 2>, 256, 0);
+}
+
 cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, cudaStream_t stream) {
     const int tpb = 256;
     const int wpb = tpb / 32;
     const int blocks = (n_slots + wpb - 1) / wpb;
     p.n_slots = n_slots;
-    cs::primal_kernel<<<blocks, tpb, 0, stream>>>(p);
+    const int minb = min_blocks_variant();
+    if (p.g.max_out_degree <= 8) {
+        if (minb == 3) cs::primal_kernel<8, 3><<<blocks, tpb, 0, stream>>>(p);
+        else cs::primal_kernel<8, 2><<<blocks, tpb, 0, stream>>>(p);
+    } else {
+        cs::primal_kernel<CS_MAX_DEGREE, 2><<<blocks, tpb, 0, stream>>>(p);
+    }
     g_counters[3]++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "primal_kernel launch");
@@ -1176,7 +1292,7 @@ cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t
     int sms = sm_count();
     if (sms <= 0) return fail(CS_ERR_CUDA, "no CUDA device");
     int bpsm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, cs::primal_kernel, 256, 0);
+    cudaError_t e = occupancy_blocks(P, &bpsm);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
     if (bpsm < 1) bpsm = 1;
     int slots = sms * bpsm * 8;
@@ -1347,7 +1463,7 @@ extern "C" cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, co
     int sms = sm_count();
     if (sms <= 0) return fail(CS_ERR_CUDA, "no CUDA device");
     int bpsm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, cs::primal_kernel, 256, 0);
+    cudaError_t e = occupancy_blocks(P, &bpsm);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
     int slots = std::max(1, sms * std::max(1, bpsm) * 8);
     while (slots > 1 && layout(g->n_bound, slots, cap, P, L).total > kNoAllocScratchBytes) {
