@@ -117,6 +117,7 @@ SIGNATURES = {
         [C.POINTER(DualGraph), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.POINTER(Plan)],
     ),
     "cs_workspace_init": (C.c_int32, [C.POINTER(Plan), C.c_int32, _ptr, C.c_size_t, _ptr]),
+    "cs_dual_workspace_init": (C.c_int32, [C.POINTER(Plan), C.c_int32, _ptr, C.c_size_t, _ptr]),
     "cs_centrality_shortest": (
         C.c_int32,
         [C.POINTER(PrimalGraph), C.POINTER(Query), C.POINTER(Plan), _ptr, C.c_size_t, Outputs, _ptr],

@@ -21,7 +21,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CUDA_SOURCES = ["cs_primal.cu", "cs_dual.cu"]
 CXX_SOURCES = ["cs_host.cpp"]
-HEADERS = ["cs_common.cuh"]
+HEADERS = ["cs_common.cuh", "cs_sort.cuh"]
 
 
 def _nvcc() -> str:
@@ -51,6 +51,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     common = [
         "-O3",
         "-std=c++17",
+        "--extended-lambda",
         "-Xcompiler",
         "-fPIC,-ffp-contract=off",
         inc,

@@ -25,7 +25,7 @@ struct WsHeader {
     unsigned int n_failed;            // sources that overflowed their slot's capacity
     unsigned int err;                 // first device-side error code (CS_ERR_*)
     unsigned int err_where;           // diagnostic: where the error was raised
-    unsigned int pad0;
+    unsigned int n_inexact;         // sources whose parallel replay disagreed (redone exactly)
     unsigned long long sources_done;
     unsigned long long edges_relaxed;
     unsigned long long nodes_settled;

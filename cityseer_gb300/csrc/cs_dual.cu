@@ -1,23 +1,1086 @@
-// cs_dual.cu -- simplest-path (angular) centrality on the dual graph.  Placeholder entry points;
-// the kernels land in a later revision of this file.
-#include <cstdint>
+// cs_dual.cu -- GB300 kernels for simplest-path (angular) centrality on the dual graph.
+//
+// Reference behaviour (cityseer-api v4.24.0):
+//   centrality_simplest          rust/src/centrality.rs:1880-2132
+//   dijkstra_brandes_angular     rust/src/centrality.rs:577-775 (doubled states, endpoint slots)
+//   dual_node_endpoint_slots     rust/src/centrality.rs:533-566
+//   best_angular_target_states   rust/src/centrality.rs:793-821
+//   brandes_backprop_with_beta   rust/src/centrality.rs:823-873
+//   dijkstra_tree_angular        rust/src/centrality.rs:1202-1332
+//
+// A state is (dual node, entry slot): index 2*node + slot.  The route cost is the summed angular
+// change plus 1e-6 * length; the search is cut off on the summed travel seconds, which travel with
+// each state's chosen route.  Per source, one warp:
+//  A. Label-correcting search over states: atomicMin on a packed (route, seconds) 64-bit key gives
+//     the lexicographic least fixpoint, route first.
+//  B. Warp radix sort of the reached states by route: the reference's settle order.
+//  C. Replay, in route order, of every state's candidate offers through the reference's tie rules:
+//     final route, seconds, predecessors and sigma, each checked bit for bit against A.  The tie
+//     window can make the reference keep seconds that differ from the lexicographic minimum; a
+//     source where any state disagrees is redone by an exact sequential heap Dijkstra (the same
+//     BinaryHeap order as the reference) and replayed again.
+//  D. Per node: the best route / seconds over offers to both of its states (the reference's
+//     best_route_cost / best_agg_seconds), closeness into target rows.
+//  E. One backward Brandes sweep over states carrying every threshold.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <algorithm>
+#include <cmath>
+
 #include "cs_common.cuh"
+#include "cs_sort.cuh"
 
 extern "C" void cs_set_error_internal(const char *msg);
 
+namespace csd {
+using namespace cs;
+
+constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
+constexpr int DPM = 8;  // max incoming / outgoing dual edges per state handled in registers
+
+__host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct DSlot {
+    unsigned long long *key;  // [2N] packed (route bits << 32 | seconds bits)
+    uint32_t *aux;            // [2N] settle position + 1 (0: unreached); bit 31 = settled (exact mode)
+    int32_t *rl;              // [cap] reached states, discovery order
+    ulonglong2 *qa, *qb, *qf;  // [2 cap] (state, key) queue entries
+    uint32_t *kb;
+    int32_t *vb;
+    uint32_t *rk;  // [cap] sorted route bits
+    int32_t *ord;  // [cap] sorted states
+    float *rB, *sB, *sig, *nbR, *nbS;  // [cap] replayed route, seconds, sigma; node best route/seconds
+    uint8_t *np;
+    int32_t *pr;  // [cap * DPM]
+    float *dl;    // [cap * K]
+    int32_t *hp;  // exact-mode heap: [2 cap] (route bits, state) pairs interleaved
+};
+
+__host__ __device__ inline size_t compact_bytes_d(size_t cap, int K) {
+    size_t b = 0;
+    b += 4 * al256(cap * 4);        // rl kb vb ord
+    b += 3 * al256(cap * 32);       // qa qb qf
+    b += 6 * al256(cap * 4);        // rk rB sB sig nbR nbS
+    b += al256(cap);                // np
+    b += al256(cap * 4 * DPM);      // pr
+    b += al256(cap * 4 * (size_t)K);  // dl
+    b += al256(cap * 16);           // hp
+    return b;
+}
+
+__host__ __device__ inline DSlot dslot(char *dense, size_t dense_stride, char *compact, size_t cap, int K, int slot,
+                                       int n_bound) {
+    DSlot s;
+    char *d = dense + dense_stride * (size_t)slot;
+    s.key = (unsigned long long *)d;
+    s.aux = (uint32_t *)(d + al256((size_t)n_bound * 16));
+    char *c = compact + compact_bytes_d(cap, K) * (size_t)slot;
+    size_t o = 0;
+    s.rl = (int32_t *)(c + o); o += al256(cap * 4);
+    s.kb = (uint32_t *)(c + o); o += al256(cap * 4);
+    s.vb = (int32_t *)(c + o); o += al256(cap * 4);
+    s.ord = (int32_t *)(c + o); o += al256(cap * 4);
+    s.qa = (ulonglong2 *)(c + o); o += al256(cap * 32);
+    s.qb = (ulonglong2 *)(c + o); o += al256(cap * 32);
+    s.qf = (ulonglong2 *)(c + o); o += al256(cap * 32);
+    s.rk = (uint32_t *)(c + o); o += al256(cap * 4);
+    s.rB = (float *)(c + o); o += al256(cap * 4);
+    s.sB = (float *)(c + o); o += al256(cap * 4);
+    s.sig = (float *)(c + o); o += al256(cap * 4);
+    s.nbR = (float *)(c + o); o += al256(cap * 4);
+    s.nbS = (float *)(c + o); o += al256(cap * 4);
+    s.np = (uint8_t *)(c + o); o += al256(cap);
+    s.pr = (int32_t *)(c + o); o += al256(cap * 4 * DPM);
+    s.dl = (float *)(c + o); o += al256(cap * 4 * (size_t)K);
+    s.hp = (int32_t *)(c + o); o += al256(cap * 16);
+    return s;
+}
+
+enum DMode { DMODE_CENTRALITY = 0, DMODE_TREE = 1 };
+
+struct DualParams {
+    cs_dual_graph g;
+    int32_t k;
+    float sk[MAXK];  // seconds thresholds as f32
+    float maxsec;
+    float tol;
+    float asu, fso;
+    float delta;     // band width in route (degrees)
+    int32_t closeness, betweenness, track_reach;
+    const int32_t *src_list;
+    int64_t n_src;
+    const float *src_wt;
+    const uint8_t *eligible;
+    double *out;     // [4][K][N]
+    double *bucket;  // [3][K][N]
+    uint32_t *reach;
+    WsHeader *hdr;
+    int32_t *failed;
+    int32_t fail_cap;
+    int32_t *inexact;     // sources whose replay disagreed with the search
+    int32_t inexact_cap;
+    char *dense;
+    size_t dense_stride;
+    char *compact;
+    int32_t cap;
+    int32_t n_slots;
+    int32_t pass;  // 0 = label-correcting pass, 1 = full-capacity retry, 2 = exact heap pass
+    const int32_t *remap;
+    int32_t mode;
+    int32_t force_exact;
+    int32_t row_cap;
+    int32_t *t_count, *t_node, *t_pred;
+    float *t_simpl, *t_agg;
+};
+
+__device__ __forceinline__ float hi_f(unsigned long long k) { return __uint_as_float((unsigned)(k >> 32)); }
+__device__ __forceinline__ float lo_f(unsigned long long k) { return __uint_as_float((unsigned)(k & 0xffffffffull)); }
+__device__ __forceinline__ unsigned long long pack(float r, float s) {
+    return ((unsigned long long)__float_as_uint(r) << 32) | (unsigned long long)__float_as_uint(s);
+}
+// route candidate exactly as rust/src/centrality.rs:665-667 evaluates it
+__device__ __forceinline__ float cand_route(float r, float ang, float len) {
+    return __fadd_rn(__fadd_rn(r, ang), __fmul_rn(ANGULAR_TIE_BREAK, len));
+}
+
+// ------------------------------------------------------------------------------------------
+// A. Label-correcting search over states.  Returns R or -1 on overflow.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void dpush(bool first, int route, int V, unsigned long long key, int &R, int &nn, int &nf,
+                                      int cap, int qcap, const DSlot &s, ulonglong2 *nxt, unsigned lt) {
+    const unsigned mf = __ballot_sync(FULL, first);
+    const unsigned mn = __ballot_sync(FULL, route == 1);
+    const unsigned mr = __ballot_sync(FULL, route == 2);
+    if (first) {
+        const int q = R + __popc(mf & lt);
+        if (q < cap) s.rl[q] = V;
+    }
+    if (route == 1) {
+        const int q = nn + __popc(mn & lt);
+        if (q < qcap) nxt[q] = make_ulonglong2((unsigned long long)V, key);
+    }
+    if (route == 2) {
+        const int q = nf + __popc(mr & lt);
+        if (q < qcap) s.qf[q] = make_ulonglong2((unsigned long long)V, key);
+    }
+    R += __popc(mf);
+    nn += __popc(mn);
+    nf += __popc(mr);
+}
+
+__device__ int dual_search(const DualParams &p, const DSlot &s, int src, long long &relaxed) {
+    const int lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    const int cap = p.cap, qcap = 2 * cap;
+    if (lane == 0) {
+        s.key[2 * src] = 0ull;
+        s.key[2 * src + 1] = 0ull;
+        s.rl[0] = 2 * src;
+        s.rl[1] = 2 * src + 1;
+        s.qa[0] = make_ulonglong2((unsigned long long)(2 * src), 0ull);
+        s.qa[1] = make_ulonglong2((unsigned long long)(2 * src + 1), 0ull);
+    }
+    __syncwarp();
+    int R = 2, nnear = 2, nfar = 0;
+    ulonglong2 *cur = s.qa, *nxt = s.qb;
+    float T = p.delta;
+    bool overflow = false;
+    while (true) {
+        while (nnear > 0) {
+            int nnext = 0;
+            for (int base = 0; base < nnear; base += 32) {
+                const int i = base + lane;
+                ulonglong2 ent = make_ulonglong2(0ull, KEY_INF);
+                if (i < nnear) ent = cur[i];
+                const int S = (int)ent.x;
+                const unsigned long long kS = (i < nnear) ? __ldcg(&s.key[S]) : KEY_INF;
+                const bool live = (i < nnear) && kS == ent.y;
+                const int u = S >> 1, e = S & 1;
+                const int beg = live ? __ldg(&p.g.ptr_dev[u]) : 0;
+                const int deg = live ? __ldg(&p.g.ptr_dev[u + 1]) - beg : 0;
+                relaxed += deg;
+                const float rU = hi_f(kS), sU = lo_f(kS);
+                const int maxdeg = warp_max_i(deg);
+                for (int j = 0; j < maxdeg; j++) {
+                    int V = 0;
+                    unsigned long long nk = KEY_INF;
+                    bool imp = false, first = false;
+                    float cr = 0.0f;
+                    if (j < deg) {
+                        const int ej = beg + j;
+                        if (__ldg(&p.g.exit_slot_dev[ej]) == 1 - e) {
+                            const float cs_ = __fadd_rn(sU, __ldg(&p.g.w_dev[ej]));
+                            if (cs_ <= p.maxsec) {
+                                V = 2 * __ldg(&p.g.to_dev[ej]) + __ldg(&p.g.entry_slot_dev[ej]);
+                                cr = cand_route(rU, __ldg(&p.g.ang_dev[ej]), __ldg(&p.g.len_dev[ej]));
+                                nk = pack(cr, cs_);
+                                const unsigned long long o = atomicMin(&s.key[V], nk);
+                                imp = nk < o;
+                                first = imp && o == KEY_INF;
+                            }
+                        }
+                    }
+                    dpush(first, imp ? (cr < T ? 1 : 2) : 0, V, nk, R, nnext, nfar, cap, qcap, s, nxt, lt);
+                }
+            }
+            __syncwarp();
+            if (R > cap || nnext > qcap || nfar > qcap) { overflow = true; break; }
+            ulonglong2 *t = cur; cur = nxt; nxt = t;
+            nnear = nnext;
+        }
+        if (overflow) break;
+        if (nfar == 0) break;
+        float mn = __int_as_float(INF_BITS);
+        for (int i = lane; i < nfar; i += 32) {
+            const ulonglong2 ent = s.qf[i];
+            const unsigned long long k = __ldcg(&s.key[(int)ent.x]);
+            if (k == ent.y) mn = fminf(mn, hi_f(k));
+        }
+        mn = warp_min_f(mn);
+        const float Told = T;
+        T = (mn == __int_as_float(INF_BITS)) ? Told
+                                             : fmaxf(__fadd_rn(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        int nn = 0, nf2 = 0;
+        for (int base = 0; base < nfar; base += 32) {
+            const int i = base + lane;
+            const bool act = i < nfar;
+            const ulonglong2 ent = act ? s.qf[i] : make_ulonglong2(0ull, KEY_INF);
+            const unsigned long long k = act ? __ldcg(&s.key[(int)ent.x]) : KEY_INF;
+            const bool live = act && k == ent.y;
+            const bool tonear = live && hi_f(k) < T;
+            const bool keep = live && !tonear;
+            const unsigned mt = __ballot_sync(FULL, tonear);
+            const unsigned mk = __ballot_sync(FULL, keep);
+            __syncwarp();
+            if (tonear) cur[nn + __popc(mt & lt)] = ent;
+            if (keep) s.qf[nf2 + __popc(mk & lt)] = ent;
+            nn += __popc(mt);
+            nf2 += __popc(mk);
+            __syncwarp();
+        }
+        nnear = nn;
+        nfar = nf2;
+    }
+    __syncwarp();
+    if (overflow) return -1;
+    return R;
+}
+
+// ------------------------------------------------------------------------------------------
+// A'. Exact sequential Dijkstra (lane 0) with the reference's BinaryHeap order
+//     (rust/src/centrality.rs:357-386, 598-705).  Writes key[] and the settle order into ord/rk.
+//     Returns R or -1 on overflow.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool hle(const int32_t *h, int a, int b) {
+    // a <= b under Ord for NodeDistance: other.metric.total_cmp(self.metric) (metrics >= 0 here)
+    return h[2 * a] >= h[2 * b];
+}
+__device__ __forceinline__ void hswap(int32_t *h, int a, int b) {
+    const int32_t m = h[2 * a], st = h[2 * a + 1];
+    h[2 * a] = h[2 * b];
+    h[2 * a + 1] = h[2 * b + 1];
+    h[2 * b] = m;
+    h[2 * b + 1] = st;
+}
+__device__ void heap_sift_up(int32_t *h, int start, int pos) {
+    while (pos > start) {
+        const int parent = (pos - 1) / 2;
+        if (hle(h, pos, parent)) break;
+        hswap(h, pos, parent);
+        pos = parent;
+    }
+}
+
+__device__ int dual_exact_search(const DualParams &p, const DSlot &s, int src) {
+    const int lane = lane_id();
+    int R = -1;
+    if (lane == 0) {
+        const int cap = p.cap, hcap = 2 * cap;
+        int32_t *h = s.hp;
+        int len = 0;
+        bool overflow = false;
+        s.key[2 * src] = 0ull;
+        s.key[2 * src + 1] = 0ull;
+        for (int sl = 0; sl < 2; sl++) {
+            h[2 * len] = 0;
+            h[2 * len + 1] = 2 * src + sl;
+            len++;
+            heap_sift_up(h, 0, len - 1);
+        }
+        const float one_plus = 1.0f + TIE_EPSILON;
+        int n = 0;
+        while (len > 0 && !overflow) {
+            // pop: swap last into the root, sift down to the bottom, then up (Rust BinaryHeap)
+            len--;
+            const int32_t s_top = h[1];
+            if (len > 0) {
+                const int32_t m_last = h[2 * len], s_last = h[2 * len + 1];
+                h[0] = m_last;
+                h[1] = s_last;
+                int pos = 0, child = 1;
+                const int end = len;
+                while (end >= 2 && child <= end - 2) {
+                    child += hle(h, child, child + 1) ? 1 : 0;
+                    h[2 * pos] = h[2 * child];
+                    h[2 * pos + 1] = h[2 * child + 1];
+                    pos = child;
+                    child = 2 * pos + 1;
+                }
+                if (child == end - 1) {
+                    h[2 * pos] = h[2 * child];
+                    h[2 * pos + 1] = h[2 * child + 1];
+                    pos = child;
+                }
+                h[2 * pos] = m_last;
+                h[2 * pos + 1] = s_last;
+                heap_sift_up(h, 0, pos);
+            }
+            const int S = s_top;
+            if (s.aux[S] & 0x80000000u) continue;
+            if (n >= cap) { overflow = true; break; }
+            s.aux[S] = 0x80000000u;
+            const unsigned long long kS = s.key[S];
+            s.ord[n] = S;
+            s.rk[n] = (uint32_t)(kS >> 32);
+            n++;
+            const int u = S >> 1, e = S & 1;
+            const float rU = hi_f(kS), sU = lo_f(kS);
+            const int beg = __ldg(&p.g.ptr_dev[u]), end2 = __ldg(&p.g.ptr_dev[u + 1]);
+            for (int ej = beg; ej < end2; ej++) {
+                if (__ldg(&p.g.exit_slot_dev[ej]) != 1 - e) continue;
+                const float cs_ = __fadd_rn(sU, __ldg(&p.g.w_dev[ej]));
+                if (cs_ > p.maxsec) continue;
+                const int V = 2 * __ldg(&p.g.to_dev[ej]) + __ldg(&p.g.entry_slot_dev[ej]);
+                if (s.aux[V] & 0x80000000u) continue;
+                const float cr = cand_route(rU, __ldg(&p.g.ang_dev[ej]), __ldg(&p.g.len_dev[ej]));
+                const unsigned long long kV = s.key[V];
+                const float curR = (kV == KEY_INF) ? __int_as_float(INF_BITS) : hi_f(kV);
+                const float curS = (kV == KEY_INF) ? __int_as_float(INF_BITS) : lo_f(kV);
+                if (cr < curR) {
+                    s.key[V] = pack(cr, cs_);
+                    if (len >= hcap) { overflow = true; break; }
+                    h[2 * len] = (int32_t)__float_as_uint(cr);
+                    h[2 * len + 1] = V;
+                    len++;
+                    heap_sift_up(h, 0, len - 1);
+                } else if (cr <= __fmul_rn(curR, one_plus) && cs_ < curS) {
+                    s.key[V] = pack(curR, cs_);
+                }
+            }
+        }
+        // clear the settled marks (positions are written after the sort step is skipped)
+        for (int i = 0; i < n; i++) s.aux[s.ord[i]] = 0u;
+        R = overflow ? -1 : n;
+    }
+    R = __shfl_sync(FULL, R, 0);
+    return R;
+}
+
+// ------------------------------------------------------------------------------------------
+// C. Replay in route order.
+// ------------------------------------------------------------------------------------------
+struct DOff {
+    int pos[DPM];
+    float cr[DPM];
+    float cs[DPM];
+    unsigned valid;  // offers settled before the target
+};
+
+// Offers to the state at position i (state V): incoming dual edges of V's node that enter at V's
+// slot, from reached states settled before it.  Needs rB/sB of those states.
+__device__ __forceinline__ void gather_doffers(const DualParams &p, const DSlot &s, int V, int i, int R, DOff &o,
+                                               bool &bad) {
+    const int v = V >> 1, sv = V & 1;
+    const int beg = __ldg(&p.g.rptr_dev[v]);
+    const int deg = min(__ldg(&p.g.rptr_dev[v + 1]) - beg, DPM);
+    o.valid = 0u;
+    int ids[DPM], us[DPM];
+#pragma unroll
+    for (int j = 0; j < DPM; j++) {
+        ids[j] = (j < deg) ? __ldg(&p.g.rid_dev[beg + j]) : 0;
+        us[j] = (j < deg) ? __ldg(&p.g.rfrom_dev[beg + j]) : 0;
+    }
+    uint32_t aa[DPM];
+#pragma unroll
+    for (int j = 0; j < DPM; j++) {
+        aa[j] = 0u;
+        if (j < deg && __ldg(&p.g.entry_slot_dev[ids[j]]) == sv) {
+            const int U = 2 * us[j] + (1 - __ldg(&p.g.exit_slot_dev[ids[j]]));
+            aa[j] = s.aux[U];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < DPM; j++) {
+        o.pos[j] = -1;
+        o.cr[j] = 0.0f;
+        o.cs[j] = 0.0f;
+        if (aa[j] > (uint32_t)R) bad = true;
+        if (aa[j] != 0u && aa[j] <= (uint32_t)R && (int)aa[j] - 1 < i) {
+            const int pu = (int)aa[j] - 1;
+            o.pos[j] = pu;
+            o.cr[j] = cand_route(s.rB[pu], __ldg(&p.g.ang_dev[ids[j]]), __ldg(&p.g.len_dev[ids[j]]));
+            o.cs[j] = __fadd_rn(s.sB[pu], __ldg(&p.g.w_dev[ids[j]]));
+            o.valid |= 1u << j;
+        }
+    }
+}
+
+__device__ __forceinline__ int dnext(const DOff &o, unsigned todo) {
+    int best = -1, bp = 0x7fffffff;
+#pragma unroll
+    for (int j = 0; j < DPM; j++)
+        if (((todo >> j) & 1u) && o.pos[j] < bp) { bp = o.pos[j]; best = j; }
+    return best;
+}
+
+__device__ __forceinline__ bool dpos_in(const DOff &o, unsigned mask, int pos) {
+    bool has = false;
+#pragma unroll
+    for (int j = 0; j < DPM; j++) has |= ((mask >> j) & 1u) && o.pos[j] == pos;
+    return has;
+}
+
+// Reference state machine (rust/src/centrality.rs:658-693) over offers in settle order; returns the
+// predecessor mask and writes the replayed route and seconds.
+__device__ __forceinline__ unsigned dreplay(const DualParams &p, const DOff &o, float &route, float &secs) {
+    const float one_plus = 1.0f + TIE_EPSILON, one_minus = 1.0f - TIE_EPSILON;
+    float cur = __int_as_float(INF_BITS), sc = __int_as_float(INF_BITS);
+    unsigned pm = 0u, t = o.valid;
+    while (t) {
+        const int j = dnext(o, t);
+        t &= ~(1u << j);
+        float crj = 0.0f, csj = 0.0f;
+        int pj = 0;
+#pragma unroll
+        for (int q = 0; q < DPM; q++)
+            if (q == j) { crj = o.cr[q]; csj = o.cs[q]; pj = o.pos[q]; }
+        if (csj > p.maxsec) continue;
+        const bool improved = crj < cur;
+        const bool tied = crj <= __fmul_rn(cur, one_plus);
+        if (improved) {
+            if (crj < __fmul_rn(cur, one_minus)) pm = 0u;
+            pm |= 1u << j;
+            cur = crj;
+            sc = csj;
+        } else if (tied && !dpos_in(o, pm, pj)) {
+            if (csj < sc) sc = csj;
+            pm |= 1u << j;
+        }
+    }
+    route = cur;
+    secs = sc;
+    if (p.tol > TIE_EPSILON) {
+        const float lim = __fmul_rn(cur, 1.0f + p.tol);
+        pm = 0u;
+        t = o.valid;
+        while (t) {
+            const int j = dnext(o, t);
+            t &= ~(1u << j);
+            float crj = 0.0f;
+            int pj = 0;
+#pragma unroll
+            for (int q = 0; q < DPM; q++)
+                if (q == j) { crj = o.cr[q]; pj = o.pos[q]; }
+            if (crj <= lim && !dpos_in(o, pm, pj)) pm |= 1u << j;
+        }
+    }
+    return pm;
+}
+
+// Node-level best route / seconds (rust/src/centrality.rs:695-703) over offers to both states of
+// the node, in the global settle order of the offering states.  Positions of the states: i0/i1
+// (-1 when unreached).
+__device__ __forceinline__ void node_best(const DualParams &p, const DSlot &s, int v, int src, int i0, int i1, int R,
+                                          float &best, float &bsecs, bool &bad) {
+    DOff o0, o1;
+    o0.valid = 0u;
+    o1.valid = 0u;
+    if (i0 >= 0) gather_doffers(p, s, 2 * v, i0, R, o0, bad);
+    if (i1 >= 0) gather_doffers(p, s, 2 * v + 1, i1, R, o1, bad);
+    const float one_plus = 1.0f + TIE_EPSILON, one_minus = 1.0f - TIE_EPSILON;
+    best = (v == src) ? 0.0f : __int_as_float(INF_BITS);
+    bsecs = best;
+    unsigned t0 = o0.valid, t1 = o1.valid;
+    while (t0 | t1) {
+        const int j0 = t0 ? dnext(o0, t0) : -1;
+        const int j1 = t1 ? dnext(o1, t1) : -1;
+        int p0 = 0x7fffffff, p1 = 0x7fffffff;
+        float c0 = 0.0f, s0 = 0.0f, c1 = 0.0f, s1 = 0.0f;
+#pragma unroll
+        for (int q = 0; q < DPM; q++) {
+            if (q == j0) { p0 = o0.pos[q]; c0 = o0.cr[q]; s0 = o0.cs[q]; }
+            if (q == j1) { p1 = o1.pos[q]; c1 = o1.cr[q]; s1 = o1.cs[q]; }
+        }
+        // equal offering positions: the offering state relaxes its out-edges in list order; the
+        // two target slots are reached through different edges, so either order is one offer each
+        const bool take0 = j0 >= 0 && (j1 < 0 || p0 <= p1);
+        float cr, cs_;
+        if (take0) { cr = c0; cs_ = s0; t0 &= ~(1u << j0); }
+        else { cr = c1; cs_ = s1; t1 &= ~(1u << j1); }
+        if (cs_ > p.maxsec) continue;
+        if (cr < __fmul_rn(best, one_minus)) {
+            best = cr;
+            bsecs = cs_;
+        } else if (cr <= __fmul_rn(best, one_plus)) {
+            bsecs = fminf(bsecs, cs_);
+        }
+    }
+}
+
+__device__ __forceinline__ double f2d(float x) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    const uint32_t lo = b << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ int first_ks(const DualParams &p, float secs) {
+    int k = 0;
+    while (k < p.k && !(secs <= p.sk[k])) k++;
+    return k;
+}
+
+// Replay + sigma in route order.  Returns false (and sets mismatch) when the replay disagrees with
+// the search's keys.
+__device__ bool dual_replay(const DualParams &p, const DSlot &s, int src, int R, bool &bad) {
+    const int lane = lane_id();
+    bool mismatch = false;
+    for (int base = 0; base < R; base += 32) {
+        const int i = base + lane;
+        const bool act = i < R;
+        const int V = act ? s.ord[i] : 0;
+        const bool is_src = act && (V >> 1) == src;
+        // in-chunk offerer positions (their rB/sB/sig must be final first)
+        DOff o;
+        o.valid = 0u;
+        unsigned pm = 0u;
+        if (act && !is_src) {
+            // positions only: recomputed after readiness with final values
+            const int v = V >> 1, sv = V & 1;
+            const int beg = __ldg(&p.g.rptr_dev[v]);
+            const int deg = min(__ldg(&p.g.rptr_dev[v + 1]) - beg, DPM);
+            for (int j = 0; j < deg; j++) {
+                const int id = __ldg(&p.g.rid_dev[beg + j]);
+                if (__ldg(&p.g.entry_slot_dev[id]) != sv) continue;
+                const int U = 2 * __ldg(&p.g.rfrom_dev[beg + j]) + (1 - __ldg(&p.g.exit_slot_dev[id]));
+                const uint32_t a = s.aux[U];
+                if (a != 0u && a <= (uint32_t)R && (int)a - 1 < i && (int)a - 1 >= base) pm |= 1u << ((int)a - 1 - base);
+            }
+        }
+        bool mine = !act;
+        unsigned done = __ballot_sync(FULL, mine);
+        int guard = 0;
+        while (done != FULL) {
+            const bool ready = !mine && ((pm & ~done) == 0u);
+            if (ready) {
+                float route, secs, sg;
+                int np = 0;
+                if (is_src) {
+                    route = 0.0f;
+                    secs = 0.0f;
+                    sg = 1.0f;
+                } else {
+                    gather_doffers(p, s, V, i, R, o, bad);
+                    const unsigned pmask = dreplay(p, o, route, secs);
+                    sg = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < DPM; j++) {
+                        if ((pmask >> j) & 1u) {
+                            s.pr[(size_t)i * DPM + np] = o.pos[j];
+                            sg = __fadd_rn(sg, s.sig[o.pos[j]]);
+                            np++;
+                        }
+                    }
+                }
+                s.rB[i] = route;
+                s.sB[i] = secs;
+                s.sig[i] = sg;
+                s.np[i] = (uint8_t)np;
+                const unsigned long long k = __ldcg(&s.key[V]);
+                if (__float_as_uint(route) != (unsigned)(k >> 32) ||
+                    __float_as_uint(secs) != (unsigned)(k & 0xffffffffull))
+                    mismatch = true;
+                mine = true;
+            }
+            __syncwarp();
+            done |= __ballot_sync(FULL, ready);
+            if (++guard > 64) break;
+        }
+        if (done != FULL) {
+            if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 21);
+            return false;
+        }
+    }
+    return !__any_sync(FULL, mismatch);
+}
+
+// ------------------------------------------------------------------------------------------
+// D + E. Node best, closeness, backward sweep.
+// ------------------------------------------------------------------------------------------
+__device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, int R, int *cnt, bool &bad) {
+    const int lane = lane_id();
+    const int K = p.k;
+    const int N = p.g.n_bound;
+    const float wt = __ldg(&p.src_wt[src]);
+    for (int q = lane; q < MAXK; q += 32) cnt[q] = 0;
+    __syncwarp();
+    // node best (the lane of the lower-positioned state of each node) + closeness
+    const size_t KN = (size_t)K * N;
+    const double wt_d = f2d(wt);
+    for (int i = lane; i < R; i += 32) {
+        const int V = s.ord[i];
+        const int v = V >> 1;
+        const uint32_t as = s.aux[V ^ 1];
+        const int isib = (as != 0u && as <= (uint32_t)R) ? (int)as - 1 : -1;
+        if (isib >= 0 && isib < i) continue;
+        const int i0 = (V & 1) ? isib : i;
+        const int i1 = (V & 1) ? i : isib;
+        float best, bsecs;
+        node_best(p, s, v, src, i0, i1, R, best, bsecs, bad);
+        s.nbR[i] = best;
+        s.nbS[i] = bsecs;
+        if (isib >= 0) {
+            s.nbR[isib] = best;
+            s.nbS[isib] = bsecs;
+        }
+        if (!p.closeness || v == src) continue;
+        if (!isfinite(best) || !isfinite(bsecs)) continue;
+        const int k0 = first_ks(p, bsecs);
+        if (k0 >= K) continue;
+        atomicAdd(&cnt[k0], 1);
+        const float ratio = __fdiv_rn(best, p.asu);
+        const float far_ang = __fadd_rn(p.fso, ratio);
+        const float harm_ang = __fadd_rn(1.0f, ratio);
+        double *bk = p.bucket + (size_t)k0 * N + v;
+        atomicAdd(bk, wt_d);
+        atomicAdd(bk + KN, f2d(__fmul_rn(far_ang, wt)));
+        atomicAdd(bk + 2 * KN, f2d(__fmul_rn(__fdiv_rn(1.0f, harm_ang), wt)));
+    }
+    __syncwarp();
+    if (p.closeness && p.track_reach && lane == 0) {
+        int run = 0;
+        for (int k = 0; k < K; k++) {
+            run += cnt[k];
+            if (run > 0) atomicAdd(&p.reach[k], (unsigned)run);
+        }
+    }
+    if (!p.betweenness) return;
+    // backward sweep over states, K lanes (rust/src/centrality.rs:2036-2096)
+    float *dl = s.dl;
+    for (int i = lane; i < R; i += 32)
+        for (int q = 0; q < K; q++) dl[(size_t)i * K + q] = 0.0f;
+    __syncwarp();
+    const bool unit_wt = (wt == 1.0f);
+    const double wtd = (double)wt;
+    const float one_tol = 1.0f + p.tol;
+    const int nchunks = (R + 31) / 32;
+    for (int ch = nchunks - 1; ch >= 0; ch--) {
+        const int base = ch * 32;
+        const int i = base + lane;
+        const bool act = i < R;
+        const int np = act ? s.np[i] : 0;
+        int pl[DPM];
+        unsigned pm = 0u;
+#pragma unroll
+        for (int r = 0; r < DPM; r++) {
+            pl[r] = (r < np) ? s.pr[(size_t)i * DPM + r] : 0;
+            if (r < np && pl[r] >= base) pm |= 1u << (pl[r] - base);
+        }
+        bool mine = !act;
+        unsigned done = __ballot_sync(FULL, mine);
+        int guard = 0;
+        while (done != FULL) {
+            const unsigned blocked = __reduce_or_sync(FULL, mine ? 0u : pm);
+            const bool ready = !mine && !((blocked >> lane) & 1u);
+            if (ready) {
+                const int V = s.ord[i];
+                const int v = V >> 1;
+                const float sw = s.sig[i];
+                const float secs = s.sB[i];
+                const float route = s.rB[i];
+                const float best = s.nbR[i], bsecs = s.nbS[i];
+                // sibling state for the seed split
+                const uint32_t as = s.aux[V ^ 1];
+                const int isib = (as != 0u && as <= (uint32_t)R) ? (int)as - 1 : -1;
+                const float sig_sib = isib >= 0 ? s.sig[isib] : 0.0f;
+                const float secs_sib = isib >= 0 ? s.sB[isib] : 0.0f;
+                const float route_sib = isib >= 0 ? s.rB[isib] : 0.0f;
+                const float pair = __ldg(&p.eligible[v]) ? 0.5f : 1.0f;
+                float fr[DPM];
+#pragma unroll
+                for (int r = 0; r < DPM; r++) {
+                    fr[r] = 0.0f;
+                    if (r < np) {
+                        const float sv = s.sig[pl[r]];
+                        fr[r] = (sv == sw) ? 1.0f : __fdiv_rn(sv, sw);
+                    }
+                }
+                float *dli = dl + (size_t)i * K;
+                for (int k = 0; k < K; k++) {
+                    const float thr = p.sk[k];
+                    if (!(secs <= thr)) continue;  // include_state: agg_seconds <= threshold
+                    if (sw == 0.0f) continue;
+                    float seed = 0.0f;
+                    if (v != src && isfinite(best) && isfinite(bsecs) && bsecs <= thr) {
+                        const bool me = sw != 0.0f && secs <= thr && route <= __fmul_rn(best, one_tol);
+                        const bool sib = isib >= 0 && sig_sib != 0.0f && secs_sib <= thr &&
+                                         route_sib <= __fmul_rn(best, one_tol);
+                        if (me) {
+                            const float tot = sib ? __fadd_rn(sw, sig_sib) : sw;
+                            seed = __fmul_rn(pair, __fdiv_rn(sw, tot));
+                        }
+                    }
+                    const float dep = __fadd_rn(seed, __ldcg(&dli[k]));
+                    if (dep == 0.0f) continue;
+#pragma unroll
+                    for (int r = 0; r < DPM; r++) {
+                        if (r >= np || fr[r] == 0.0f) continue;
+                        atomicAdd(&dl[(size_t)pl[r] * K + k], __fmul_rn(fr[r], dep));
+                    }
+                    if (v == src) continue;
+                    const float credit = __fadd_rn(dep, -seed);
+                    if (credit > 0.0f)
+                        atomicAdd(p.out + ((size_t)3 * K + k) * N + v, unit_wt ? f2d(credit) : f2d(credit) * wtd);
+                }
+                mine = true;
+            }
+            __syncwarp();
+            done |= __ballot_sync(FULL, ready);
+            if (++guard > 64) break;
+        }
+        if (done != FULL) {
+            if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 22);
+            return;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Persistent kernel.
+// ------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
+    __shared__ uint32_t hist_all[8][256];
+    __shared__ int cnt_all[8][MAXK];
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
+    if (slot >= p.n_slots) return;
+    const DSlot s = dslot(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.k, slot, p.g.n_bound);
+    long long relaxed = 0, settled = 0, done_src = 0;
+    const int N2 = 2 * p.g.n_bound;
+    while (true) {
+        unsigned long long idx = 0;
+        if (lane == 0) idx = atomicAdd(p.pass ? &p.hdr->work_next2 : &p.hdr->work_next, 1ull);
+        idx = __shfl_sync(FULL, idx, 0);
+        if (idx >= (unsigned long long)p.n_src) break;
+        if (__ldcg(&p.hdr->err) != 0u) break;
+        const int li = p.remap ? p.remap[idx] : (int)idx;
+        const int src = p.src_list[li];
+        const bool exact = (p.pass == 2) || p.force_exact;
+        int R;
+        if (exact) {
+            R = dual_exact_search(p, s, src);
+        } else {
+            R = dual_search(p, s, src, relaxed);
+        }
+        if (R < 0) {
+            for (int j = lane; j < N2; j += 32) {
+                s.key[j] = KEY_INF;
+                s.aux[j] = 0u;
+            }
+            if (lane == 0) {
+                if (p.pass != 0) {
+                    raise_err(p.hdr, CS_ERR_CAPACITY, 27);  // full-capacity passes must not overflow
+                } else {
+                    const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
+                    if (f < (unsigned)p.fail_cap) p.failed[f] = li;
+                    else raise_err(p.hdr, CS_ERR_CAPACITY, 23);
+                }
+            }
+            __syncwarp();
+            continue;
+        }
+        if (!exact) warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb,
+                                    s.vb, s.rk, s.ord, hist_all[wib]);
+        __syncwarp();
+        for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+        __syncwarp();
+        bool bad = false;
+        const bool ok = dual_replay(p, s, src, R, bad);
+        if (ok) {
+            dual_accumulate(p, s, src, R, cnt_all[wib], bad);
+        } else if (lane == 0) {
+            if (exact) raise_err(p.hdr, CS_ERR_INTERNAL, 24);  // the exact pass must replay cleanly
+            else {
+                const unsigned f = atomicAdd(&p.hdr->n_inexact, 1u);
+                if (f < (unsigned)p.inexact_cap) p.inexact[f] = li;
+                else raise_err(p.hdr, CS_ERR_CAPACITY, 25);
+            }
+        }
+        if (__any_sync(FULL, bad) && lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 26);
+        __syncwarp();
+        for (int i = lane; i < R; i += 32) {
+            const int S = s.ord[i];
+            s.key[S] = KEY_INF;
+            s.aux[S] = 0u;
+        }
+        __syncwarp();
+        settled += R;
+        if (ok) done_src += 1;
+    }
+    const long long rsum = warp_sum_ll(relaxed);
+    if (lane == 0) {
+        atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
+        atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
+        atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
+    }
+}
+
+__global__ void fill_dual_dense(char *dense, size_t stride, int n_bound, int n_slots) {
+    const size_t per = 2 * (size_t)n_bound;
+    const size_t total = per * (size_t)n_slots;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int slot = (int)(t / per);
+        const size_t j = t % per;
+        char *d = dense + stride * (size_t)slot;
+        ((unsigned long long *)d)[j] = KEY_INF;
+        ((uint32_t *)(d + al256((size_t)n_bound * 16)))[j] = 0u;
+    }
+}
+
+__global__ void dual_bucket_prefix(const double *bucket, double *out, int K, int N) {
+    const size_t KN = (size_t)K * N;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+        for (int m = 0; m < 3; m++) {
+            double acc = 0.0;
+            for (int k = 0; k < K; k++) {
+                acc += bucket[(size_t)m * KN + (size_t)k * N + t];
+                out[(size_t)m * KN + (size_t)k * N + t] += acc;
+            }
+        }
+    }
+}
+
+}  // namespace csd
+
+// ==========================================================================================
+// Host side (C-ABI).
+// ==========================================================================================
+namespace {
+thread_local std::string d_err;
+
+cs_status dfail(cs_status code, const std::string &msg) {
+    cs_set_error_internal(msg.c_str());
+    return code;
+}
+cs_status dcuda(cudaError_t e, const char *what) {
+    return dfail(CS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+int dsm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return n;
+}
+
+struct DLayout {
+    size_t failed_off, inexact_off, bucket_off, dense_off, compact_off, compact_total, total, dense_stride;
+    int fail_cap;
+};
+
+DLayout dlayout(int n_bound, int n_slots, int cap, int K) {
+    DLayout l;
+    l.fail_cap = std::max(n_slots, 1 << 18);
+    l.failed_off = 256;
+    l.inexact_off = csd::al256(l.failed_off + 4 * (size_t)l.fail_cap);
+    l.bucket_off = csd::al256(l.inexact_off + 4 * (size_t)l.fail_cap);
+    l.dense_off = csd::al256(l.bucket_off + sizeof(double) * 3 * (size_t)K * (size_t)n_bound);
+    l.dense_stride = csd::al256((size_t)n_bound * 16) + csd::al256((size_t)n_bound * 8);
+    l.compact_off = l.dense_off + l.dense_stride * (size_t)n_slots;
+    l.compact_total = std::max(csd::compact_bytes_d((size_t)cap, K) * (size_t)n_slots,
+                               csd::compact_bytes_d(2 * (size_t)n_bound, K));
+    l.total = l.compact_off + l.compact_total;
+    return l;
+}
+
+cs_status dvalidate(const cs_dual_graph *g) {
+    if (!g) return dfail(CS_ERR_ARG, "graph is NULL");
+    if (g->n_bound <= 0) return dfail(CS_ERR_ARG, "NetworkStructure contains no nodes.");
+    if (g->max_out_degree > csd::DPM)
+        return dfail(CS_ERR_ARG, "a dual node has more than 8 incoming or outgoing dual edges (intersections of "
+                                 "degree above 5); not supported by the simplest-path kernels");
+    return CS_OK;
+}
+
+cs_status dreset(char *dense, size_t stride, int n_bound, int n_slots, cudaStream_t s) {
+    const size_t total = 2 * (size_t)n_bound * (size_t)n_slots;
+    int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)std::max(1, dsm_count()) * 16);
+    csd::fill_dual_dense<<<std::max(1, blocks), 256, 0, s>>>(dense, stride, n_bound, n_slots);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CS_OK : dcuda(e, "fill_dual_dense launch");
+}
+
+cs_status dlaunch(csd::DualParams &p, int n_slots, cudaStream_t s) {
+    p.n_slots = n_slots;
+    csd::dual_kernel<<<(n_slots + 7) / 8, 256, 0, s>>>(p);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CS_OK : dcuda(e, "dual_kernel launch");
+}
+
+cs_status dsync_header(cs::WsHeader *hd, cs::WsHeader &h, cudaStream_t s) {
+    cudaError_t e = cudaMemcpyAsync(&h, hd, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return dcuda(e, "dual kernel");
+    if (h.err != 0u)
+        return dfail((cs_status)h.err, "device-side check failed (code " + std::to_string(h.err) + " at " +
+                                           std::to_string(h.err_where) + ")");
+    return CS_OK;
+}
+}  // namespace
+
 extern "C" {
-cs_status cs_plan_dual(const cs_dual_graph *, int32_t, int32_t, int32_t, int32_t, int64_t, cs_plan *) {
-    cs_set_error_internal("simplest-path kernels are not built yet");
-    return CS_ERR_ARG;
+
+cs_status cs_plan_dual(const cs_dual_graph *g, int32_t mode, int32_t k, int32_t cap, int32_t max_slots,
+                       int64_t mem_budget_bytes, cs_plan *plan) {
+    cs_status st = dvalidate(g);
+    if (st != CS_OK) return st;
+    if (!plan) return dfail(CS_ERR_ARG, "plan is NULL");
+    if (mode != 0) return dfail(CS_ERR_ARG, "unknown dual mode");
+    if (k < 1 || k > CS_MAX_THRESHOLDS) return dfail(CS_ERR_ARG, "threshold count out of range");
+    const int sms = dsm_count();
+    if (sms <= 0) return dfail(CS_ERR_CUDA, "no CUDA device");
+    int bpsm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, csd::dual_kernel, 256, 0);
+    if (e != cudaSuccess) return dcuda(e, "occupancy query");
+    int slots = sms * std::max(1, bpsm) * 8;
+    if (max_slots > 0) slots = std::min(slots, max_slots);
+    const int n2 = 2 * g->n_bound;
+    if (cap <= 0) cap = std::min(n2, 16384);
+    cap = std::max(64, std::min(cap, n2));
+    if (mem_budget_bytes > 0)
+        while (slots > 8 && (int64_t)dlayout(g->n_bound, slots, cap, k).total > mem_budget_bytes) slots = slots * 7 / 8;
+    plan->n_slots = std::max(1, slots);
+    plan->cap = cap;
+    plan->threads_per_block = 256;
+    plan->blocks = (plan->n_slots + 7) / 8;
+    if (!(plan->delta_seconds > 0.0f)) plan->delta_seconds = 30.0f;  // band width in route degrees
+    plan->lanes = k;
+    plan->workspace_bytes = dlayout(g->n_bound, plan->n_slots, cap, k).total;
+    return CS_OK;
 }
-cs_status cs_centrality_simplest(const cs_dual_graph *, const cs_query *, const cs_plan *, void *, size_t, cs_outputs,
-                                 void *) {
-    cs_set_error_internal("simplest-path kernels are not built yet");
-    return CS_ERR_ARG;
+
+cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, const cs_plan *plan, void *ws,
+                                 size_t ws_bytes, cs_outputs out, void *stream_v) {
+    cs_status st = dvalidate(g);
+    if (st != CS_OK) return st;
+    if (!q || !plan || !ws) return dfail(CS_ERR_ARG, "query/plan/workspace is NULL");
+    const int K = q->k;
+    if (K < 1 || K > CS_MAX_THRESHOLDS) return dfail(CS_ERR_ARG, "threshold count out of range");
+    if (plan->lanes < K) return dfail(CS_ERR_ARG, "plan was made for fewer thresholds");
+    const DLayout lay = dlayout(g->n_bound, plan->n_slots, plan->cap, plan->lanes);
+    if (ws_bytes < lay.total) return dfail(CS_ERR_ARG, "workspace too small for this plan");
+    if (!out.out_dev) return dfail(CS_ERR_ARG, "out_dev is NULL");
+    if (q->track_reach && !out.reach_dev) return dfail(CS_ERR_ARG, "reach_dev required when track_reach");
+    if (!(q->speed_m_s > 0.0f)) return dfail(CS_ERR_ARG, "speed_m_s must be finite and positive");
+    cudaStream_t s = (cudaStream_t)stream_v;
+    char *base = (char *)ws;
+    csd::DualParams p;
+    memset(&p, 0, sizeof(p));
+    p.g = *g;
+    p.k = K;
+    uint32_t maxs = 0;
+    for (int i = 0; i < K; i++) {
+        p.sk[i] = (float)q->seconds[i];
+        maxs = std::max(maxs, q->seconds[i]);
+    }
+    p.maxsec = (float)maxs;
+    p.tol = q->tolerance;
+    p.asu = q->angular_scaling_unit;
+    p.fso = q->farness_scaling_offset;
+    p.delta = plan->delta_seconds > 0.0f ? plan->delta_seconds : 30.0f;
+    p.closeness = q->compute_closeness;
+    p.betweenness = q->compute_betweenness;
+    p.track_reach = q->track_reach;
+    p.src_list = q->sources_dev;
+    p.n_src = q->n_sources;
+    p.src_wt = q->src_wt_dev;
+    p.eligible = q->eligible_dev;
+    p.out = out.out_dev;
+    p.reach = out.reach_dev;
+    p.hdr = (cs::WsHeader *)base;
+    p.failed = (int32_t *)(base + lay.failed_off);
+    p.fail_cap = lay.fail_cap;
+    p.inexact = (int32_t *)(base + lay.inexact_off);
+    p.inexact_cap = lay.fail_cap;
+    p.bucket = (double *)(base + lay.bucket_off);
+    p.dense = base + lay.dense_off;
+    p.dense_stride = lay.dense_stride;
+    p.compact = base + lay.compact_off;
+    p.cap = plan->cap;
+    const char *fe = getenv("CS_DUAL_FORCE_EXACT");
+    p.force_exact = (fe && fe[0] == '1') ? 1 : 0;
+    if (p.n_src <= 0) return CS_OK;
+    cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), s);
+    if (e == cudaSuccess && p.closeness)
+        e = cudaMemsetAsync(p.bucket, 0, sizeof(double) * 3 * (size_t)K * (size_t)g->n_bound, s);
+    if (e != cudaSuccess) return dcuda(e, "workspace reset");
+    st = dlaunch(p, plan->n_slots, s);
+    if (st != CS_OK) return st;
+    cs::WsHeader h;
+    st = dsync_header(p.hdr, h, s);
+    if (st != CS_OK) return st;
+    const size_t per_full = csd::compact_bytes_d(2 * (size_t)g->n_bound, K);
+    // pass 1: sources that overflowed their slot, at full capacity (label-correcting)
+    // pass 2: sources whose replay disagreed with the label-correcting search, exact heap order
+    for (int pass = 1; pass <= 2; pass++) {
+        const unsigned n_list = pass == 1 ? h.n_failed : h.n_inexact;
+        if (n_list == 0u) continue;
+        const int nl = (int)std::min<unsigned>(n_list, (unsigned)lay.fail_cap);
+        csd::DualParams p2 = p;
+        p2.pass = pass;
+        p2.cap = 2 * g->n_bound;
+        p2.remap = pass == 1 ? p.failed : p.inexact;
+        p2.n_src = nl;
+        if (pass == 2) {
+            // the exact pass writes new overflow / inexact entries nowhere: it cannot overflow at
+            // full capacity and its replay must agree
+            p2.inexact = p.failed;  // unused
+        }
+        e = cudaMemsetAsync(&p.hdr->work_next2, 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess) return dcuda(e, "retry counter reset");
+        int slots2 = (int)std::min<size_t>(lay.compact_total / per_full, (size_t)plan->n_slots);
+        slots2 = std::max(1, std::min(slots2, nl));
+        st = dlaunch(p2, slots2, s);
+        if (st != CS_OK) return st;
+        cs::WsHeader h2;
+        st = dsync_header(p.hdr, h2, s);
+        if (st != CS_OK) return st;
+        if (pass == 1) h.n_inexact = h2.n_inexact;  // retries may add inexact sources
+    }
+    if (p.closeness) {
+        int blocks = std::max(1, std::min((g->n_bound + 255) / 256, dsm_count() * 8));
+        csd::dual_bucket_prefix<<<blocks, 256, 0, s>>>(p.bucket, p.out, K, g->n_bound);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return dcuda(e, "dual_bucket_prefix launch");
+    }
+    return CS_OK;
 }
+
+cs_status cs_dual_workspace_init(const cs_plan *plan, int32_t n_bound, void *ws, size_t ws_bytes, void *stream) {
+    if (!plan || !ws) return dfail(CS_ERR_ARG, "plan/workspace is NULL");
+    if (ws_bytes < plan->workspace_bytes) return dfail(CS_ERR_ARG, "workspace smaller than plan");
+    const DLayout lay = dlayout(n_bound, plan->n_slots, plan->cap, plan->lanes);
+    cudaError_t e = cudaMemsetAsync(ws, 0, 256, (cudaStream_t)stream);
+    if (e != cudaSuccess) return dcuda(e, "workspace init");
+    return dreset((char *)ws + lay.dense_off, lay.dense_stride, n_bound, plan->n_slots, (cudaStream_t)stream);
+}
+
 cs_status cs_tree_simplest(const cs_dual_graph *, int32_t, const int32_t *, uint32_t, float, const cs_plan *, void *,
                            size_t, int32_t, int32_t *, int32_t *, float *, float *, int32_t *, void *) {
-    cs_set_error_internal("simplest-path kernels are not built yet");
-    return CS_ERR_ARG;
+    return dfail(CS_ERR_ARG, "dijkstra_tree_simplest is not available on the GPU yet");
 }
-}
+
+}  // extern "C"

@@ -1,10 +1,209 @@
-"""Simplest-path (angular) centrality on the dual graph -- device CSR and drivers."""
+"""Simplest-path (angular) centrality on the dual graph: device CSR and drivers.
+
+Dual CSR layout in HBM:
+  forward   per dual node u: its outgoing dual edges in petgraph Outgoing order (newest first)
+            ptr[N+1], to[E], w[E] (travel seconds, no impedance), ang[E] (angle_sum), len[E],
+            exit_slot[E] / entry_slot[E] (endpoint slot of the shared primal node at each end)
+  reverse   per dual node v: its incoming dual edges: rptr[N+1], rfrom[E], rid[E] (forward index)
+Endpoint slots restate dual_node_endpoint_slots (rust/src/centrality.rs:533-566): in edge order,
+each dual node's shared primal keys take slots 0 and 1 in order of first appearance.
+"""
 from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _native, device
+
+DPM = 8
+
+
+def endpoint_slots(src, dst, key, n_bound):
+    """Slot of each edge's shared key at its source and at its target (arrays over edges)."""
+    m = len(src)
+    if m == 0:
+        return np.zeros(0, np.uint8), np.zeros(0, np.uint8)
+    if np.any(key < 0):
+        e = int(np.nonzero(key < 0)[0][0])
+        raise ValueError(f"dual edge {int(src[e])} -> {int(dst[e])} is missing shared_primal_node_key metadata")
+    node = np.stack([src, dst], 1).reshape(-1)
+    kk = np.stack([key, key], 1).reshape(-1)
+    order = np.arange(2 * m)
+    rec = np.zeros(2 * m, dtype=[("n", np.int64), ("k", np.int64), ("o", np.int64)])
+    rec["n"], rec["k"], rec["o"] = node, kk, order
+    srt = np.argsort(rec, order=("n", "k", "o"))
+    r = rec[srt]
+    first = np.ones(2 * m, bool)
+    first[1:] = (r["n"][1:] != r["n"][:-1]) | (r["k"][1:] != r["k"][:-1])
+    fo = r[first]  # first occurrence of each (node, key)
+    # per node: rank of its keys by first appearance
+    srt2 = np.lexsort((fo["o"], fo["n"]))
+    fo = fo[srt2]
+    start = np.ones(len(fo), bool)
+    start[1:] = fo["n"][1:] != fo["n"][:-1]
+    grp = np.cumsum(start) - 1
+    first_idx = np.nonzero(start)[0]
+    rank = np.arange(len(fo)) - first_idx[grp]
+    if np.any(rank > 1):
+        bad = int(fo["n"][np.nonzero(rank > 1)[0][0]])
+        raise ValueError(f"dual node {bad} references more than two primal endpoints")
+    # look up the slot of (node, key)
+    q = np.zeros(2 * m, dtype=[("n", np.int64), ("k", np.int64)])
+    q["n"], q["k"] = node, kk
+    keys = np.zeros(len(fo), dtype=[("n", np.int64), ("k", np.int64)])
+    keys["n"], keys["k"] = fo["n"], fo["k"]
+    o2 = np.argsort(keys, order=("n", "k"))
+    pos = np.searchsorted(keys[o2], q)
+    slot = rank[o2][pos].reshape(m, 2)
+    return slot[:, 0].astype(np.uint8), slot[:, 1].astype(np.uint8)
+
+
+class DualCSR:
+    def __init__(self, ns, dev: torch.device | None = None):
+        self.device = dev or device._require_cuda()
+        a = ns.arrays()
+        self.arr = a
+        n = ns.node_bound()
+        self.n_bound = n
+        ex = np.nonzero(a["e_exists"])[0]
+        src = a["e_src"][ex].astype(np.int64)
+        dst = a["e_dst"][ex].astype(np.int64)
+        key = a["e_shared"][ex].astype(np.int64)
+        exit_s, entry_s = endpoint_slots(src, dst, key, n)
+        self.ex = ex
+        self.m = len(ex)
+        fo = np.lexsort((-ex, src)) if self.m else np.zeros(0, np.int64)
+        ro = np.lexsort((-ex, dst)) if self.m else np.zeros(0, np.int64)
+        pos_in_fwd = np.empty(self.m, np.int64)
+        pos_in_fwd[fo] = np.arange(self.m)
+        out_cnt = np.bincount(src, minlength=n) if self.m else np.zeros(n, np.int64)
+        in_cnt = np.bincount(dst, minlength=n) if self.m else np.zeros(n, np.int64)
+        ptr = np.zeros(n + 1, np.int64)
+        rptr = np.zeros(n + 1, np.int64)
+        ptr[1:] = np.cumsum(out_cnt)
+        rptr[1:] = np.cumsum(in_cnt)
+        self.max_degree = int(max(out_cnt.max(initial=0), in_cnt.max(initial=0)))
+        self.fo, self.ro = fo, ro
+        t = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x).astype(dt)).to(self.device)  # noqa: E731
+        self.ptr = t(ptr, np.int32)
+        self.to = t(dst[fo], np.int32)
+        self.ang = t(a["e_ang"][ex][fo], np.float32)
+        self.len = t(a["e_len"][ex][fo], np.float32)
+        self.exit_slot = t(exit_s[fo], np.uint8)
+        self.entry_slot = t(entry_s[fo], np.uint8)
+        self.rptr = t(rptr, np.int32)
+        self.rfrom = t(src[ro], np.int32)
+        self.rid = t(pos_in_fwd[ro], np.int32)
+        self._w: dict[float, torch.Tensor] = {}
+
+    def w(self, speed: float) -> torch.Tensor:
+        k = float(np.float32(speed))
+        hit = self._w.get(k)
+        if hit is None:
+            w = device.edge_seconds(self.arr, speed, False)[self.ex][self.fo]
+            hit = torch.from_numpy(np.ascontiguousarray(w)).to(self.device)
+            self._w[k] = hit
+        return hit
+
+    def struct(self, speed: float) -> _native.DualGraph:
+        g = _native.DualGraph()
+        g.n_bound = self.n_bound
+        g.n_edges = self.m
+        g.max_out_degree = self.max_degree
+        g.ptr = self.ptr.data_ptr()
+        g.to = self.to.data_ptr()
+        g.w = self.w(speed).data_ptr()
+        g.ang = self.ang.data_ptr()
+        g.len = self.len.data_ptr()
+        g.exit_slot = self.exit_slot.data_ptr()
+        g.entry_slot = self.entry_slot.data_ptr()
+        g.rptr = self.rptr.data_ptr()
+        g.rfrom = self.rfrom.data_ptr()
+        g.rid = self.rid.data_ptr()
+        return g
+
+
+class DualWorkspace(device.Workspace):
+    def init(self, stream=None):
+        lib = _native.load()
+        rc = lib.cs_dual_workspace_init(C.byref(self.plan), self.n_bound, self.ptr, self.nbytes, stream)
+        _native.check(rc, "cs_dual_workspace_init")
+
+
+def dual_csr(ns) -> DualCSR:
+    c = ns._cache.get("dual_csr")
+    if c is None:
+        c = DualCSR(ns)
+        if c.max_degree > DPM:
+            raise ValueError("a dual node has more than 8 incoming or outgoing dual edges (intersections of degree "
+                             "above 5); not supported by the simplest-path kernels")
+        ns._cache["dual_csr"] = c
+    return c
+
+
+def dual_workspace(ns, csr: DualCSR, k: int, speed: float, cap: int = 0, max_slots: int = 0):
+    from .centrality import _mem_budget
+
+    key = ("wsd", k, cap, max_slots)
+    ws = ns._cache.get(key)
+    if ws is None:
+        for kk in [kk for kk in ns._cache if isinstance(kk, tuple) and kk and kk[0] in ("ws", "wsd")]:
+            del ns._cache[kk]
+        torch.cuda.empty_cache()
+        lib = _native.load()
+        plan = _native.Plan()
+        rc = lib.cs_plan_dual(C.byref(csr.struct(speed)), 0, k, cap, max_slots, _mem_budget(csr.device),
+                              C.byref(plan))
+        _native.check(rc, "cs_plan_dual")
+        ws = DualWorkspace(plan, csr.n_bound, csr.device)
+        ns._cache[key] = ws
+    return ws
 
 
 def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, betweenness, sp):
-    raise NotImplementedError("simplest-path kernels are not built yet")
+    from .centrality import CentralitySimplestResult, _groups, _make_query, _stream_ptr
+
+    nb = ns.node_bound()
+    node_indices = ns.node_indices()
+    K = len(dists)
+    data = np.zeros((4, K, nb), np.float64)
+    reach_tot = np.zeros(K, np.int64)
+    track = sp.sample_probability is not None or sp.is_source_indexed
+    csr = dual_csr(ns)
+    dev = csr.device
+    proc_t = torch.from_numpy(sp.process).to(dev)
+    wt_t = torch.from_numpy(sp.src_wt).to(dev)
+    el_t = torch.from_numpy(sp.eligible).to(dev)
+    g = csr.struct(speed)
+    lib = _native.load()
+    for lo, hi in _groups(K):
+        k = hi - lo
+        ws = dual_workspace(ns, csr, k, speed)
+        out = torch.zeros((4, k, nb), dtype=torch.float64, device=dev)
+        reach = torch.zeros(k, dtype=torch.int32, device=dev)
+        q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, tol, closeness, betweenness, track, proc_t,
+                        wt_t, el_t, asu, fso)
+        o = _native.Outputs(out.data_ptr(), reach.data_ptr())
+        rc = lib.cs_centrality_simplest(C.byref(g), C.byref(q), C.byref(ws.plan), ws.ptr, ws.nbytes, o, _stream_ptr())
+        if rc != _native.CS_OK:
+            ws.init(_stream_ptr())
+        _native.check(rc, "cs_centrality_simplest")
+        data[:, lo:hi] = out.cpu().numpy()
+        reach_tot[lo:hi] = reach.cpu().numpy().astype(np.int64)
+    if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
+        scale = sp.n_live / sp.n_sources
+        if scale != 1.0:
+            idx = np.asarray(node_indices, np.int64)
+            data[3][:, idx] *= scale
+    ns._progress = sp.n_sources
+    res = CentralitySimplestResult(dists, ns.node_keys_py(), node_indices, data)
+    if track:
+        res.sampled_source_count = sp.sampled_count
+        res.reachability_totals = [int(x) for x in reach_tot]
+    return res
 
 
 def tree_simplest(ns, sources, max_seconds, speed):
-    raise NotImplementedError("simplest-path kernels are not built yet")
+    raise NotImplementedError("dijkstra_tree_simplest is not available on the GPU yet")

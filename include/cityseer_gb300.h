@@ -136,6 +136,10 @@ cs_status cs_plan_primal(const cs_primal_graph *g, int32_t mode, int32_t k, int3
 cs_status cs_plan_dual(const cs_dual_graph *g, int32_t mode, int32_t k, int32_t cap, int32_t max_slots,
                        int64_t mem_budget_bytes, cs_plan *plan);
 
+/* Clean-state initialisation of a workspace planned by cs_plan_dual. */
+cs_status cs_dual_workspace_init(const cs_plan *plan, int32_t n_bound, void *workspace_dev, size_t workspace_bytes,
+                                 void *stream);
+
 /* Puts a freshly allocated workspace into the clean state every call expects (and leaves).
  * Call once after allocating it, and again after any call that returned an error. */
 cs_status cs_workspace_init(const cs_plan *plan, int32_t n_bound, void *workspace_dev, size_t workspace_bytes,
@@ -160,7 +164,9 @@ cs_status cs_centrality_shortest(const cs_primal_graph *g, const cs_query *q, co
 cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, const cs_query *q, cs_outputs out, void *stream);
 
 /* Replaces NetworkStructure.centrality_simplest (rust/src/centrality.rs:1880-2132) on a dual graph.
- * out rows: 0 density, 1 farness, 2 harmonic, 3 betweenness. */
+ * out rows: 0 density, 1 farness, 2 harmonic, 3 betweenness.  Workspaces from cs_plan_dual are put
+ * in their clean state by cs_dual_workspace_init.  Setting CS_DUAL_FORCE_EXACT=1 in the environment
+ * runs every source through the exact sequential search (a check of the parallel path). */
 cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, const cs_plan *plan,
                                  void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream);
 

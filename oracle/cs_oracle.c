@@ -1187,3 +1187,8 @@ int32_t og_sizeof_nvisit(void) { return (int32_t)sizeof(nvisit); }
 int32_t og_sizeof_evisit(void) { return (int32_t)sizeof(evisit); }
 int32_t og_sizeof_args(void) { return (int32_t)sizeof(og_args); }
 int32_t og_sizeof_desc(void) { return (int32_t)sizeof(og_graph_desc); }
+
+/* dual endpoint slots per node (2 entries, -1 empty) as computed above (test accessor) */
+void og_get_slots(const og_graph *g, int32_t *out) {
+    memcpy(out, g->slots, sizeof(int32_t) * 2 * (size_t)g->d.n_bound);
+}

@@ -92,6 +92,7 @@ def lib() -> C.CDLL:
         L.og_seconds_from_distances.argtypes = [_P, C.c_int32, C.c_float, _P]
         L.og_edge_travel_seconds.restype = C.c_float
         L.og_edge_travel_seconds.argtypes = [_P, C.c_int32, C.c_float, C.c_int32]
+        L.og_get_slots.argtypes = [_P, _P]
         for n in ("og_sizeof_nvisit", "og_sizeof_evisit", "og_sizeof_args", "og_sizeof_desc"):
             getattr(L, n).restype = C.c_int32
         assert L.og_sizeof_nvisit() == C.sizeof(_NVisit)
@@ -145,6 +146,11 @@ class OracleGraph:
     @property
     def slots_ok(self) -> bool:
         return bool(lib().og_slots_ok(self.h))
+
+    def slots(self) -> np.ndarray:
+        out = np.zeros(2 * max(self.nb, 1), np.int32)
+        lib().og_get_slots(self.h, out.ctypes.data)
+        return out[: 2 * self.nb].reshape(-1, 2)
 
 
 def _args(nb, dists, betas, secs, speed, tol, closeness, betweenness, plan, nthreads, asu=180.0, fso=1.0):

@@ -116,3 +116,20 @@ def test_synthetic_lattices_are_connected():
     nsd = synth.dual_structure(p)
     assert nsd.is_dual and nsd.node_count() == len(p.u)
     assert all(k is not None for k in nsd._e_shared)
+
+
+def test_dual_endpoint_slots_match_oracle():
+    import oracle
+    from cityseer_gb300 import dual
+
+    p, _ = synth.lattice_config("c3", side=10)
+    ns = synth.dual_structure(p)
+    a = ns.arrays()
+    ex = np.nonzero(a["e_exists"])[0]
+    src, dst, key = (a["e_src"][ex].astype(np.int64), a["e_dst"][ex].astype(np.int64),
+                     a["e_shared"][ex].astype(np.int64))
+    es, en = dual.endpoint_slots(src, dst, key, ns.node_bound())
+    slots = oracle.OracleGraph(ns).slots()
+    for e in range(len(ex)):
+        assert slots[src[e], es[e]] == key[e]
+        assert slots[dst[e], en[e]] == key[e]
