@@ -155,6 +155,18 @@ def cpu_baseline(ns, dists, n_total: int, target_seconds: float, nthreads: int |
     }
 
 
+def traffic_ratio():
+    """DRAM bytes per algorithmic byte of primal_kernel, from the committed ncu summary."""
+    p = ROOT / "profiles" / "primal_kernel_lattice160_shortest.md"
+    try:
+        for line in p.read_text().splitlines():
+            if line.startswith("traffic_per_alg_byte:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def flush_l2(buf):
     buf.add_(1.0)
 
@@ -292,7 +304,9 @@ def run_gpu(args):
         "peak": peak,
         "unit": "GB/s",
         "frac": achieved / peak,
-        "traffic": None,
+        "traffic": (traffic_ratio() * alg_bytes) if traffic_ratio() else None,
+        "traffic_note": "DRAM bytes per launch scaled from the 160x160 ncu capture "
+                        "(profiles/primal_kernel_lattice160_shortest.md) by algorithmic bytes",
         "peak_kind": peak_kind,
         "alg_bytes_per_launch": alg_bytes,
         "edges_relaxed": int(e_relax),

@@ -1,0 +1,23 @@
+"""Namespace mirror of the reference's compiled module `cityseer.rustalgos` (rust/src/lib.rs:37-164)
+for the parts this package implements: `rustalgos.graph.NetworkStructure`, the centrality result
+classes and the threshold conversions."""
+from types import SimpleNamespace
+
+from . import centrality as _c
+from . import graph as _g
+from .common import (
+    betas_from_distances,
+    distances_from_betas,
+    pair_distances_betas_time,
+    seconds_from_distances,
+)
+
+graph = SimpleNamespace(NetworkStructure=_g.NetworkStructure, NodeVisit=_g.NodeVisit, EdgeVisit=_g.EdgeVisit)
+centrality = SimpleNamespace(
+    CentralityShortestResult=_c.CentralityShortestResult,
+    CentralitySimplestResult=_c.CentralitySimplestResult,
+    CentralitySegmentResult=_c.CentralitySegmentResult,
+)
+
+__all__ = ["graph", "centrality", "pair_distances_betas_time", "betas_from_distances", "distances_from_betas",
+           "seconds_from_distances"]

@@ -133,3 +133,15 @@ def test_dual_endpoint_slots_match_oracle():
     for e in range(len(ex)):
         assert slots[src[e], es[e]] == key[e]
         assert slots[dst[e], en[e]] == key[e]
+
+
+def test_sampling_probability_schedule():
+    from cityseer_gb300 import sampling
+
+    assert sampling.compute_distance_p(1000) == 1.0
+    assert sampling.compute_distance_p(0) == 1.0
+    p5 = sampling.compute_distance_p(5000)
+    p20 = sampling.compute_distance_p(20000)
+    # pysrc/cityseer/metrics/networks.py:17-23 table, eps = 0.06: 58.7% at 5 km, 4.6% at 20 km
+    assert round(p5 * 100, 1) == 58.7 and round(p20 * 100, 1) == 4.6
+    assert sampling.compute_hoeffding_p(float("nan")) == 1.0
