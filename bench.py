@@ -369,6 +369,157 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+BATCH_METRIC = "sources/s, 96 mixed-size graphs (2k-150k nodes), shortest + segment: batched vs plain GPU"
+
+
+def run_batch(args):
+    """Batched form: 96 lattices of log-uniform size 2k-150k nodes (built like the 40x40 case, own
+    seeds), 2-4 thresholds each from {400, 800, 1200, 1600, 3200, 4800} m, every node a source of a
+    shortest-path job (closeness + betweenness) and of a segment job.  `value` replays the captured
+    batched launch (CUDA graph) with everything resident; `plain` runs the same jobs as per-graph
+    C-ABI calls of the plain path (each with its own plan and a workspace re-initialised in place),
+    also resident and timed with CUDA events on the same stream."""
+    import torch
+
+    from cityseer_gb300 import _native, centrality, device, synth
+    from cityseer_gb300.batch import Batch
+    from cityseer_gb300.common import pair_distances_betas_time
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    lib = _native.load()
+    t0 = time.perf_counter()
+    work = synth.batch_workload(n_graphs=args.graphs)
+    graphs = [(synth.primal_structure(p), d) for p, d in work]
+    t_build = time.perf_counter() - t0
+    jobs = []
+    for ns, dists in graphs:
+        jobs.append(dict(ns=ns, mode="shortest", distances=dists))
+        jobs.append(dict(ns=ns, mode="segment", distances=dists))
+    t0 = time.perf_counter()
+    b = Batch(jobs, tune=False)
+    t_setup = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    # ---- batched: one captured graph = zero outputs + header reset + one persistent launch + prefixes
+    b.capture()
+    for _ in range(args.warmup):
+        b.replay()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.graph.replay()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1000.0)
+    overflowed, done = b.status()
+    clk = clocks.stop()
+    if overflowed:
+        b.replay()  # re-run with in-call retry so the parity check below sees complete results
+    t_batch = float(np.mean(times))
+    counters = centrality.last_counters()
+    batched_rows = [jb["out"].clone() for jb in b.jobs]
+    # e2e of the batched form: replay + every job's result rows device->host
+    e2e = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.graph.replay()
+        host_rows = [jb["out"].cpu() for jb in b.jobs]
+        e2e.append(time.perf_counter() - t0)
+    d2h = sum(r.numel() * 8 for r in host_rows)
+    # ---- plain: per-graph calls of the plain C-ABI path, resident inputs and outputs
+    plain_jobs = []
+    ws_bytes = 0
+    for j, spec in enumerate(jobs):
+        ns = spec["ns"]
+        mode = 0 if spec["mode"] == "shortest" else 1
+        jb = b.jobs[j]
+        csr = jb["csr"]
+        d, bb, s = pair_distances_betas_time(1.33333, distances=spec["distances"])
+        r = centrality.estimate_reach(ns, csr, 1.33333, max(s))
+        cap = int(min(csr.n_bound, max(1024, -(-int(r * 1.3) // 256) * 256)))
+        plan = device.plan_primal(csr, mode, len(d), 1.33333, cap=cap, mem_budget=centrality._mem_budget(dev))
+        ws_bytes = max(ws_bytes, int(plan.workspace_bytes))
+        q = centrality._make_query(d, bb, s, 1.33333, float(centrality.TIE_EPSILON), True, True, False,
+                                   jb["keep"][0], jb["keep"][1], jb["keep"][2])
+        out = torch.zeros_like(jb["out"])
+        plain_jobs.append((mode, csr.struct(1.33333), q, plan, csr.n_bound, out))
+    del b.graph
+    b.graph = None
+    torch.cuda.empty_cache()
+    wsbuf = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+
+    def plain_pass():
+        for mode, g, q, plan, nb, out in plain_jobs:
+            out.zero_()
+            _native.check(lib.cs_workspace_init(C.byref(plan), nb, wsbuf.data_ptr(), ws_bytes, stream.cuda_stream),
+                          "cs_workspace_init")
+            fn = lib.cs_centrality_shortest if mode == 0 else lib.cs_segment_centrality
+            _native.check(fn(C.byref(g), C.byref(q), C.byref(plan), wsbuf.data_ptr(), ws_bytes,
+                             _native.Outputs(out.data_ptr(), None), stream.cuda_stream), "plain call")
+
+    plain_pass()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ptimes = []
+    for _ in range(max(1, args.plain_steps)):
+        e0.record(stream)
+        plain_pass()
+        e1.record(stream)
+        e1.synchronize()
+        ptimes.append(e0.elapsed_time(e1) / 1000.0)
+    t_plain = float(np.mean(ptimes))
+    # ---- parity guard: every job's batched rows equal its plain rows (order-of-summation tolerance)
+    worst = 0.0
+    for (mode, g, q, plan, nb, out), rows in zip(plain_jobs, batched_rows):
+        a, c = rows.double(), out.double()
+        if mode == 0:
+            assert torch.equal(a[0], c[0]), "batched density differs from the plain call"
+        worst = max(worst, float(((a - c).abs() / c.abs().clamp_min(1e-3)).max()))
+    assert worst < 1e-6, f"batched rows differ from plain rows (rel {worst})"
+    n_items = b.n_items
+    n_nodes = sum(ns.node_count() for ns, _ in graphs)
+    line = {
+        "metric": BATCH_METRIC,
+        "value": n_items / t_batch,
+        "unit": UNIT,
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_batch * 1000.0,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded jittered lattices, cityseer_gb300/synth.py batch_workload)",
+        "config": {
+            "workload": f"batch{len(graphs)}_mixed_2k_150k",
+            "graphs": len(graphs),
+            "jobs": len(jobs),
+            "nodes_total": n_nodes,
+            "items_per_step": n_items,
+            "l2": "inputs larger than L2 (workspace + 96 graphs)",
+            "slots": int(b.plan.n_slots),
+            "cap": int(b.plan.cap),
+            "variant": int(b.plan.variant),
+        },
+        "plain": {"value": n_items / t_plain, "ms_per_step": t_plain * 1000.0, "launch_calls": len(plain_jobs)},
+        "batched_over_plain": t_plain / t_batch,
+        "e2e": {"value": n_items / float(np.min(e2e)), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(d2h)},
+        "edges_relaxed_per_s": counters[1] / t_batch,
+        "parity_max_rel": worst,
+        "setup_s": {"graphs": round(t_build, 2), "batch": round(t_setup, 2)},
+        "gpu_launches": 1 + sum(1 for jb in b.jobs if jb["mode"] == 0 and jb["closeness"]),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -379,8 +530,14 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "batch"],
+                    help="c2: the 202,500-node lattice (default); batch: the 96-graph batched form")
+    ap.add_argument("--graphs", type=int, default=96)
+    ap.add_argument("--plain-steps", type=int, default=1)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "batch" and args.impl != "reference":
+        run_batch(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -20,6 +20,7 @@ CS_ERR_CAPACITY = 2
 CS_ERR_CUDA = 3
 CS_ERR_TIMEOUT = 4
 CS_ERR_INTERNAL = 5
+CS_BATCH_ASYNC = 1
 
 _ptr = C.c_void_p
 
@@ -89,7 +90,32 @@ class Plan(C.Structure):
         ("blocks", C.c_int32),
         ("delta_seconds", C.c_float),
         ("lanes", C.c_int32),
+        ("variant", C.c_int32),
+        ("max_degree", C.c_int32),
         ("workspace_bytes", C.c_size_t),
+    ]
+
+
+class BatchJob(C.Structure):
+    _fields_ = [
+        ("g", PrimalGraph),
+        ("mode", C.c_int32),
+        ("k", C.c_int32),
+        ("distances", C.c_uint32 * MAX_K),
+        ("betas", C.c_float * MAX_K),
+        ("seconds", C.c_uint32 * MAX_K),
+        ("speed_m_s", C.c_float),
+        ("tolerance", C.c_float),
+        ("delta_seconds", C.c_float),
+        ("compute_closeness", C.c_int32),
+        ("compute_betweenness", C.c_int32),
+        ("n_sources", C.c_int32),
+        ("sources", _ptr),
+        ("src_wt", _ptr),
+        ("eligible", _ptr),
+        ("out", _ptr),
+        ("bucket", _ptr),
+        ("item_begin", C.c_int64),
     ]
 
 
@@ -145,6 +171,14 @@ SIGNATURES = {
         ],
     ),
     "cs_last_counters": (C.c_int32, [C.POINTER(C.c_int64)] * 4),
+    "cs_batch_prepare": (C.c_int32, [C.POINTER(BatchJob), C.c_int32, C.POINTER(C.c_int64)]),
+    "cs_batch_plan": (C.c_int32, [C.POINTER(BatchJob), C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.POINTER(Plan)]),
+    "cs_batch_run": (
+        C.c_int32,
+        [C.POINTER(BatchJob), _ptr, C.c_int32, C.POINTER(Plan), _ptr, C.c_size_t, C.c_int32, _ptr],
+    ),
+    "cs_batch_status": (C.c_int32, [_ptr, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _ptr]),
+    "cs_abi_sizes": (C.c_int32, [_ptr, C.c_int32]),
     "cs_device_sm_count": (C.c_int32, []),
     "cs_last_phase_cycles": (C.c_int32, [_ptr, C.c_int32]),
     "cs_centrality_shortest_noalloc": (
@@ -186,6 +220,11 @@ def load(auto_build: bool = True) -> C.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        sizes = (C.c_int32 * 6)()
+        lib.cs_abi_sizes(sizes, 6)
+        want = [C.sizeof(t) for t in (PrimalGraph, DualGraph, Query, Plan, Outputs, BatchJob)]
+        if list(sizes) != want:
+            raise RuntimeError(f"libcsgpu.so struct layouts {list(sizes)} differ from the binding's {want}")
         _lib = lib
         return lib
 

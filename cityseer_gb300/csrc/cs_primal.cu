@@ -907,6 +907,66 @@ __device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, in
 // ------------------------------------------------------------------------------------------
 // Persistent kernel: each warp owns one scratch slot and pulls sources until the list is empty.
 // ------------------------------------------------------------------------------------------
+// One source on this warp's slot: search, sort, mode-specific accumulation, scratch reset.
+// Returns false when the source overflowed the slot's capacity (recorded for the retry).
+template <int PM>
+__device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs &s, int li, int src, uint32_t *hist,
+                                           int *cnt, long long *ph, long long &relaxed, long long &settled) {
+    const int lane = lane_id();
+    long long t0 = clock64();
+    const int R = warp_search(p, s, src, relaxed);
+    phase_mark(ph, 0, t0);
+    if (R < 0) {
+        // Reach exceeded this slot's capacity: the reached list lost track of touched entries, so
+        // reset the slot's whole dense state, record the source for the full-capacity retry and
+        // carry on with the next source.
+        for (int j = lane; j < p.g.n_bound; j += 32) {
+            s.dist[j] = __int_as_float(INF_BITS);
+            s.aux[j] = 0u;
+        }
+        if (lane == 0) {
+            const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
+            if (f < (unsigned)p.fail_cap) p.failed[f] = li;
+            else raise_err(p.hdr, CS_ERR_CAPACITY, 8);
+        }
+        __syncwarp();
+        return false;
+    }
+    warp_sort(s, R, hist);
+    __syncwarp();
+    for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+    __syncwarp();
+    phase_mark(ph, 1, t0);
+    if (p.mode == MODE_SHORTEST) shortest_accumulate<PM>(p, s, src, R, ph, cnt);
+    else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
+    else tree_rows<PM>(p, s, li, R);
+    __syncwarp();
+    t0 = clock64();
+    for (int i = lane; i < R; i += 32) {
+        const int v = s.ord[i];
+        s.dist[v] = __int_as_float(INF_BITS);
+        s.aux[v] = 0u;
+    }
+    __syncwarp();
+    phase_mark(ph, 6, t0);
+    settled += R;
+    return true;
+}
+
+__device__ __forceinline__ void flush_counters(const PrimalParams &p, long long *ph, long long relaxed,
+                                               long long settled, long long done_src) {
+    const long long rsum = warp_sum_ll(relaxed);
+    if (lane_id() == 0) {
+        for (int q = 0; q < 8; q++) atomicAdd(&p.hdr->pad[q], (unsigned long long)ph[q]);
+        atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
+        atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
+        atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Persistent kernel: each warp owns one scratch slot and pulls sources until the list is empty.
+// ------------------------------------------------------------------------------------------
 template <int PM, int MINB>
 __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p) {
     __shared__ uint32_t hist_all[8][256];
@@ -915,7 +975,6 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
     if (slot >= p.n_slots) return;
-    uint32_t *hist = hist_all[wib];
     const SlotPtrs s = slot_ptrs(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.P, p.L, slot, p.g.n_bound);
     long long relaxed = 0, settled = 0, done_src = 0;
     long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -926,53 +985,87 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
         if (idx >= (unsigned long long)p.n_src) break;
         if (__ldcg(&p.hdr->err) != 0u) break;
         const int li = p.remap ? p.remap[idx] : (int)idx;
-        const int src = p.src_list[li];
-        long long t0 = clock64();
-        const int R = warp_search(p, s, src, relaxed);
-        phase_mark(ph, 0, t0);
-        if (R < 0) {
-            // Reach exceeded this slot's capacity: the reached list lost track of touched entries,
-            // so reset the slot's whole dense state, record the source for the full-capacity retry
-            // and carry on with the next source.
-            for (int j = lane; j < p.g.n_bound; j += 32) {
-                s.dist[j] = __int_as_float(INF_BITS);
-                s.aux[j] = 0u;
-            }
-            if (lane == 0) {
-                const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
-                if (f < (unsigned)p.fail_cap) p.failed[f] = li;
-                else raise_err(p.hdr, CS_ERR_CAPACITY, 8);
-            }
-            __syncwarp();
-            continue;
-        }
-        warp_sort(s, R, hist);
-        __syncwarp();
-        for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
-        __syncwarp();
-        phase_mark(ph, 1, t0);
-        if (p.mode == MODE_SHORTEST) shortest_accumulate<PM>(p, s, src, R, ph, cnt_all[wib]);
-        else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
-        else tree_rows<PM>(p, s, li, R);
-        __syncwarp();
-        t0 = clock64();
-        for (int i = lane; i < R; i += 32) {
-            const int v = s.ord[i];
-            s.dist[v] = __int_as_float(INF_BITS);
-            s.aux[v] = 0u;
-        }
-        __syncwarp();
-        phase_mark(ph, 6, t0);
-        settled += R;
-        done_src += 1;
+        if (run_source<PM>(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled)) done_src++;
     }
-    const long long rsum = warp_sum_ll(relaxed);
-    if (lane == 0) {
-        for (int q = 0; q < 8; q++) atomicAdd(&p.hdr->pad[q], (unsigned long long)ph[q]);
-        atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
-        atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
-        atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
+    flush_counters(p, ph, relaxed, settled, done_src);
+}
+
+// ------------------------------------------------------------------------------------------
+// Batched persistent kernel: one launch over the (job, source) items of many graphs, thresholds
+// and modes.  Item i belongs to the job whose item_begin is the largest <= i.  Every warp's slot
+// is sized for the largest graph, capacity and lane count of the batch.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ int job_of(const cs_batch_job *jobs, int n_jobs, long long item) {
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].item_begin <= item) lo = mid;
+        else hi = mid - 1;
     }
+    return lo;
+}
+
+__device__ __forceinline__ void job_params(const PrimalParams &base, const cs_batch_job &j, PrimalParams &p) {
+    p = base;
+    p.g = j.g;
+    p.k = j.k;
+    uint32_t maxs = 0;
+    for (int i = 0; i < MAXK; i++) {
+        p.dk[i] = i < j.k ? (float)j.distances[i] : 0.0f;
+        p.beta[i] = i < j.k ? j.betas[i] : 0.0f;
+        if (i < j.k) maxs = max(maxs, j.seconds[i]);
+    }
+    p.maxsec = (float)maxs;
+    p.speed = j.speed_m_s;
+    p.tol = j.tolerance;
+    p.delta = j.delta_seconds > 0.0f ? j.delta_seconds : fmaxf(1.0f, p.maxsec / 48.0f);
+    p.closeness = j.compute_closeness;
+    p.betweenness = j.compute_betweenness;
+    p.track_reach = 0;
+    p.src_list = j.sources_dev;
+    p.n_src = j.n_sources;
+    p.src_wt = j.src_wt_dev;
+    p.eligible = j.eligible_dev;
+    p.out = j.out_dev;
+    p.bucket = j.bucket_dev;
+    p.mode = j.mode;
+}
+
+template <int PM, int MINB>
+__global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams base, const cs_batch_job *jobs,
+                                                          int n_jobs, long long n_items) {
+    __shared__ uint32_t hist_all[8][256];
+    __shared__ int cnt_all[8][2 * MAXK];
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
+    if (slot >= base.n_slots) return;
+    // slot geometry from the batch maxima (base.g.n_bound = largest graph)
+    const SlotPtrs s = slot_ptrs(base.dense, base.dense_stride, base.compact, (size_t)base.cap, base.P, base.L, slot,
+                                 base.g.n_bound);
+    long long relaxed = 0, settled = 0, done_src = 0;
+    long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    PrimalParams p;
+    int cur_job = -1;
+    while (true) {
+        unsigned long long idx = 0;
+        if (lane == 0) idx = atomicAdd(base.rerun ? &base.hdr->work_next2 : &base.hdr->work_next, 1ull);
+        idx = __shfl_sync(FULL, idx, 0);
+        const long long n = base.rerun ? base.n_src : n_items;
+        if ((long long)idx >= n) break;
+        if (__ldcg(&base.hdr->err) != 0u) break;
+        const long long item = base.remap ? (long long)base.remap[idx] : (long long)idx;
+        const int jb = job_of(jobs, n_jobs, item);
+        if (jb != cur_job) {
+            job_params(base, jobs[jb], p);
+            cur_job = jb;
+        }
+        const int li = (int)(item - jobs[jb].item_begin);
+        // failures record the global item index
+        if (run_source<PM>(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled))
+            done_src++;
+    }
+    flush_counters(base, ph, relaxed, settled, done_src);
 }
 
 __global__ void fill_dense_kernel(char *dense, size_t dense_stride, int n_bound, const int32_t *slots, int n_list,
@@ -1060,16 +1153,18 @@ cs_status validate_primal(const cs_primal_graph *g) {
     return CS_OK;
 }
 
-// register budget of the P <= 8 kernel: 3 (default, 80 registers) or 2 (128 registers) resident
-// 256-thread blocks per SM; CS_MIN_BLOCKS_PER_SM=2 selects the larger budget
-int min_blocks_variant() {
+// Register budget of the P <= 8 kernels: 3 resident 256-thread blocks per SM (80 registers) or 2
+// (128 registers).  A plan's variant field selects it; 0 means the default (3), which the
+// environment variable CS_MIN_BLOCKS_PER_SM=2 overrides.
+int resolve_variant(const cs_plan *plan) {
+    if (plan && (plan->variant == 2 || plan->variant == 3)) return plan->variant;
     const char *e = getenv("CS_MIN_BLOCKS_PER_SM");
     return (e && e[0] == '2') ? 2 : 3;
 }
 
-cudaError_t occupancy_blocks(int P, int *bpsm) {
+cudaError_t occupancy_blocks(int P, int variant, int *bpsm) {
     if (P > 8) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<CS_MAX_DEGREE, 2>, 256, 0);
-    if (min_blocks_variant() == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 3>, 256, 0);
+    if (variant == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 3>, 256, 0);
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 2>, 256, 0);
 }
 
@@ -1078,8 +1173,8 @@ cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, c
     const int wpb = tpb / 32;
     const int blocks = (n_slots + wpb - 1) / wpb;
     p.n_slots = n_slots;
-    const int minb = min_blocks_variant();
-    if (p.g.max_out_degree <= 8) {
+    const int minb = resolve_variant(plan);
+    if (p.P <= 8) {
         if (minb == 3) cs::primal_kernel<8, 3><<<blocks, tpb, 0, stream>>>(p);
         else cs::primal_kernel<8, 2><<<blocks, tpb, 0, stream>>>(p);
     } else {
@@ -1088,6 +1183,23 @@ cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, c
     g_counters[3]++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "primal_kernel launch");
+    return CS_OK;
+}
+
+cs_status launch_batch(cs::PrimalParams &p, const cs_plan *plan, const cs_batch_job *jobs_dev, int n_jobs,
+                       long long n_items, int n_slots, cudaStream_t stream) {
+    const int blocks = (n_slots + 7) / 8;
+    p.n_slots = n_slots;
+    const int minb = resolve_variant(plan);
+    if (p.P <= 8) {
+        if (minb == 3) cs::batch_kernel<8, 3><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, n_items);
+        else cs::batch_kernel<8, 2><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, n_items);
+    } else {
+        cs::batch_kernel<CS_MAX_DEGREE, 2><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, n_items);
+    }
+    g_counters[3]++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "batch_kernel launch");
     return CS_OK;
 }
 
@@ -1226,11 +1338,12 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
 }
 
 cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t budget, cs_plan *plan) {
+    const int variant = resolve_variant(plan);
     if (!plan) return fail(CS_ERR_ARG, "plan is NULL");
     int sms = sm_count();
     if (sms <= 0) return fail(CS_ERR_CUDA, "no CUDA device");
     int bpsm = 0;
-    cudaError_t e = occupancy_blocks(P, &bpsm);
+    cudaError_t e = occupancy_blocks(P, variant, &bpsm);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
     if (bpsm < 1) bpsm = 1;
     int slots = sms * bpsm * 8;
@@ -1248,6 +1361,8 @@ cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t
     plan->blocks = (slots + 7) / 8;
     if (plan->delta_seconds != plan->delta_seconds) plan->delta_seconds = 0.0f;
     plan->lanes = L;
+    plan->variant = variant;
+    plan->max_degree = P;
     plan->workspace_bytes = total_for(slots);
     return CS_OK;
 }
@@ -1401,7 +1516,7 @@ extern "C" cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, co
     int sms = sm_count();
     if (sms <= 0) return fail(CS_ERR_CUDA, "no CUDA device");
     int bpsm = 0;
-    cudaError_t e = occupancy_blocks(P, &bpsm);
+    cudaError_t e = occupancy_blocks(P, resolve_variant(nullptr), &bpsm);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
     int slots = std::max(1, sms * std::max(1, bpsm) * 8);
     while (slots > 1 && layout(g->n_bound, slots, cap, P, L).total > kNoAllocScratchBytes) {
@@ -1419,6 +1534,8 @@ extern "C" cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, co
     plan.blocks = (slots + 7) / 8;
     plan.delta_seconds = 0.0f;
     plan.lanes = L;
+    plan.variant = resolve_variant(nullptr);
+    plan.max_degree = P;
     const Layout lay = layout(g->n_bound, slots, cap, P, L);
     plan.workspace_bytes = lay.total;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1429,4 +1546,162 @@ extern "C" cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, co
     if (st != CS_OK) return st;
     return run_primal(g, q, &plan, ws, kNoAllocScratchBytes, out, stream, cs::MODE_SHORTEST, 0, nullptr, nullptr,
                       nullptr, nullptr, nullptr, 0, 0, 0.0f);
+}
+
+// ==========================================================================================
+// Batched persistent form (cs_batch_*).
+// ==========================================================================================
+namespace {
+struct BatchShape {
+    int max_n, P, L;
+};
+
+cs_status batch_shape(const cs_batch_job *jobs, int n_jobs, BatchShape &b) {
+    if (!jobs || n_jobs <= 0) return fail(CS_ERR_ARG, "empty batch");
+    b.max_n = 1;
+    b.P = 1;
+    b.L = 1;
+    for (int j = 0; j < n_jobs; j++) {
+        cs_status st = validate_primal(&jobs[j].g);
+        if (st != CS_OK) return st;
+        if (jobs[j].mode != cs::MODE_SHORTEST && jobs[j].mode != cs::MODE_SEGMENT)
+            return fail(CS_ERR_ARG, "batch job mode must be 0 (shortest) or 1 (segment)");
+        if (jobs[j].k < 1 || jobs[j].k > CS_MAX_THRESHOLDS) return fail(CS_ERR_ARG, "threshold count out of range");
+        if (!(jobs[j].speed_m_s > 0.0f)) return fail(CS_ERR_ARG, "speed_m_s must be finite and positive");
+        if (!jobs[j].out_dev) return fail(CS_ERR_ARG, "job without out_dev");
+        if (jobs[j].mode == cs::MODE_SHORTEST && jobs[j].compute_closeness && !jobs[j].bucket_dev)
+            return fail(CS_ERR_ARG, "shortest job with closeness needs bucket_dev");
+        b.max_n = std::max(b.max_n, jobs[j].g.n_bound);
+        b.P = std::max(b.P, jobs[j].g.max_out_degree);
+        b.L = std::max(b.L, lanes_for(jobs[j].mode, jobs[j].k));
+    }
+    return CS_OK;
+}
+}  // namespace
+
+extern "C" {
+
+cs_status cs_batch_prepare(cs_batch_job *jobs_host, int32_t n_jobs, int64_t *n_items) {
+    if (!jobs_host || n_jobs <= 0 || !n_items) return fail(CS_ERR_ARG, "empty batch");
+    int64_t acc = 0;
+    for (int j = 0; j < n_jobs; j++) {
+        jobs_host[j].item_begin = acc;
+        acc += std::max(0, jobs_host[j].n_sources);
+    }
+    *n_items = acc;
+    return CS_OK;
+}
+
+cs_status cs_batch_plan(const cs_batch_job *jobs_host, int32_t n_jobs, int32_t cap, int32_t max_slots,
+                        int64_t mem_budget_bytes, cs_plan *plan) {
+    BatchShape b;
+    cs_status st = batch_shape(jobs_host, n_jobs, b);
+    if (st != CS_OK) return st;
+    return plan_common(b.max_n, b.P, b.L, cap, max_slots, mem_budget_bytes, plan);
+}
+
+cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_dev, int32_t n_jobs, const cs_plan *plan,
+                       void *ws, size_t ws_bytes, int32_t flags, void *stream_v) {
+    BatchShape b;
+    cs_status st = batch_shape(jobs_host, n_jobs, b);
+    if (st != CS_OK) return st;
+    if (!plan || !ws || !jobs_dev) return fail(CS_ERR_ARG, "plan/workspace/jobs_dev is NULL");
+    if (plan->lanes < b.L) return fail(CS_ERR_ARG, "plan was made for fewer lanes");
+    const int P = std::max(1, plan->max_degree);
+    if (P < b.P) return fail(CS_ERR_ARG, "plan was made for a smaller degree");
+    const Layout lay = layout(b.max_n, plan->n_slots, plan->cap, P, plan->lanes);
+    if (ws_bytes < lay.total) return fail(CS_ERR_ARG, "workspace too small for this plan");
+    long long n_items = 0;
+    for (int j = 0; j < n_jobs; j++) {
+        if (jobs_host[j].item_begin != n_items) return fail(CS_ERR_ARG, "jobs not prepared (cs_batch_prepare)");
+        n_items += std::max(0, jobs_host[j].n_sources);
+    }
+    cudaStream_t stream = (cudaStream_t)stream_v;
+    char *base = (char *)ws;
+    cs::PrimalParams p;
+    memset(&p, 0, sizeof(p));
+    p.g.n_bound = b.max_n;  // slot geometry only; each job brings its own graph
+    p.hdr = (cs::WsHeader *)(base + lay.hdr_off);
+    p.failed = (int32_t *)(base + lay.failed_off);
+    p.fail_cap = lay.fail_cap;
+    p.dense = base + lay.dense_off;
+    p.dense_stride = lay.dense_stride;
+    p.compact = base + lay.compact_off;
+    p.cap = plan->cap;
+    p.P = P;
+    p.L = plan->lanes;
+    g_counters[0] = g_counters[1] = g_counters[2] = g_counters[3] = 0;
+    cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), stream);
+    for (int j = 0; j < n_jobs && e == cudaSuccess; j++)
+        if (jobs_host[j].mode == cs::MODE_SHORTEST && jobs_host[j].compute_closeness)
+            e = cudaMemsetAsync(jobs_host[j].bucket_dev, 0,
+                                sizeof(double) * 3 * (size_t)jobs_host[j].k * (size_t)jobs_host[j].g.n_bound, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "batch reset");
+    if (n_items == 0) return CS_OK;
+    st = launch_batch(p, plan, jobs_dev, n_jobs, n_items, plan->n_slots, stream);
+    if (st != CS_OK) return st;
+    if (!(flags & CS_BATCH_ASYNC)) {
+        cs::WsHeader h;
+        e = cudaMemcpyAsync(&h, p.hdr, sizeof(h), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_fail(e, "batch kernel");
+        if (h.err != 0u) return fail((cs_status)h.err, "device-side check failed (code " + std::to_string(h.err) + ")");
+        if (h.n_failed > 0u) {
+            const int nf = (int)std::min<unsigned>(h.n_failed, (unsigned)lay.fail_cap);
+            const size_t per = cs::compact_bytes((size_t)b.max_n, P, plan->lanes);
+            int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
+            slots2 = std::max(1, std::min(slots2, nf));
+            cs::PrimalParams p2 = p;
+            p2.cap = b.max_n;
+            p2.rerun = 1;
+            p2.remap = p.failed;
+            p2.n_src = nf;
+            st = launch_batch(p2, plan, jobs_dev, n_jobs, n_items, slots2, stream);
+            if (st != CS_OK) return st;
+            e = cudaMemcpyAsync(&h, p.hdr, sizeof(h), cudaMemcpyDeviceToHost, stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess) return cuda_fail(e, "batch retry kernel");
+            if (h.err != 0u) return fail((cs_status)h.err, "device-side check failed in retry");
+        }
+        g_counters[0] = (long long)h.sources_done;
+        g_counters[1] = (long long)h.edges_relaxed;
+        g_counters[2] = (long long)h.nodes_settled;
+    }
+    for (int j = 0; j < n_jobs; j++) {
+        const cs_batch_job &jb = jobs_host[j];
+        if (jb.mode == cs::MODE_SHORTEST && jb.compute_closeness && jb.n_sources > 0) {
+            int blocks = std::max(1, std::min((jb.g.n_bound + 255) / 256, std::max(1, sm_count()) * 8));
+            cs::bucket_prefix_kernel<<<blocks, 256, 0, stream>>>(jb.bucket_dev, jb.out_dev, jb.k, jb.g.n_bound);
+            g_counters[3]++;
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return cuda_fail(e, "bucket_prefix_kernel launch");
+        }
+    }
+    return CS_OK;
+}
+
+cs_status cs_batch_status(void *ws, int64_t *n_overflowed, int64_t *sources_done, void *stream) {
+    if (!ws) return fail(CS_ERR_ARG, "workspace is NULL");
+    cs::WsHeader h;
+    cudaError_t e = cudaMemcpyAsync(&h, ws, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "batch status");
+    if (n_overflowed) *n_overflowed = (int64_t)h.n_failed;
+    if (sources_done) *sources_done = (int64_t)h.sources_done;
+    g_counters[0] = (long long)h.sources_done;
+    g_counters[1] = (long long)h.edges_relaxed;
+    g_counters[2] = (long long)h.nodes_settled;
+    if (h.err != 0u) return fail((cs_status)h.err, "device-side check failed (code " + std::to_string(h.err) + ")");
+    return CS_OK;
+}
+
+}  // extern "C"
+
+extern "C" cs_status cs_abi_sizes(int32_t *out, int32_t n) {
+    // sizes of the public structs, for bindings to check their layouts against
+    const int32_t v[6] = {(int32_t)sizeof(cs_primal_graph), (int32_t)sizeof(cs_dual_graph), (int32_t)sizeof(cs_query),
+                          (int32_t)sizeof(cs_plan), (int32_t)sizeof(cs_outputs), (int32_t)sizeof(cs_batch_job)};
+    if (!out) return fail(CS_ERR_ARG, "out is NULL");
+    for (int i = 0; i < n && i < 6; i++) out[i] = v[i];
+    return CS_OK;
 }

@@ -224,10 +224,11 @@ class Workspace:
 
 
 def plan_primal(csr: PrimalCSR, mode: int, k: int, speed: float, cap: int = 0, max_slots: int = 0,
-                mem_budget: int = 0, delta: float = 0.0) -> _native.Plan:
+                mem_budget: int = 0, delta: float = 0.0, variant: int = 0) -> _native.Plan:
     lib = _native.load()
     plan = _native.Plan()
     plan.delta_seconds = delta
+    plan.variant = variant
     g = csr.struct(speed)
     rc = lib.cs_plan_primal(C.byref(g), mode, k, cap, max_slots, mem_budget, C.byref(plan))
     _native.check(rc, "cs_plan_primal")

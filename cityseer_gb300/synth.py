@@ -222,3 +222,23 @@ def lattice_config(name: str, side: int | None = None):
     if side is not None:
         cfg["side"] = side
     return lattice(**cfg), dists
+
+
+BATCH_THRESHOLDS = (400, 800, 1200, 1600, 3200, 4800)
+
+
+def batch_workload(n_graphs: int = 96, min_nodes: int = 2000, max_nodes: int = 150_000, seed: int = 4):
+    """Mixed-size workload of the batched form: `n_graphs` lattices built like "c1" (100 m, jitter
+    +-20 m, 15% of streets dropped), node counts log-uniform over [min_nodes, max_nodes] (side =
+    round(sqrt(N))), each with its own seed and 2-4 thresholds drawn from BATCH_THRESHOLDS.
+    Returns [(Primal, distances)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for g in range(n_graphs):
+        n = float(np.exp(rng.uniform(np.log(min_nodes), np.log(max_nodes))))
+        side = max(2, int(round(np.sqrt(n))))
+        k = int(rng.integers(2, 5))
+        dists = sorted(int(x) for x in rng.choice(BATCH_THRESHOLDS, size=k, replace=False))
+        p = lattice(side=side, spacing=100.0, jitter=20.0, drop=0.15, seed=10_000 + seed * 1000 + g)
+        out.append((p, dists))
+    return out

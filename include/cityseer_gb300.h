@@ -102,9 +102,34 @@ typedef struct {
     int32_t threads_per_block;
     int32_t blocks;
     float delta_seconds;  /* band width of the label-correcting search; <= 0 picks a default */
-    int32_t lanes;        /* f64 accumulator lanes per reached node */
+    int32_t lanes;        /* accumulator lanes per reached node */
+    int32_t variant;      /* register budget: 3 (default) or 2 resident 256-thread blocks per SM */
+    int32_t max_degree;   /* batches: largest out-degree over the jobs */
     size_t workspace_bytes;
 } cs_plan;
+
+/* One job of a batched launch: a graph, a mode, its thresholds, sources and outputs.  Many jobs of
+ * uneven size run in one persistent launch (cs_batch_run), each source an item of a device queue. */
+typedef struct {
+    cs_primal_graph g;
+    int32_t mode;             /* 0 = centrality_shortest, 1 = segment_centrality */
+    int32_t k;
+    uint32_t distances[CS_MAX_THRESHOLDS];
+    float betas[CS_MAX_THRESHOLDS];
+    uint32_t seconds[CS_MAX_THRESHOLDS];
+    float speed_m_s;
+    float tolerance;
+    float delta_seconds;      /* per-job band width (autotuned); <= 0: default */
+    int32_t compute_closeness;
+    int32_t compute_betweenness;
+    int32_t n_sources;
+    const int32_t *sources_dev;
+    const float *src_wt_dev;
+    const uint8_t *eligible_dev;
+    double *out_dev;          /* [7 (shortest) or 4 (segment)][k][n_bound], zeroed by the caller */
+    double *bucket_dev;       /* [3][k][n_bound] scratch for shortest closeness (zeroed by the launch) */
+    int64_t item_begin;       /* first queue item of this job (set by cs_batch_prepare) */
+} cs_batch_job;
 
 /* Outputs: f64 rows [metric][k][n_bound]; reach_dev: u32[k] (may be NULL when !track_reach). */
 typedef struct {
@@ -192,6 +217,23 @@ cs_status cs_tree_simplest(const cs_dual_graph *g, int32_t n_queries, const int3
                            int32_t row_cap, int32_t *count_dev, int32_t *node_dev, float *simpl_dev,
                            float *agg_seconds_dev, int32_t *pred_dev, void *stream);
 
+/* Batched persistent form (no reference counterpart: the reference runs one graph per call).
+ * cs_batch_prepare fills item_begin for jobs[0..n_jobs) (host array) and returns the item count.
+ * cs_batch_plan sizes one workspace for all jobs (largest graph, degree, lanes; cap = reach capacity).
+ * cs_batch_run enqueues the whole batch on `stream`: header and bucket resets, one persistent launch
+ * over every item, the closeness threshold prefix per job.  jobs_dev is a device copy of the prepared
+ * host array.  With flags & CS_BATCH_ASYNC the call neither synchronises nor retries (it can be
+ * captured in a CUDA graph); cs_batch_status then reports overflowed items, whose results are
+ * incomplete (rerun without CS_BATCH_ASYNC or with a larger cap).  Without the flag, overflowed
+ * items are redone at full capacity inside the call. */
+#define CS_BATCH_ASYNC 1
+cs_status cs_batch_prepare(cs_batch_job *jobs_host, int32_t n_jobs, int64_t *n_items);
+cs_status cs_batch_plan(const cs_batch_job *jobs_host, int32_t n_jobs, int32_t cap, int32_t max_slots,
+                        int64_t mem_budget_bytes, cs_plan *plan);
+cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_dev, int32_t n_jobs, const cs_plan *plan,
+                       void *workspace_dev, size_t workspace_bytes, int32_t flags, void *stream);
+cs_status cs_batch_status(void *workspace_dev, int64_t *n_overflowed, int64_t *sources_done, void *stream);
+
 /* Device counters of the last call on this thread: sources done, edges relaxed, nodes settled
  * (used for throughput and roofline accounting) and the number of kernels it launched. */
 cs_status cs_last_counters(int64_t *sources, int64_t *edges_relaxed, int64_t *nodes_settled, int64_t *launches);
@@ -199,6 +241,9 @@ cs_status cs_last_counters(int64_t *sources, int64_t *edges_relaxed, int64_t *no
 /* Per-phase SM cycles of the last call on this thread, summed over warps: 0 search, 1 sort,
  * 2 predecessor replay, 3 closeness, 4 sigma, 5 backward sweep, 6 scratch reset (n <= 8). */
 cs_status cs_last_phase_cycles(int64_t *cycles, int32_t n);
+
+/* sizeof of cs_primal_graph, cs_dual_graph, cs_query, cs_plan, cs_outputs, cs_batch_job (first n). */
+cs_status cs_abi_sizes(int32_t *out, int32_t n);
 
 /* Number of SMs of the current device (0 on failure). */
 int32_t cs_device_sm_count(void);
