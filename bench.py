@@ -520,6 +520,187 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+SERVE_METRIC = "served p50/p99 latency and sources/s, 6 resident graphs (50k-1.2M nodes), Poisson arrivals"
+
+
+def _serve_requests(prims, duals, rate: float, duration: float, seed: int):
+    """Poisson request stream: graph uniform, source subset log-uniform 1-8192 drawn uniformly,
+    1-4 thresholds with the maximum U(400, 5000) m, shortest w.p. 0.8 else simplest on the dual."""
+    from cityseer_gb300.serve import Query
+
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    idx = {g: np.asarray(ns.node_indices()) for g, ns in prims.items()}
+    didx = {g: np.asarray(ns.node_indices()) for g, ns in duals.items()}
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        gid = int(rng.integers(0, len(prims)))
+        simplest = bool(rng.random() < 0.2)
+        pool = didx[gid] if simplest else idx[gid]
+        size = min(len(pool), int(np.exp(rng.uniform(0.0, np.log(8192.0)))))
+        src = rng.choice(pool, size=size, replace=False)
+        k = int(rng.integers(1, 5))
+        dmax = int(rng.uniform(400, 5000))
+        dists = sorted(set([dmax] + [int(rng.uniform(100, dmax)) for _ in range(k - 1)]))
+        out.append((t, Query(gid, src.tolist(), dists, "simplest" if simplest else "shortest")))
+    return out
+
+
+def run_serve(args):
+    """Served form: 6 device-resident lattices (C1 recipe) of 50k-1.2M nodes plus their duals; Poisson
+    request streams at each rate; latency = arrival -> rows complete on the device.  Beside it, the
+    same 500 req/s stream as a serial loop of plain C-ABI calls (resident, one call per request)."""
+    import torch
+
+    from cityseer_gb300 import _native, centrality, dual, synth
+    from cityseer_gb300.common import pair_distances_betas_time
+    from cityseer_gb300.serve import Server, latency_summary
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    sizes = [int(x) for x in args.serve_sizes.split(",")]
+    t0 = time.perf_counter()
+    prims, duals = {}, {}
+    for gid, n in enumerate(sizes):
+        p = synth.lattice(side=int(round(np.sqrt(n))), spacing=100.0, jitter=20.0, drop=0.15, seed=500 + gid)
+        prims[gid] = synth.primal_structure(p)
+        duals[gid] = synth.dual_structure(p)
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    srv = Server(prims, duals, max_distance=5000, max_thresholds=4, keep_results=False)
+    t_setup = time.perf_counter() - t0
+    srv.start()
+    # warm-up: a few queries of each mode on each graph
+    from cityseer_gb300.serve import Query
+
+    warm = []
+    for gid in prims:
+        warm.append(srv.submit(Query(gid, list(range(0, 64)), [800, 5000], "shortest")))
+        warm.append(srv.submit(Query(gid, list(range(0, 8)), [800], "simplest")))
+    srv.drain(timeout=600)
+    rates = [float(x) for x in args.serve_rates.split(",")]
+    sweep = []
+    clocks = ClockSampler(0)
+    clocks.start()
+    streams = {}
+    for ri, rate in enumerate(rates):
+        reqs = _serve_requests(prims, duals, rate, args.serve_seconds, seed=900 + ri)
+        streams[rate] = reqs
+        tickets = []
+        start = time.perf_counter()
+        for at, q in reqs:
+            now = time.perf_counter() - start
+            if at > now:
+                time.sleep(at - now)
+            tickets.append(srv.submit(q, t_arrival=start + at))
+        saturated = False
+        try:
+            srv.drain(timeout=max(30.0, 10.0 * args.serve_seconds))
+        except TimeoutError:
+            saturated = True
+            srv.cancel()
+            srv.drain(timeout=900)
+        ok = [t for t in tickets if t.error is None]
+        end = max(t.t_done for t in ok) if ok else start
+        n_src = sum(len(t.query.sources) for t in ok)
+        errs = [t.error for t in tickets if t.error is not None and "cancelled" not in str(t.error)]
+        if errs:
+            raise errs[0]
+        sweep.append({
+            "rate_req_s": rate, "requests": len(reqs), "completed": len(ok), "saturated": saturated,
+            "sources": n_src, "sources_per_s": n_src / max(1e-9, end - start),
+            "all": latency_summary(ok), "le_1k_sources": latency_summary(ok, 1000),
+            "shortest": latency_summary([t for t in ok if t.query.mode == "shortest"]),
+            "simplest": latency_summary([t for t in ok if t.query.mode == "simplest"]),
+        })
+        if saturated:
+            break
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.stop()
+    dws = srv.dws
+    del srv
+    torch.cuda.empty_cache()
+    # ---- serial loop of plain calls on the 500 req/s stream (or the nearest rate)
+    rate_ser = min(streams, key=lambda r: abs(r - 500.0))
+    reqs = streams[rate_ser]
+    lib = _native.load()
+    speed = 1.33333
+    stream = torch.cuda.current_stream()
+    ws_p = {}
+    for gid, ns in prims.items():
+        csr = centrality._primal_csr(ns)
+        _, _, s5 = pair_distances_betas_time(speed, distances=[5000])
+        ws_p[gid] = centrality._workspace(ns, csr, 0, 4, speed, s5[0])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n_ser = 0
+    n_req_ser = 0
+    for _, q in reqs:
+        if time.perf_counter() - t0 > args.serial_seconds:
+            break
+        n_ser += len(q.sources)
+        n_req_ser += 1
+        d, b, s = pair_distances_betas_time(speed, distances=q.distances)
+        if q.mode == "shortest":
+            ns = prims[q.graph]
+            csr = centrality._primal_csr(ns)
+            g = csr.struct(speed)
+            ws = ws_p[q.graph]
+            nb = csr.n_bound
+            fn = lib.cs_centrality_shortest
+            rows = 7
+        else:
+            ns = duals[q.graph]
+            csr = dual.dual_csr(ns)
+            g = csr.struct(speed)
+            ws = dws
+            nb = csr.n_bound
+            fn = lib.cs_centrality_simplest
+            rows = 4
+        src_t = torch.tensor(q.sources, dtype=torch.int32, device=dev)
+        wt_t = torch.zeros(nb, dtype=torch.float32, device=dev)
+        el_t = torch.zeros(nb, dtype=torch.uint8, device=dev)
+        wt_t[src_t.long()] = 1.0
+        el_t[src_t.long()] = 1
+        out = torch.zeros((rows, len(d), nb), dtype=torch.float64, device=dev)
+        reach = torch.zeros(len(d), dtype=torch.int32, device=dev)
+        qq = centrality._make_query(d, b, s, speed, float(centrality.TIE_EPSILON), True, True, True, src_t, wt_t,
+                                    el_t)
+        _native.check(fn(C.byref(g), C.byref(qq), C.byref(ws.plan), ws.ptr, ws.nbytes,
+                         _native.Outputs(out.data_ptr(), reach.data_ptr()), stream.cuda_stream), "serial plain call")
+    torch.cuda.synchronize()
+    t_ser = time.perf_counter() - t0
+    at500 = next(x for x in sweep if x["rate_req_s"] == rate_ser)
+    line = {
+        "metric": SERVE_METRIC,
+        "value": at500["sources_per_s"],
+        "unit": "sources/s",
+        "n_gpus": 1,
+        "steps": len(rates),
+        "warmup": len(warm),
+        "ms_per_step": None,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded jittered lattices and their duals, Poisson request streams)",
+        "config": {"workload": "serve6_50k_1200k", "graph_nodes": [ns.node_count() for ns in prims.values()],
+                   "dual_nodes": [ns.node_count() for ns in duals.values()], "seconds_per_rate": args.serve_seconds,
+                   "latency": "arrival to result rows complete on the device", **st},
+        "sweep": sweep,
+        "serial_plain": {"rate_req_s": rate_ser, "requests": n_req_ser, "of": len(reqs),
+                         "sources_per_s": n_ser / t_ser, "seconds": t_ser},
+        "served_over_serial_sources_per_s": at500["sources_per_s"] / (n_ser / t_ser),
+        "p99_ms_le_1k_sources_at_rate": {str(x["rate_req_s"]): x["le_1k_sources"].get("p99_ms") for x in sweep},
+        "setup_s": {"graphs": round(t_build, 1), "server": round(t_setup, 1)},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -530,13 +711,20 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "batch"],
-                    help="c2: the 202,500-node lattice (default); batch: the 96-graph batched form")
+    ap.add_argument("--workload", default="c2", choices=["c2", "batch", "serve"],
+                    help="c2: the 202,500-node lattice (default); batch: the 96-graph batched form; "
+                         "serve: the served form")
+    ap.add_argument("--serve-sizes", default="50000,100000,200000,400000,800000,1200000")
+    ap.add_argument("--serve-rates", default="20,100,500,2000")
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serial-seconds", type=float, default=60.0)
     ap.add_argument("--graphs", type=int, default=96)
     ap.add_argument("--plain-steps", type=int, default=1)
     args = ap.parse_args()
     if args.workload == "batch" and args.impl != "reference":
         run_batch(args)
+    elif args.workload == "serve" and args.impl != "reference":
+        run_serve(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

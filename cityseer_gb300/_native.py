@@ -92,6 +92,7 @@ class Plan(C.Structure):
         ("lanes", C.c_int32),
         ("variant", C.c_int32),
         ("max_degree", C.c_int32),
+        ("n_bound", C.c_int32),
         ("workspace_bytes", C.c_size_t),
     ]
 
@@ -178,7 +179,11 @@ SIGNATURES = {
         [C.POINTER(BatchJob), _ptr, C.c_int32, C.POINTER(Plan), _ptr, C.c_size_t, C.c_int32, _ptr],
     ),
     "cs_batch_status": (C.c_int32, [_ptr, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _ptr]),
+    "cs_batch_failed": (C.c_int32, [_ptr, C.POINTER(Plan), C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int64),
+                                    _ptr]),
     "cs_abi_sizes": (C.c_int32, [_ptr, C.c_int32]),
+    "cs_last_retries": (C.c_int32, [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "cs_source_weights": (C.c_int32, [_ptr, C.c_int64, _ptr, C.c_int32, _ptr, _ptr, _ptr]),
     "cs_device_sm_count": (C.c_int32, []),
     "cs_last_phase_cycles": (C.c_int32, [_ptr, C.c_int32]),
     "cs_centrality_shortest_noalloc": (

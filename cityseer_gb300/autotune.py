@@ -27,12 +27,24 @@ def cache_path() -> Path:
     return Path(os.environ.get("CS_AUTOTUNE_CACHE", Path.home() / ".cache" / "cityseer_gb300" / "autotune.json"))
 
 
+_memo: dict = {}
+
+
 def _load() -> dict:
     p = cache_path()
     try:
-        return json.loads(p.read_text())
+        mt = p.stat().st_mtime_ns
+    except OSError:
+        return {}
+    hit = _memo.get(str(p))
+    if hit is not None and hit[0] == mt:
+        return hit[1]
+    try:
+        db = json.loads(p.read_text())
     except (OSError, ValueError):
         return {}
+    _memo[str(p)] = (mt, db)
+    return db
 
 
 def _store(db: dict) -> None:

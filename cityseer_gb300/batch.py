@@ -98,10 +98,9 @@ class Batch:
         _native.check(self.lib.cs_batch_plan(self.table, len(jobs), cap, max_slots, centrality._mem_budget(dev),
                                              C.byref(plan)), "cs_batch_plan")
         self.plan = plan
-        max_n = max(jb["csr"].n_bound for jb in self.jobs)
         from .device import Workspace
 
-        self.ws = Workspace(plan, max_n, dev)
+        self.ws = Workspace(plan, plan.n_bound, dev)
         self.graph = None
 
     def run(self, async_: bool = False, stream=None) -> None:
@@ -111,6 +110,9 @@ class Batch:
                                    self.ws.ptr, self.ws.nbytes, _native.CS_BATCH_ASYNC if async_ else 0, st)
         if rc != _native.CS_OK:
             self.ws.init(st)
+            for jb in self.jobs:
+                if jb["bucket"] is not None:
+                    jb["bucket"].zero_()
         _native.check(rc, "cs_batch_run")
 
     def zero_outputs(self) -> None:

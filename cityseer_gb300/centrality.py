@@ -192,7 +192,7 @@ def _primal_csr(ns) -> device.PrimalCSR:
 def drop_device_state(ns, keep_workspace: bool = True) -> None:
     """Forgets the device-resident CSR (and optionally the workspaces) of a graph."""
     for k in list(ns._cache):
-        if k == "primal_csr" or k == "dual_csr" or (not keep_workspace and isinstance(k, tuple) and k[0] == "ws"):
+        if k == "primal_csr" or k == "dual_csr" or (not keep_workspace and k in ("ws", "wsd")):
             del ns._cache[k]
 
 
@@ -230,21 +230,30 @@ def _mem_budget(device_: torch.device) -> int:
     return int(min(free * 0.6, 96 << 30))
 
 
+def _lanes_for(mode: int, k: int) -> int:
+    return 2 * k if mode == 0 else (k if mode == 1 else 1)
+
+
 def _workspace(ns, csr, mode: int, k: int, speed: float, max_seconds: int | None = None) -> device.Workspace:
+    """The graph's workspace, grown (never shrunk) to the lanes and reach capacity this call needs,
+    so calls that vary thresholds or modes reuse one allocation."""
     cap = 0
     if max_seconds is not None and mode != 2:
         r = estimate_reach(ns, csr, speed, max_seconds)
         cap = int(min(csr.n_bound, max(1024, -(-int(r * 1.3) // 256) * 256)))
-    key = ("ws", mode, k, cap)
-    ws = ns._cache.get(key)
-    if ws is None:
-        # free other workspaces of this graph first: they can be large
-        for kk in [kk for kk in ns._cache if isinstance(kk, tuple) and kk and kk[0] == "ws"]:
-            del ns._cache[kk]
-        torch.cuda.empty_cache()
-        plan = device.plan_primal(csr, mode, k, speed, cap=cap, mem_budget=_mem_budget(csr.device))
-        ws = device.Workspace(plan, csr.n_bound, csr.device)
-        ns._cache[key] = ws
+    need_l = _lanes_for(mode, k)
+    ws = ns._cache.get("ws")
+    if ws is not None and ws.plan.lanes >= need_l and ws.plan.cap >= cap:
+        return ws
+    if ws is not None:
+        need_l = max(need_l, int(ws.plan.lanes))
+        cap = max(cap, int(ws.plan.cap))
+        del ns._cache["ws"]
+        del ws
+    torch.cuda.empty_cache()
+    plan = device.plan_primal(csr, 0, (need_l + 1) // 2, speed, cap=cap, mem_budget=_mem_budget(csr.device))
+    ws = device.Workspace(plan, csr.n_bound, csr.device)
+    ns._cache["ws"] = ws
     return ws
 
 

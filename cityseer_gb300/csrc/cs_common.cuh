@@ -1,6 +1,8 @@
 // cs_common.cuh -- shared device helpers for the cityseer_gb300 kernels (sm_103a).
 #pragma once
+#include <chrono>
 #include <cstdint>
+#include <thread>
 #include <cuda_runtime.h>
 
 #include "../../include/cityseer_gb300.h"
@@ -66,6 +68,21 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 
 __device__ __forceinline__ void raise_err(WsHeader *h, unsigned code, unsigned where) {
     if (atomicCAS(&h->err, 0u, code) == 0u) h->err_where = where;
+}
+
+// Reads a workspace header after the work queued on `s`.  With poll, waits for the stream by
+// querying it between short sleeps first: a device->host copy into pageable memory issued while
+// long kernels are still queued holds driver resources until they finish, which stalls other host
+// threads' CUDA calls (allocations, event creation) for that long.
+inline cudaError_t read_header(const WsHeader *dev, WsHeader &h, cudaStream_t s, bool poll) {
+    cudaError_t e;
+    if (poll) {
+        while ((e = cudaStreamQuery(s)) == cudaErrorNotReady) std::this_thread::sleep_for(std::chrono::microseconds(20));
+        if (e != cudaSuccess) return e;
+    }
+    e = cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
 }
 
 }  // namespace cs

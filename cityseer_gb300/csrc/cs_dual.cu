@@ -32,6 +32,7 @@
 #include "cs_sort.cuh"
 
 extern "C" void cs_set_error_internal(const char *msg);
+extern "C" void cs_set_retries_internal(long long overflowed, long long inexact);
 
 namespace csd {
 using namespace cs;
@@ -126,8 +127,10 @@ struct DualParams {
     int32_t cap;
     int32_t n_slots;
     int32_t pass;  // 0 = label-correcting pass, 1 = full-capacity retry, 2 = exact heap pass
+    int32_t geo_n; // node bound the workspace's slot geometry was planned for (>= g.n_bound)
     const int32_t *remap;
     int32_t mode;
+    int32_t fail_final;  // an overflow at this capacity is an error (capacity = every state)
     int32_t force_exact;
     int32_t row_cap;
     int32_t *t_count, *t_node, *t_pred;
@@ -545,9 +548,18 @@ __device__ __forceinline__ int first_ks(const DualParams &p, float secs) {
 
 // Replay + sigma in route order.  Returns false (and sets mismatch) when the replay disagrees with
 // the search's keys.
-__device__ bool dual_replay(const DualParams &p, const DSlot &s, int src, int R, bool &bad) {
+// Returns 0 when the replay is exact, 1 when some replayed route differs from the search's key (the
+// keys are then rewritten with the replayed values, so that sorting them again gives the next
+// settle-order estimate), 2 when the replayed seconds would reach a state the search did not.
+__device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, bool &bad, bool rewrite) {
     const int lane = lane_id();
     bool mismatch = false;
+    // The replay recomputes every state's (route, seconds) from its offers in settle order, as the
+    // reference's heap search does.  Routes must equal the search's (then the settle order is the
+    // reference's).  Seconds may differ where near-tied offers arrived in another order: the
+    // reference's seconds are then never larger, so the replay is exact as long as no state the
+    // search left unreached is offered within the cutoff by the replayed seconds (checked below).
+    bool secs_diff = false;
     for (int base = 0; base < R; base += 32) {
         const int i = base + lane;
         const bool act = i < R;
@@ -600,9 +612,12 @@ __device__ bool dual_replay(const DualParams &p, const DSlot &s, int src, int R,
                 s.sig[i] = sg;
                 s.np[i] = (uint8_t)np;
                 const unsigned long long k = __ldcg(&s.key[V]);
-                if (__float_as_uint(route) != (unsigned)(k >> 32) ||
-                    __float_as_uint(secs) != (unsigned)(k & 0xffffffffull))
+                if (__float_as_uint(route) != (unsigned)(k >> 32)) {
                     mismatch = true;
+                    if (rewrite) s.key[V] = pack(route, secs);
+                } else if (__float_as_uint(secs) != (unsigned)(k & 0xffffffffull)) {
+                    secs_diff = true;
+                }
                 mine = true;
             }
             __syncwarp();
@@ -611,10 +626,27 @@ __device__ bool dual_replay(const DualParams &p, const DSlot &s, int src, int R,
         }
         if (done != FULL) {
             if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 21);
-            return false;
+            return 2;
         }
     }
-    return !__any_sync(FULL, mismatch);
+    if (__any_sync(FULL, mismatch)) return 1;
+    if (!__any_sync(FULL, secs_diff)) return 0;
+    __syncwarp();
+    // reach check with the replayed seconds: every in-cutoff offer must land on a reached state
+    bool escape = false;
+    for (int i = lane; i < R; i += 32) {
+        const int U = s.ord[i];
+        const int u = U >> 1, e = U & 1;
+        const float sU = s.sB[i];
+        const int beg = __ldg(&p.g.ptr_dev[u]), end = __ldg(&p.g.ptr_dev[u + 1]);
+        for (int ej = beg; ej < end; ej++) {
+            if (__ldg(&p.g.exit_slot_dev[ej]) != 1 - e) continue;
+            if (__fadd_rn(sU, __ldg(&p.g.w_dev[ej])) > p.maxsec) continue;
+            const int V = 2 * __ldg(&p.g.to_dev[ej]) + __ldg(&p.g.entry_slot_dev[ej]);
+            if (s.aux[V] == 0u) escape = true;
+        }
+    }
+    return __any_sync(FULL, escape) ? 2 : 0;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -768,7 +800,7 @@ __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
     if (slot >= p.n_slots) return;
-    const DSlot s = dslot(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.k, slot, p.g.n_bound);
+    const DSlot s = dslot(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.k, slot, p.geo_n);
     long long relaxed = 0, settled = 0, done_src = 0;
     const int N2 = 2 * p.g.n_bound;
     while (true) {
@@ -792,7 +824,7 @@ __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
                 s.aux[j] = 0u;
             }
             if (lane == 0) {
-                if (p.pass != 0) {
+                if (p.fail_final) {
                     raise_err(p.hdr, CS_ERR_CAPACITY, 27);  // full-capacity passes must not overflow
                 } else {
                     const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
@@ -803,13 +835,22 @@ __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
             __syncwarp();
             continue;
         }
-        if (!exact) warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb,
-                                    s.vb, s.rk, s.ord, hist_all[wib]);
-        __syncwarp();
-        for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
-        __syncwarp();
+        // Replay in settle order.  A search key can hold a route from an offer its offering state
+        // later withdrew (that state improved its route but its new seconds crossed the cutoff), so
+        // the first order is an estimate: replay, re-sort by the replayed routes, and replay again
+        // until the order is consistent (the reference's), else fall back to the exact search.
         bool bad = false;
-        const bool ok = dual_replay(p, s, src, R, bad);
+        int rr = 1;
+        for (int it = 0; it < (exact ? 1 : 4) && rr == 1; it++) {
+            if (!exact) warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb,
+                                        s.vb, s.rk, s.ord, hist_all[wib]);
+            __syncwarp();
+            for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+            __syncwarp();
+            rr = dual_replay(p, s, src, R, bad, !exact);
+            __syncwarp();
+        }
+        const bool ok = rr == 0;
         if (ok) {
             dual_accumulate(p, s, src, R, cnt_all[wib], bad);
         } else if (lane == 0) {
@@ -887,7 +928,8 @@ int dsm_count() {
 }
 
 struct DLayout {
-    size_t failed_off, inexact_off, bucket_off, dense_off, compact_off, compact_total, total, dense_stride;
+    size_t failed_off, failed2_off, inexact_off, bucket_off, dense_off, compact_off, compact_total, total,
+        dense_stride;
     int fail_cap;
 };
 
@@ -895,7 +937,8 @@ DLayout dlayout(int n_bound, int n_slots, int cap, int K) {
     DLayout l;
     l.fail_cap = std::max(n_slots, 1 << 18);
     l.failed_off = 256;
-    l.inexact_off = csd::al256(l.failed_off + 4 * (size_t)l.fail_cap);
+    l.failed2_off = csd::al256(l.failed_off + 4 * (size_t)l.fail_cap);
+    l.inexact_off = csd::al256(l.failed2_off + 4 * (size_t)l.fail_cap);
     l.bucket_off = csd::al256(l.inexact_off + 4 * (size_t)l.fail_cap);
     l.dense_off = csd::al256(l.bucket_off + sizeof(double) * 3 * (size_t)K * (size_t)n_bound);
     l.dense_stride = csd::al256((size_t)n_bound * 16) + csd::al256((size_t)n_bound * 8);
@@ -931,8 +974,7 @@ cs_status dlaunch(csd::DualParams &p, int n_slots, cudaStream_t s) {
 }
 
 cs_status dsync_header(cs::WsHeader *hd, cs::WsHeader &h, cudaStream_t s) {
-    cudaError_t e = cudaMemcpyAsync(&h, hd, sizeof(h), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaError_t e = cs::read_header(hd, h, s, true);
     if (e != cudaSuccess) return dcuda(e, "dual kernel");
     if (h.err != 0u)
         return dfail((cs_status)h.err, "device-side check failed (code " + std::to_string(h.err) + " at " +
@@ -968,6 +1010,7 @@ cs_status cs_plan_dual(const cs_dual_graph *g, int32_t mode, int32_t k, int32_t 
     plan->blocks = (plan->n_slots + 7) / 8;
     if (!(plan->delta_seconds > 0.0f)) plan->delta_seconds = 30.0f;  // band width in route degrees
     plan->lanes = k;
+    plan->n_bound = g->n_bound;
     plan->workspace_bytes = dlayout(g->n_bound, plan->n_slots, cap, k).total;
     return CS_OK;
 }
@@ -980,7 +1023,10 @@ cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, cons
     const int K = q->k;
     if (K < 1 || K > CS_MAX_THRESHOLDS) return dfail(CS_ERR_ARG, "threshold count out of range");
     if (plan->lanes < K) return dfail(CS_ERR_ARG, "plan was made for fewer thresholds");
-    const DLayout lay = dlayout(g->n_bound, plan->n_slots, plan->cap, plan->lanes);
+    // slot geometry is the plan's: one workspace serves every dual graph up to its node bound
+    const int geo_n = plan->n_bound > 0 ? plan->n_bound : g->n_bound;
+    if (geo_n < g->n_bound) return dfail(CS_ERR_ARG, "plan was made for a smaller graph");
+    const DLayout lay = dlayout(geo_n, plan->n_slots, plan->cap, plan->lanes);
     if (ws_bytes < lay.total) return dfail(CS_ERR_ARG, "workspace too small for this plan");
     if (!out.out_dev) return dfail(CS_ERR_ARG, "out_dev is NULL");
     if (q->track_reach && !out.reach_dev) return dfail(CS_ERR_ARG, "reach_dev required when track_reach");
@@ -990,6 +1036,7 @@ cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, cons
     csd::DualParams p;
     memset(&p, 0, sizeof(p));
     p.g = *g;
+    p.geo_n = geo_n;
     p.k = K;
     uint32_t maxs = 0;
     for (int i = 0; i < K; i++) {
@@ -1032,34 +1079,57 @@ cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, cons
     cs::WsHeader h;
     st = dsync_header(p.hdr, h, s);
     if (st != CS_OK) return st;
-    const size_t per_full = csd::compact_bytes_d(2 * (size_t)g->n_bound, K);
-    // pass 1: sources that overflowed their slot, at full capacity (label-correcting)
-    // pass 2: sources whose replay disagreed with the label-correcting search, exact heap order
-    for (int pass = 1; pass <= 2; pass++) {
-        const unsigned n_list = pass == 1 ? h.n_failed : h.n_inexact;
-        if (n_list == 0u) continue;
-        const int nl = (int)std::min<unsigned>(n_list, (unsigned)lay.fail_cap);
-        csd::DualParams p2 = p;
-        p2.pass = pass;
-        p2.cap = 2 * g->n_bound;
-        p2.remap = pass == 1 ? p.failed : p.inexact;
-        p2.n_src = nl;
-        if (pass == 2) {
-            // the exact pass writes new overflow / inexact entries nowhere: it cannot overflow at
-            // full capacity and its replay must agree
-            p2.inexact = p.failed;  // unused
+    // Sources that overflowed their slot run again at 4x the capacity (then 4x again, up to every
+    // state), each level on as many slots as the workspace's compact region holds at that
+    // capacity.  Sources whose replay disagreed with the search then run the exact heap search,
+    // starting at the plan's capacity.
+    const int N2 = 2 * g->n_bound;
+    int32_t *listA = p.failed;
+    int32_t *listB = (int32_t *)(base + lay.failed2_off);
+    long long n_retried = 0;
+    auto chain = [&](int pass, const int32_t *in, unsigned n_in, int cap0) -> cs_status {
+        int cap_l = std::min(N2, cap0);
+        const int32_t *list = in;
+        while (n_in > 0u) {
+            const bool final = cap_l >= N2;
+            int32_t *out_l = (list == listA) ? listB : listA;
+            csd::DualParams p2 = p;
+            p2.pass = pass;
+            p2.cap = cap_l;
+            p2.remap = list;
+            p2.n_src = std::min<unsigned>(n_in, (unsigned)lay.fail_cap);
+            p2.failed = out_l;
+            p2.fail_final = final ? 1 : 0;
+            cudaError_t e2 = cudaMemsetAsync(&p.hdr->work_next2, 0, sizeof(unsigned long long), s);
+            if (e2 == cudaSuccess) e2 = cudaMemsetAsync(&p.hdr->n_failed, 0, sizeof(unsigned), s);
+            if (e2 != cudaSuccess) return dcuda(e2, "retry counter reset");
+            const size_t per = csd::compact_bytes_d((size_t)cap_l, K);
+            int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
+            slots2 = std::max(1, std::min<int>(slots2, (int)p2.n_src));
+            cs_status st2 = dlaunch(p2, slots2, s);
+            if (st2 != CS_OK) return st2;
+            cs::WsHeader h2;
+            st2 = dsync_header(p.hdr, h2, s);
+            if (st2 != CS_OK) return st2;
+            n_retried += (long long)p2.n_src;
+            h.n_inexact = h2.n_inexact;  // label-correcting retries may add inexact sources
+            n_in = final ? 0u : h2.n_failed;
+            list = out_l;
+            cap_l = (int)std::min<long long>(N2, 4ll * cap_l);
         }
-        e = cudaMemsetAsync(&p.hdr->work_next2, 0, sizeof(unsigned long long), s);
-        if (e != cudaSuccess) return dcuda(e, "retry counter reset");
-        int slots2 = (int)std::min<size_t>(lay.compact_total / per_full, (size_t)plan->n_slots);
-        slots2 = std::max(1, std::min(slots2, nl));
-        st = dlaunch(p2, slots2, s);
+        return CS_OK;
+    };
+    const long long n_over = h.n_failed;
+    if (h.n_failed > 0u) {
+        st = chain(1, listA, h.n_failed, 4 * std::max(plan->cap, 16));
         if (st != CS_OK) return st;
-        cs::WsHeader h2;
-        st = dsync_header(p.hdr, h2, s);
-        if (st != CS_OK) return st;
-        if (pass == 1) h.n_inexact = h2.n_inexact;  // retries may add inexact sources
     }
+    const long long n_inexact = h.n_inexact;
+    if (h.n_inexact > 0u) {
+        st = chain(2, p.inexact, std::min<unsigned>(h.n_inexact, (unsigned)lay.fail_cap), plan->cap);
+        if (st != CS_OK) return st;
+    }
+    cs_set_retries_internal(n_over, n_inexact);
     if (p.closeness) {
         int blocks = std::max(1, std::min((g->n_bound + 255) / 256, dsm_count() * 8));
         csd::dual_bucket_prefix<<<blocks, 256, 0, s>>>(p.bucket, p.out, K, g->n_bound);

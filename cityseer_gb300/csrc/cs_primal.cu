@@ -681,6 +681,31 @@ __global__ void bucket_prefix_kernel(const double *bucket, double *out, int K, i
     }
 }
 
+// Batched form: the same prefix for every shortest-path job with closeness (blockIdx.y strides the
+// jobs), and the bucket is zeroed as it is read, so that buckets are zero between runs.
+__global__ void batch_prefix_kernel(const cs_batch_job *jobs, int n_jobs) {
+    for (int j = blockIdx.y; j < n_jobs; j += gridDim.y) {
+        const cs_batch_job &jb = jobs[j];
+        if (jb.mode != MODE_SHORTEST || !jb.compute_closeness || jb.n_sources <= 0) continue;
+        const int K = jb.k, N = jb.g.n_bound;
+        const size_t KN = (size_t)K * N;
+        double *bucket = jb.bucket_dev;
+        double *out = jb.out_dev;
+        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+            const int rows[3] = {0, 1, 3};
+            for (int m = 0; m < 3; m++) {
+                double acc = 0.0;
+                for (int k = 0; k < K; k++) {
+                    const size_t o = (size_t)m * KN + (size_t)k * N + t;
+                    acc += bucket[o];
+                    bucket[o] = 0.0;
+                    out[(size_t)rows[m] * KN + (size_t)k * N + t] += acc;
+                }
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // 4b. Segment centrality for one source.
 // ------------------------------------------------------------------------------------------
@@ -1068,6 +1093,27 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
     flush_counters(base, ph, relaxed, settled, done_src);
 }
 
+// Source-indexed plan on the device (prepare_source_sampling with source_indices): src_wt = node
+// weight and eligible = 1 at each listed source, 0 elsewhere.  Pass 0 clears, pass 1 scatters.
+__global__ void source_weights_kernel(const int32_t *sources, long long n, const float *node_w, int n_bound,
+                                      float *src_wt, uint8_t *eligible, int pass) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pass == 0) {
+        for (; t < n_bound; t += stride) {
+            src_wt[t] = 0.0f;
+            eligible[t] = 0u;
+        }
+    } else {
+        for (; t < n; t += stride) {
+            const int s = sources[t];
+            if (s < 0 || s >= n_bound) continue;
+            src_wt[s] = node_w[s];
+            eligible[s] = 1u;
+        }
+    }
+}
+
 __global__ void fill_dense_kernel(char *dense, size_t dense_stride, int n_bound, const int32_t *slots, int n_list,
                                   int all_slots) {
     // Resets dist (=inf) and aux (=0) of the listed slots (or of slots [0, all_slots)).
@@ -1098,6 +1144,19 @@ thread_local long long g_phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
 extern "C" void cs_set_error_internal(const char *msg) { cs_host::g_last_error = msg ? msg : ""; }
 
+namespace cs_host {
+thread_local long long g_retries[2] = {0, 0};
+}
+extern "C" void cs_set_retries_internal(long long overflowed, long long inexact) {
+    cs_host::g_retries[0] = overflowed;
+    cs_host::g_retries[1] = inexact;
+}
+extern "C" cs_status cs_last_retries(int64_t *overflowed, int64_t *inexact) {
+    if (overflowed) *overflowed = cs_host::g_retries[0];
+    if (inexact) *inexact = cs_host::g_retries[1];
+    return CS_OK;
+}
+
 namespace {
 using cs_host::g_counters;
 using cs_host::g_phase;
@@ -1118,7 +1177,7 @@ int sm_count() {
 }
 
 struct Layout {
-    size_t hdr_off, failed_off, bucket_off, dense_off, compact_off, compact_total, total;
+    size_t hdr_off, failed_off, failed2_off, bucket_off, dense_off, compact_off, compact_total, total;
     size_t dense_stride;
     int fail_cap;
 };
@@ -1132,7 +1191,8 @@ Layout layout(int n_bound, int n_slots, int cap, int P, int L) {
     l.hdr_off = 0;
     l.failed_off = 256;
     l.fail_cap = fail_capacity(n_slots);
-    l.bucket_off = cs::al256(l.failed_off + sizeof(int32_t) * (size_t)l.fail_cap);
+    l.failed2_off = cs::al256(l.failed_off + sizeof(int32_t) * (size_t)l.fail_cap);
+    l.bucket_off = cs::al256(l.failed2_off + sizeof(int32_t) * (size_t)l.fail_cap);
     l.dense_off = cs::al256(l.bucket_off + sizeof(double) * 3 * (size_t)L * (size_t)n_bound);
     l.dense_stride = cs::al256((size_t)n_bound * 4) * 2;
     l.compact_off = l.dense_off + l.dense_stride * (size_t)n_slots;
@@ -1141,6 +1201,47 @@ Layout layout(int n_bound, int n_slots, int cap, int P, int L) {
     l.compact_total = std::max(l.compact_total, cs::compact_bytes((size_t)n_bound, P, L));
     l.total = l.compact_off + l.compact_total;
     return l;
+}
+
+// Items that overflowed their slot's capacity run again at 4x the capacity (then 4x again, up to
+// cap = full_n, where nothing can overflow), each level on as many slots as the compact region
+// holds at that capacity; overflows of one level are listed for the next.  `run` launches one
+// level: run(params, slots).  Leaves the last header in h.
+template <typename Launch>
+cs_status retry_chain(const cs::PrimalParams &p, const cs_plan *plan, const Layout &lay, char *base, int full_n, int P,
+                      cs::WsHeader &h, cudaStream_t stream, bool poll, Launch run) {
+    int32_t *listA = (int32_t *)(base + lay.failed_off);
+    int32_t *listB = (int32_t *)(base + lay.failed2_off);
+    const int32_t *list = listA;
+    unsigned n_in = h.n_failed;
+    int cap_l = (int)std::min<long long>(full_n, 4ll * std::max(plan->cap, 8));
+    while (n_in > 0u) {
+        if (n_in > (unsigned)lay.fail_cap) return fail(CS_ERR_CAPACITY, "more overflowed sources than the list holds");
+        int32_t *out_l = (list == listA) ? listB : listA;
+        cs::PrimalParams p2 = p;
+        p2.cap = cap_l;
+        p2.rerun = 1;
+        p2.remap = list;
+        p2.n_src = (int64_t)n_in;
+        p2.failed = out_l;
+        cudaError_t e = cudaMemsetAsync(&p.hdr->work_next2, 0, sizeof(unsigned long long), stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(&p.hdr->n_failed, 0, sizeof(unsigned), stream);
+        if (e != cudaSuccess) return cuda_fail(e, "retry counter reset");
+        const size_t per = cs::compact_bytes((size_t)cap_l, P, plan->lanes);
+        int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
+        slots2 = std::max(1, std::min<int>(slots2, (int)n_in));
+        cs_status st = run(p2, slots2);
+        if (st != CS_OK) return st;
+        e = cs::read_header(p.hdr, h, stream, poll);
+        if (e != cudaSuccess) return cuda_fail(e, "retry kernel");
+        if (h.err != 0u)
+            return fail((cs_status)h.err, "device-side check failed in retry (code " + std::to_string(h.err) + ")");
+        if (cap_l >= full_n && h.n_failed > 0u) return fail(CS_ERR_INTERNAL, "overflow at full capacity");
+        n_in = h.n_failed;
+        list = out_l;
+        cap_l = (int)std::min<long long>(full_n, 4ll * cap_l);
+    }
+    return CS_OK;
 }
 
 int lanes_for(int mode, int k) { return mode == cs::MODE_SHORTEST ? 2 * k : (mode == cs::MODE_SEGMENT ? k : 1); }
@@ -1217,7 +1318,7 @@ cs_status reset_dense(char *dense, size_t stride, int n_bound, int n_slots, cuda
 cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan, void *ws, size_t ws_bytes,
                      cs_outputs out, void *stream_v, int mode, int32_t row_cap, int32_t *t_count, int32_t *t_node,
                      float *t_agg, int32_t *t_pred, const int32_t *tree_src, int32_t n_tree, uint32_t tree_maxsec,
-                     float tree_speed) {
+                     float tree_speed, bool poll = false) {
     cs_status st = validate_primal(g);
     if (st != CS_OK) return st;
     if (!plan || !ws) return fail(CS_ERR_ARG, "plan/workspace is NULL");
@@ -1226,6 +1327,8 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     if (K < 1 || K > CS_MAX_THRESHOLDS) return fail(CS_ERR_ARG, "threshold count out of range");
     const int L = lanes_for(mode, K);
     if (plan->lanes < L) return fail(CS_ERR_ARG, "plan was made for fewer thresholds");
+    if (plan->n_bound > 0 && plan->n_bound != g->n_bound)
+        return fail(CS_ERR_ARG, "plan was made for a graph of another node bound");
     Layout lay = layout(g->n_bound, plan->n_slots, plan->cap, P, plan->lanes);
     if (ws_bytes < lay.total) return fail(CS_ERR_ARG, "workspace too small for this plan");
     cudaStream_t stream = (cudaStream_t)stream_v;
@@ -1293,32 +1396,18 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     st = launch_primal(p, plan, plan->n_slots, stream);
     if (st != CS_OK) return st;
     cs::WsHeader h;
-    e = cudaMemcpyAsync(&h, p.hdr, sizeof(h), cudaMemcpyDeviceToHost, stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    e = cs::read_header(p.hdr, h, stream, poll);
     if (e != cudaSuccess) return cuda_fail(e, "centrality kernel");
     if (h.err != 0u)
         return fail((cs_status)h.err, "device-side check failed (code " + std::to_string(h.err) + " at " +
                                           std::to_string(h.err_where) + ")");
     long long done = (long long)h.sources_done, rel = (long long)h.edges_relaxed, set = (long long)h.nodes_settled;
+    const long long n_over = h.n_failed;
     if (h.n_failed > 0u) {
-        // Sources whose reach overflowed `cap` (their slots already reset themselves): redo them at
-        // cap = n_bound on as many slots as the compact region holds.
-        const int nf = (int)std::min<unsigned>(h.n_failed, (unsigned)lay.fail_cap);
-        const size_t per = cs::compact_bytes((size_t)g->n_bound, P, plan->lanes);
-        int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
-        slots2 = std::max(1, std::min(slots2, nf));
-        cs::PrimalParams p2 = p;
-        p2.cap = g->n_bound;
-        p2.rerun = 1;
-        p2.remap = p.failed;
-        p2.n_src = nf;
-        st = launch_primal(p2, plan, slots2, stream);
+        // Sources whose reach overflowed `cap` (their slots already reset themselves)
+        st = retry_chain(p, plan, lay, base, g->n_bound, P, h, stream, poll,
+                         [&](cs::PrimalParams &p2, int slots2) { return launch_primal(p2, plan, slots2, stream); });
         if (st != CS_OK) return st;
-        e = cudaMemcpyAsync(&h, p.hdr, sizeof(h), cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-        if (e != cudaSuccess) return cuda_fail(e, "centrality retry kernel");
-        if (h.err != 0u)
-            return fail((cs_status)h.err, "device-side check failed in retry (code " + std::to_string(h.err) + ")");
         done = (long long)h.sources_done;
         rel = (long long)h.edges_relaxed;
         set = (long long)h.nodes_settled;
@@ -1334,6 +1423,7 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     g_counters[1] = rel;
     g_counters[2] = set;
     for (int i = 0; i < 8; i++) cs_host::g_phase[i] = (long long)h.pad[i];
+    cs_set_retries_internal(n_over, 0);
     return CS_OK;
 }
 
@@ -1363,6 +1453,7 @@ cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t
     plan->lanes = L;
     plan->variant = variant;
     plan->max_degree = P;
+    plan->n_bound = n_bound;
     plan->workspace_bytes = total_for(slots);
     return CS_OK;
 }
@@ -1427,13 +1518,13 @@ cs_status cs_workspace_init(const cs_plan *plan, int32_t n_bound, void *workspac
 cs_status cs_centrality_shortest(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan,
                                  void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream) {
     return run_primal(g, q, plan, workspace_dev, workspace_bytes, out, stream, cs::MODE_SHORTEST, 0, nullptr, nullptr,
-                      nullptr, nullptr, nullptr, 0, 0, 0.0f);
+                      nullptr, nullptr, nullptr, 0, 0, 0.0f, true);
 }
 
 cs_status cs_segment_centrality(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan,
                                 void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream) {
     return run_primal(g, q, plan, workspace_dev, workspace_bytes, out, stream, cs::MODE_SEGMENT, 0, nullptr, nullptr,
-                      nullptr, nullptr, nullptr, 0, 0, 0.0f);
+                      nullptr, nullptr, nullptr, 0, 0, 0.0f, true);
 }
 
 cs_status cs_tree_shortest(const cs_primal_graph *g, int32_t n_queries, const int32_t *src_dev, uint32_t max_seconds,
@@ -1444,7 +1535,7 @@ cs_status cs_tree_shortest(const cs_primal_graph *g, int32_t n_queries, const in
         return fail(CS_ERR_ARG, "tree outputs missing");
     cs_outputs o{nullptr, nullptr};
     return run_primal(g, nullptr, plan, workspace_dev, workspace_bytes, o, stream, cs::MODE_TREE, row_cap, count_dev,
-                      node_dev, agg_seconds_dev, pred_dev, src_dev, n_queries, max_seconds, speed_m_s);
+                      node_dev, agg_seconds_dev, pred_dev, src_dev, n_queries, max_seconds, speed_m_s, true);
 }
 
 }  // extern "C"
@@ -1609,7 +1700,10 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
     if (plan->lanes < b.L) return fail(CS_ERR_ARG, "plan was made for fewer lanes");
     const int P = std::max(1, plan->max_degree);
     if (P < b.P) return fail(CS_ERR_ARG, "plan was made for a smaller degree");
-    const Layout lay = layout(b.max_n, plan->n_slots, plan->cap, P, plan->lanes);
+    // slot geometry is the plan's, so one workspace serves batches of any graphs up to its size
+    const int geo_n = plan->n_bound > 0 ? plan->n_bound : b.max_n;
+    if (geo_n < b.max_n) return fail(CS_ERR_ARG, "plan was made for a smaller graph");
+    const Layout lay = layout(geo_n, plan->n_slots, plan->cap, P, plan->lanes);
     if (ws_bytes < lay.total) return fail(CS_ERR_ARG, "workspace too small for this plan");
     long long n_items = 0;
     for (int j = 0; j < n_jobs; j++) {
@@ -1620,7 +1714,7 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
     char *base = (char *)ws;
     cs::PrimalParams p;
     memset(&p, 0, sizeof(p));
-    p.g.n_bound = b.max_n;  // slot geometry only; each job brings its own graph
+    p.g.n_bound = geo_n;  // slot geometry only; each job brings its own graph
     p.hdr = (cs::WsHeader *)(base + lay.hdr_off);
     p.failed = (int32_t *)(base + lay.failed_off);
     p.fail_cap = lay.fail_cap;
@@ -1632,50 +1726,43 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
     p.L = plan->lanes;
     g_counters[0] = g_counters[1] = g_counters[2] = g_counters[3] = 0;
     cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), stream);
-    for (int j = 0; j < n_jobs && e == cudaSuccess; j++)
-        if (jobs_host[j].mode == cs::MODE_SHORTEST && jobs_host[j].compute_closeness)
-            e = cudaMemsetAsync(jobs_host[j].bucket_dev, 0,
-                                sizeof(double) * 3 * (size_t)jobs_host[j].k * (size_t)jobs_host[j].g.n_bound, stream);
     if (e != cudaSuccess) return cuda_fail(e, "batch reset");
     if (n_items == 0) return CS_OK;
     st = launch_batch(p, plan, jobs_dev, n_jobs, n_items, plan->n_slots, stream);
     if (st != CS_OK) return st;
     if (!(flags & CS_BATCH_ASYNC)) {
         cs::WsHeader h;
-        e = cudaMemcpyAsync(&h, p.hdr, sizeof(h), cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        e = cs::read_header(p.hdr, h, stream, true);
         if (e != cudaSuccess) return cuda_fail(e, "batch kernel");
         if (h.err != 0u) return fail((cs_status)h.err, "device-side check failed (code " + std::to_string(h.err) + ")");
+        const long long n_over = h.n_failed;
         if (h.n_failed > 0u) {
-            const int nf = (int)std::min<unsigned>(h.n_failed, (unsigned)lay.fail_cap);
-            const size_t per = cs::compact_bytes((size_t)b.max_n, P, plan->lanes);
-            int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
-            slots2 = std::max(1, std::min(slots2, nf));
-            cs::PrimalParams p2 = p;
-            p2.cap = b.max_n;
-            p2.rerun = 1;
-            p2.remap = p.failed;
-            p2.n_src = nf;
-            st = launch_batch(p2, plan, jobs_dev, n_jobs, n_items, slots2, stream);
+            st = retry_chain(p, plan, lay, base, b.max_n, P, h, stream, true, [&](cs::PrimalParams &p2, int slots2) {
+                return launch_batch(p2, plan, jobs_dev, n_jobs, n_items, slots2, stream);
+            });
             if (st != CS_OK) return st;
-            e = cudaMemcpyAsync(&h, p.hdr, sizeof(h), cudaMemcpyDeviceToHost, stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-            if (e != cudaSuccess) return cuda_fail(e, "batch retry kernel");
-            if (h.err != 0u) return fail((cs_status)h.err, "device-side check failed in retry");
         }
+        cs_set_retries_internal(n_over, 0);
         g_counters[0] = (long long)h.sources_done;
         g_counters[1] = (long long)h.edges_relaxed;
         g_counters[2] = (long long)h.nodes_settled;
     }
+    int max_n = 0, n_pref = 0;
     for (int j = 0; j < n_jobs; j++) {
         const cs_batch_job &jb = jobs_host[j];
         if (jb.mode == cs::MODE_SHORTEST && jb.compute_closeness && jb.n_sources > 0) {
-            int blocks = std::max(1, std::min((jb.g.n_bound + 255) / 256, std::max(1, sm_count()) * 8));
-            cs::bucket_prefix_kernel<<<blocks, 256, 0, stream>>>(jb.bucket_dev, jb.out_dev, jb.k, jb.g.n_bound);
-            g_counters[3]++;
-            e = cudaGetLastError();
-            if (e != cudaSuccess) return cuda_fail(e, "bucket_prefix_kernel launch");
+            max_n = std::max(max_n, jb.g.n_bound);
+            n_pref++;
         }
+    }
+    if (n_pref > 0) {
+        const int sms = std::max(1, sm_count());
+        const int gy = std::min(n_pref, 65535);
+        const int gx = std::max(1, std::min((max_n + 255) / 256, std::max(1, sms * 8 / gy)));
+        cs::batch_prefix_kernel<<<dim3(gx, gy), 256, 0, stream>>>(jobs_dev, n_jobs);
+        g_counters[3]++;
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "batch_prefix_kernel launch");
     }
     return CS_OK;
 }
@@ -1683,8 +1770,7 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
 cs_status cs_batch_status(void *ws, int64_t *n_overflowed, int64_t *sources_done, void *stream) {
     if (!ws) return fail(CS_ERR_ARG, "workspace is NULL");
     cs::WsHeader h;
-    cudaError_t e = cudaMemcpyAsync(&h, ws, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    cudaError_t e = cs::read_header((const cs::WsHeader *)ws, h, (cudaStream_t)stream, true);
     if (e != cudaSuccess) return cuda_fail(e, "batch status");
     if (n_overflowed) *n_overflowed = (int64_t)h.n_failed;
     if (sources_done) *sources_done = (int64_t)h.sources_done;
@@ -1695,7 +1781,46 @@ cs_status cs_batch_status(void *ws, int64_t *n_overflowed, int64_t *sources_done
     return CS_OK;
 }
 
+cs_status cs_batch_failed(void *ws, const cs_plan *plan, int32_t *items_host, int32_t max_items, int64_t *n_failed,
+                          void *stream) {
+    if (!ws || !plan || !n_failed) return fail(CS_ERR_ARG, "workspace/plan/n_failed is NULL");
+    cs::WsHeader h;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cs::read_header((const cs::WsHeader *)ws, h, st, true);
+    if (e != cudaSuccess) return cuda_fail(e, "batch failed list");
+    const Layout lay = layout(std::max(1, plan->n_bound), plan->n_slots, plan->cap, 1, plan->lanes);
+    const int64_t nf = (int64_t)h.n_failed;
+    *n_failed = nf;
+    if (nf > (int64_t)lay.fail_cap) return fail(CS_ERR_CAPACITY, "more overflowed items than the failed list holds");
+    const int64_t c = std::min<int64_t>(nf, std::max(0, max_items));
+    if (c > 0 && items_host) {
+        e = cudaMemcpyAsync(items_host, (char *)ws + lay.failed_off, sizeof(int32_t) * (size_t)c, cudaMemcpyDeviceToHost,
+                            st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(e, "batch failed list");
+    }
+    return CS_OK;
+}
+
 }  // extern "C"
+
+extern "C" cs_status cs_source_weights(const int32_t *sources_dev, int64_t n_sources, const float *node_w_dev,
+                                        int32_t n_bound, float *src_wt_dev, uint8_t *eligible_dev, void *stream) {
+    if (n_bound <= 0 || !node_w_dev || !src_wt_dev || !eligible_dev || (n_sources > 0 && !sources_dev))
+        return fail(CS_ERR_ARG, "source weights: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int sms = std::max(1, sm_count());
+    const int b0 = std::max(1, std::min((n_bound + 255) / 256, sms * 4));
+    cs::source_weights_kernel<<<b0, 256, 0, st>>>(sources_dev, n_sources, node_w_dev, n_bound, src_wt_dev, eligible_dev,
+                                                  0);
+    if (n_sources > 0) {
+        const int b1 = (int)std::max<long long>(1, std::min<long long>((n_sources + 255) / 256, sms * 4));
+        cs::source_weights_kernel<<<b1, 256, 0, st>>>(sources_dev, n_sources, node_w_dev, n_bound, src_wt_dev,
+                                                      eligible_dev, 1);
+    }
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CS_OK : cuda_fail(e, "source_weights_kernel launch");
+}
 
 extern "C" cs_status cs_abi_sizes(int32_t *out, int32_t n) {
     // sizes of the public structs, for bindings to check their layouts against

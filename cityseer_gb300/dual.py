@@ -144,22 +144,41 @@ def dual_csr(ns) -> DualCSR:
 
 
 def dual_workspace(ns, csr: DualCSR, k: int, speed: float, cap: int = 0, max_slots: int = 0):
+    """The dual graph's workspace, grown (never shrunk) to the thresholds this call needs."""
     from .centrality import _mem_budget
 
-    key = ("wsd", k, cap, max_slots)
-    ws = ns._cache.get(key)
-    if ws is None:
-        for kk in [kk for kk in ns._cache if isinstance(kk, tuple) and kk and kk[0] in ("ws", "wsd")]:
-            del ns._cache[kk]
-        torch.cuda.empty_cache()
-        lib = _native.load()
-        plan = _native.Plan()
-        rc = lib.cs_plan_dual(C.byref(csr.struct(speed)), 0, k, cap, max_slots, _mem_budget(csr.device),
-                              C.byref(plan))
-        _native.check(rc, "cs_plan_dual")
-        ws = DualWorkspace(plan, csr.n_bound, csr.device)
-        ns._cache[key] = ws
+    ws = ns._cache.get("wsd")
+    if ws is not None and ws.plan.lanes >= k and (cap <= 0 or ws.plan.cap >= cap) and \
+            (max_slots <= 0 or ws.plan.n_slots <= max_slots):
+        return ws
+    if ws is not None:
+        k = max(k, int(ws.plan.lanes))
+        del ns._cache["wsd"]
+        del ws
+    torch.cuda.empty_cache()
+    lib = _native.load()
+    plan = _native.Plan()
+    rc = lib.cs_plan_dual(C.byref(csr.struct(speed)), 0, k, cap, max_slots, _mem_budget(csr.device), C.byref(plan))
+    _native.check(rc, "cs_plan_dual")
+    ws = DualWorkspace(plan, csr.n_bound, csr.device)
+    ns._cache["wsd"] = ws
     return ws
+
+
+def estimate_states(ns, speed: float, max_seconds: int) -> int:
+    """Search capacity (angular states) for sources of this dual graph up to max_seconds: twice the
+    largest metric reach (dual nodes within max_seconds by shortest metric distance, from the tree
+    kernel on the dual's own edges over a sample of sources) plus 30%.  A simplest route is never
+    shorter than the shortest one, so the angular search reaches a subset of those nodes."""
+    from .centrality import _primal_csr, estimate_reach
+
+    key = ("dual_states", float(np.float32(speed)), int(max_seconds))
+    hit = ns._cache.get(key)
+    if hit is None:
+        r = estimate_reach(ns, _primal_csr(ns), speed, int(max_seconds))
+        hit = int(min(2 * ns.node_bound(), max(1024, -(-int(2.6 * r) // 256) * 256)))
+        ns._cache[key] = hit
+    return hit
 
 
 def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, betweenness, sp):
@@ -180,7 +199,7 @@ def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, between
     lib = _native.load()
     for lo, hi in _groups(K):
         k = hi - lo
-        ws = dual_workspace(ns, csr, k, speed)
+        ws = dual_workspace(ns, csr, k, speed, cap=estimate_states(ns, speed, max(secs[lo:hi])))
         out = torch.zeros((4, k, nb), dtype=torch.float64, device=dev)
         reach = torch.zeros(k, dtype=torch.int32, device=dev)
         q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, tol, closeness, betweenness, track, proc_t,

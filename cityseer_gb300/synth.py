@@ -163,11 +163,52 @@ def _half_polylines(p: Primal):
     return out_u, out_v, np.array(mids)
 
 
+def _dual_structure_straight(p: Primal) -> NetworkStructure:
+    """dual_structure for lattices whose streets are all straight, vectorised: each dual edge a -> b
+    through primal node n is the polyline mid_a -> n -> mid_b."""
+    x, y = p.x, p.y
+    ax, ay = x[p.u], y[p.u]
+    bx, by = x[p.v], y[p.v]
+    seg = np.hypot(bx - ax, by - ay)
+    frac = np.where(seg > 0, (seg / 2.0) / np.where(seg > 0, seg, 1.0), 0.0)
+    mx = ax + (bx - ax) * frac
+    my = ay + (by - ay) * frac
+    m = len(p.u)
+    node_of = np.concatenate([p.u, p.v]).astype(np.int64)
+    e_of = np.concatenate([np.arange(m), np.arange(m)]).astype(np.int64)
+    order = np.lexsort((e_of, node_of))
+    node_of, e_of = node_of[order], e_of[order]
+    starts = np.flatnonzero(np.r_[True, node_of[1:] != node_of[:-1]])
+    counts = np.diff(np.r_[starts, len(node_of)])
+    pa, pb = [], []
+    for i in range(int(counts.max()) if len(counts) else 0):
+        for j in range(i + 1, int(counts.max())):
+            sel = counts > j
+            pa.append(starts[sel] + i)
+            pb.append(starts[sel] + j)
+    pa = np.concatenate(pa) if pa else np.zeros(0, np.int64)
+    pb = np.concatenate(pb) if pb else np.zeros(0, np.int64)
+    ea = np.concatenate([e_of[pa], e_of[pb]])
+    eb = np.concatenate([e_of[pb], e_of[pa]])
+    nd = np.concatenate([node_of[pa], node_of[pa]])
+    nx_, ny_ = x[nd], y[nd]
+    s0 = np.hypot(nx_ - mx[ea], ny_ - my[ea])
+    s1 = np.hypot(mx[eb] - nx_, my[eb] - ny_)
+    lens = (0.0 + s0) + s1
+    angs = 0.0 + _turn(mx[ea], my[ea], nx_, ny_, mx[eb], my[eb])
+    order = np.lexsort((nd, eb, ea))
+    return NetworkStructure.from_arrays(
+        mx, my, ea[order], eb[order], lens[order].astype(np.float32), edge_idx=np.zeros(len(ea), np.int64),
+        edge_angle_sum=angs[order].astype(np.float32), edge_shared_key=[str(s) for s in nd[order]], is_dual=True)
+
+
 def dual_structure(p: Primal) -> NetworkStructure:
     """The dual graph as nx_to_dual builds it (pysrc/cityseer/tools/graphs.py:1965-2149): one node
     per street at its midpoint, one undirected dual edge per pair of streets sharing a primal node,
     geometry = half street + half street welded at the shared node, shared_primal_node_key = that
-    node.  Directed edges are inserted per dual node in ascending order."""
+    node.  Directed edges are inserted per dual node in ascending order of (neighbour, shared node)."""
+    if all(g is None for g in p.geoms):
+        return _dual_structure_straight(p)
     half_u, half_v, mids = _half_polylines(p)
     m = len(p.u)
     inc: dict[int, list[tuple[int, int]]] = {}
@@ -199,7 +240,8 @@ def dual_structure(p: Primal) -> NetworkStructure:
                     shared.append(node)
     src = np.array(src, np.int64)
     dst = np.array(dst, np.int64)
-    order = np.lexsort((dst, src))
+    # parallel streets give two dual edges with the same ends: order those by the shared node
+    order = np.lexsort((np.array(shared, np.int64), dst, src))
     return NetworkStructure.from_arrays(
         mids[:, 0], mids[:, 1], src[order], dst[order], np.array(lens)[order].astype(np.float32),
         edge_idx=np.zeros(len(src), np.int64), edge_angle_sum=np.array(angs)[order].astype(np.float32),

@@ -105,6 +105,7 @@ typedef struct {
     int32_t lanes;        /* accumulator lanes per reached node */
     int32_t variant;      /* register budget: 3 (default) or 2 resident 256-thread blocks per SM */
     int32_t max_degree;   /* batches: largest out-degree over the jobs */
+    int32_t n_bound;      /* node bound the slot geometry was sized for (set by the planners) */
     size_t workspace_bytes;
 } cs_plan;
 
@@ -127,7 +128,8 @@ typedef struct {
     const float *src_wt_dev;
     const uint8_t *eligible_dev;
     double *out_dev;          /* [7 (shortest) or 4 (segment)][k][n_bound], zeroed by the caller */
-    double *bucket_dev;       /* [3][k][n_bound] scratch for shortest closeness (zeroed by the launch) */
+    double *bucket_dev;       /* [3][k][n_bound] scratch for shortest closeness: zero before the first run;
+                                 every successful run leaves it zero again */
     int64_t item_begin;       /* first queue item of this job (set by cs_batch_prepare) */
 } cs_batch_job;
 
@@ -220,12 +222,13 @@ cs_status cs_tree_simplest(const cs_dual_graph *g, int32_t n_queries, const int3
 /* Batched persistent form (no reference counterpart: the reference runs one graph per call).
  * cs_batch_prepare fills item_begin for jobs[0..n_jobs) (host array) and returns the item count.
  * cs_batch_plan sizes one workspace for all jobs (largest graph, degree, lanes; cap = reach capacity).
- * cs_batch_run enqueues the whole batch on `stream`: header and bucket resets, one persistent launch
- * over every item, the closeness threshold prefix per job.  jobs_dev is a device copy of the prepared
- * host array.  With flags & CS_BATCH_ASYNC the call neither synchronises nor retries (it can be
- * captured in a CUDA graph); cs_batch_status then reports overflowed items, whose results are
- * incomplete (rerun without CS_BATCH_ASYNC or with a larger cap).  Without the flag, overflowed
- * items are redone at full capacity inside the call. */
+ * cs_batch_run enqueues the whole batch on `stream`: a header reset, one persistent launch over
+ * every item, and one launch for the closeness threshold prefixes of all jobs (which re-zeroes the
+ * buckets).  jobs_dev is a device copy of the prepared host array.  With flags & CS_BATCH_ASYNC the
+ * call neither synchronises nor retries (it can be captured in a CUDA graph); cs_batch_status /
+ * cs_batch_failed then report the overflowed items, which contributed nothing (run them again, e.g.
+ * as a batch without CS_BATCH_ASYNC).  Without the flag, overflowed items are redone inside the
+ * call at growing capacities. */
 #define CS_BATCH_ASYNC 1
 cs_status cs_batch_prepare(cs_batch_job *jobs_host, int32_t n_jobs, int64_t *n_items);
 cs_status cs_batch_plan(const cs_batch_job *jobs_host, int32_t n_jobs, int32_t cap, int32_t max_slots,
@@ -233,6 +236,11 @@ cs_status cs_batch_plan(const cs_batch_job *jobs_host, int32_t n_jobs, int32_t c
 cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_dev, int32_t n_jobs, const cs_plan *plan,
                        void *workspace_dev, size_t workspace_bytes, int32_t flags, void *stream);
 cs_status cs_batch_status(void *workspace_dev, int64_t *n_overflowed, int64_t *sources_done, void *stream);
+/* After a CS_BATCH_ASYNC launch: the global item indices of the overflowed items (first max_items
+ * of *n_failed) so that the caller can run them again, e.g. as a synchronous batch (which retries
+ * at full capacity).  Overflowed items contributed nothing to the outputs. */
+cs_status cs_batch_failed(void *workspace_dev, const cs_plan *plan, int32_t *items_host, int32_t max_items,
+                          int64_t *n_failed, void *stream);
 
 /* Device counters of the last call on this thread: sources done, edges relaxed, nodes settled
  * (used for throughput and roofline accounting) and the number of kernels it launched. */
@@ -241,6 +249,17 @@ cs_status cs_last_counters(int64_t *sources, int64_t *edges_relaxed, int64_t *no
 /* Per-phase SM cycles of the last call on this thread, summed over warps: 0 search, 1 sort,
  * 2 predecessor replay, 3 closeness, 4 sigma, 5 backward sweep, 6 scratch reset (n <= 8). */
 cs_status cs_last_phase_cycles(int64_t *cycles, int32_t n);
+
+/* Source-indexed plan built on the device without synchronising (prepare_source_sampling with
+ * source_indices, rust/src/centrality.rs:1032-1104): src_wt[s] = node_w[s] and eligible[s] = 1 for
+ * each listed source, zero elsewhere (node_w: f32[n_bound]). */
+cs_status cs_source_weights(const int32_t *sources_dev, int64_t n_sources, const float *node_w_dev, int32_t n_bound,
+                            float *src_wt_dev, uint8_t *eligible_dev, void *stream);
+
+/* Sources of the last call on this thread that overflowed their slot's capacity (and were run again
+ * at a larger one) and, for simplest-path calls, whose replay disagreed with the label-correcting
+ * search (and were run again with the exact heap search). */
+cs_status cs_last_retries(int64_t *overflowed, int64_t *inexact);
 
 /* sizeof of cs_primal_graph, cs_dual_graph, cs_query, cs_plan, cs_outputs, cs_batch_job (first n). */
 cs_status cs_abi_sizes(int32_t *out, int32_t n);

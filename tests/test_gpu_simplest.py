@@ -78,3 +78,46 @@ def test_simplest_diamond_golden_harmonic():
     gold = [g for g in FIX["centrality"]["local_centrality_all"] if g["result"] == "node_result_simplest"]
     for gd in gold:
         assert np.allclose(getattr(res, gd["attr"])[gd["distance"]], gd["values"], atol=0.01, rtol=1e-4)
+
+
+@pytest.mark.gpu
+def test_simplest_capacity_chain_and_replay_counts():
+    """A plan with a tiny capacity makes most sources overflow; they run again at 4x capacities
+    until they fit, and the results equal the default plan's (itself checked against the oracle)."""
+    import ctypes as C
+
+    import torch
+
+    from cityseer_gb300 import _native, centrality, dual
+
+    p, dists = synth.lattice_config("c3", side=14)
+    ns = synth.dual_structure(p)
+    want = _run(ns, dists)
+    lib = _native.load()
+    over, inexact = C.c_int64(), C.c_int64()
+    lib.cs_last_retries(C.byref(over), C.byref(inexact))
+    assert inexact.value < len(ns.node_indices())
+    d, b, s = common.pair_distances_betas_time(1.33333, distances=dists)
+    csr = dual.dual_csr(ns)
+    plan = _native.Plan()
+    _native.check(lib.cs_plan_dual(C.byref(csr.struct(1.33333)), 0, len(d), 64, 64, 0, C.byref(plan)), "plan")
+    ws = dual.DualWorkspace(plan, csr.n_bound, csr.device)
+    sp = prepare_source_sampling(ns, None, None, None, None)
+    dev = csr.device
+    keep = [torch.from_numpy(x).to(dev) for x in (sp.process, sp.src_wt, sp.eligible)]
+    q = centrality._make_query(d, b, s, 1.33333, 1e-4, True, True, False, *keep)
+    out = torch.zeros((4, len(d), csr.n_bound), dtype=torch.float64, device=dev)
+    _native.check(lib.cs_centrality_simplest(C.byref(csr.struct(1.33333)), C.byref(q), C.byref(plan), ws.ptr,
+                                             ws.nbytes, _native.Outputs(out.data_ptr(), None),
+                                             torch.cuda.current_stream().cuda_stream), "simplest small cap")
+    lib.cs_last_retries(C.byref(over), C.byref(inexact))
+    assert over.value > 0
+    got = out.cpu().numpy()
+    idx = np.asarray(ns.node_indices())
+    for m, name in enumerate(ROWS):
+        for i, dist in enumerate(d):
+            if name == "node_density":
+                np.testing.assert_array_equal(got[m, i][idx], getattr(want, name)[dist])
+            else:
+                assert_close_sums(got[m, i][idx], getattr(want, name)[dist], rtol=1e-9, atol=1e-9,
+                                  what=f"{name}[{dist}] (cap 64)")
