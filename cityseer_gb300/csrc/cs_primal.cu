@@ -159,7 +159,11 @@ __device__ __forceinline__ void push_entries(bool first, int route, int v, float
     nfar += __popc(mr);
 }
 
-__device__ int warp_search(const PrimalParams &p, const SlotPtrs &s, int src, long long &relaxed) {
+#ifndef CS_PHASE_INLINE
+#define CS_PHASE_INLINE
+#endif
+
+CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs &s, int src, long long &relaxed) {
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
     const int cap = p.cap;
@@ -434,9 +438,10 @@ __device__ __forceinline__ int replay_first_min(const PrimalParams &p, const Nb<
 // ------------------------------------------------------------------------------------------
 // 4a. Shortest-path centrality for one source (after search and sort).
 // ------------------------------------------------------------------------------------------
+// Per-phase cycle counters live in the warp's shared-memory row (lane 0 adds), not in registers.
 __device__ __forceinline__ void phase_mark(long long *ph, int idx, long long &t) {
     const long long now = clock64();
-    ph[idx] += now - t;
+    if (lane_id() == 0) ph[idx] += now - t;
     t = now;
 }
 
@@ -468,7 +473,7 @@ __device__ __forceinline__ int load_preds(const SlotPtrs &s, int i, int P, int *
 }
 
 template <int PM>
-__device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R, long long *ph,
+CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R, long long *ph,
                                     int *cnt) {
     const int lane = lane_id();
     long long tph = clock64();
@@ -519,17 +524,21 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
     // depend on the threshold: they go once into the bucket of the first qualifying threshold and a
     // prefix over thresholds after the launch completes them.  Cycles and beta terms are per k.
     if (p.closeness) {
-        float rankw[MAXK];
-        long long nc = 0, ec = 0;
-#pragma unroll
-        for (int k = 0; k < MAXK; k++) {
-            nc += cnt[k];
-            ec += cnt[MAXK + k];
-            const long long r = ec - nc + 1;
-            const float rank = (nc == 0) ? 0.0f : (float)(r > 0 ? r : 0);
-            rankw[k] = fmul(rank, cycles_wt);
-            if (p.track_reach && k < K && lane == 0 && nc > 1) atomicAdd(&p.reach[k], (unsigned)(nc - 1));
+        // per-threshold circuit-rank weights, computed by lane 0 into the (now free) edge-count half
+        // of the warp's shared counters
+        float *rankw = (float *)(cnt + MAXK);
+        if (lane == 0) {
+            long long nc = 0, ec = 0;
+            for (int k = 0; k < K; k++) {
+                nc += cnt[k];
+                ec += cnt[MAXK + k];
+                const long long r = ec - nc + 1;
+                const float rank = (nc == 0) ? 0.0f : (float)(r > 0 ? r : 0);
+                rankw[k] = fmul(rank, cycles_wt);
+                if (p.track_reach && nc > 1) atomicAdd(&p.reach[k], (unsigned)(nc - 1));
+            }
         }
+        __syncwarp();
         const double wt_d = f2d(wt);
         const size_t KN = (size_t)K * N;
         for (int i = 1 + lane; i < R; i += 32) {
@@ -541,9 +550,7 @@ __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, in
             atomicAdd(bk, wt_d);
             atomicAdd(bk + KN, f2d(fmul(c, wt)));
             atomicAdd(bk + 2 * KN, f2d(fmul(__fdiv_rn(1.0f, c), wt)));
-#pragma unroll
-            for (int k = 0; k < MAXK; k++) {
-                if (k < k0 || k >= K) continue;
+            for (int k = k0; k < K; k++) {
                 double *row = p.out + (size_t)k * N + t;
                 atomicAdd(row + 2 * KN, f2d(rankw[k]));
                 atomicAdd(row + 4 * KN, f2d(fmul(expf(fmul(-p.beta[k], c)), wt)));
@@ -710,7 +717,7 @@ __global__ void batch_prefix_kernel(const cs_batch_job *jobs, int n_jobs) {
 // 4b. Segment centrality for one source.
 // ------------------------------------------------------------------------------------------
 template <int PM>
-__device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R) {
+CS_PHASE_INLINE __device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R) {
     const int lane = lane_id();
     const int K = p.k;
     const int N = p.g.n_bound;
@@ -898,7 +905,7 @@ __device__ void segment_accumulate(const PrimalParams &p, const SlotPtrs &s, int
 // 4c. Shortest-path tree rows (isochrone query).
 // ------------------------------------------------------------------------------------------
 template <int PM>
-__device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, int R) {
+CS_PHASE_INLINE __device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, int R) {
     const int lane = lane_id();
     if (R > p.row_cap) {
         if (lane == 0) p.t_count[qidx] = -R;  // rows too narrow: report the reach only
@@ -934,7 +941,9 @@ __device__ void tree_rows(const PrimalParams &p, const SlotPtrs &s, int qidx, in
 // ------------------------------------------------------------------------------------------
 // One source on this warp's slot: search, sort, mode-specific accumulation, scratch reset.
 // Returns false when the source overflowed the slot's capacity (recorded for the retry).
-template <int PM>
+// MODE is the accumulation compiled in (a kernel per mode keeps each kernel's code, and so its
+// instruction-cache footprint, to what that mode runs); -1 dispatches on p.mode at run time.
+template <int PM, int MODE>
 __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs &s, int li, int src, uint32_t *hist,
                                            int *cnt, long long *ph, long long &relaxed, long long &settled) {
     const int lane = lane_id();
@@ -962,9 +971,17 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
     for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
     __syncwarp();
     phase_mark(ph, 1, t0);
-    if (p.mode == MODE_SHORTEST) shortest_accumulate<PM>(p, s, src, R, ph, cnt);
-    else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
-    else tree_rows<PM>(p, s, li, R);
+    if constexpr (MODE == MODE_SHORTEST) {
+        shortest_accumulate<PM>(p, s, src, R, ph, cnt);
+    } else if constexpr (MODE == MODE_SEGMENT) {
+        segment_accumulate<PM>(p, s, src, R);
+    } else if constexpr (MODE == MODE_TREE) {
+        tree_rows<PM>(p, s, li, R);
+    } else {
+        if (p.mode == MODE_SHORTEST) shortest_accumulate<PM>(p, s, src, R, ph, cnt);
+        else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
+        else tree_rows<PM>(p, s, li, R);
+    }
     __syncwarp();
     t0 = clock64();
     for (int i = lane; i < R; i += 32) {
@@ -981,6 +998,7 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
 __device__ __forceinline__ void flush_counters(const PrimalParams &p, long long *ph, long long relaxed,
                                                long long settled, long long done_src) {
     const long long rsum = warp_sum_ll(relaxed);
+    __syncwarp();
     if (lane_id() == 0) {
         for (int q = 0; q < 8; q++) atomicAdd(&p.hdr->pad[q], (unsigned long long)ph[q]);
         atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
@@ -992,17 +1010,20 @@ __device__ __forceinline__ void flush_counters(const PrimalParams &p, long long 
 // ------------------------------------------------------------------------------------------
 // Persistent kernel: each warp owns one scratch slot and pulls sources until the list is empty.
 // ------------------------------------------------------------------------------------------
-template <int PM, int MINB>
+template <int PM, int MINB, int MODE>
 __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][2 * MAXK];
+    __shared__ long long ph_all[8][8];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
     if (slot >= p.n_slots) return;
     const SlotPtrs s = slot_ptrs(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.P, p.L, slot, p.g.n_bound);
     long long relaxed = 0, settled = 0, done_src = 0;
-    long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long *ph = ph_all[wib];
+    if (lane < 8) ph[lane] = 0;
+    __syncwarp();
     while (true) {
         unsigned long long idx = 0;
         if (lane == 0) idx = atomicAdd(p.rerun ? &p.hdr->work_next2 : &p.hdr->work_next, 1ull);
@@ -1010,7 +1031,8 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
         if (idx >= (unsigned long long)p.n_src) break;
         if (__ldcg(&p.hdr->err) != 0u) break;
         const int li = p.remap ? p.remap[idx] : (int)idx;
-        if (run_source<PM>(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled)) done_src++;
+        if (run_source<PM, MODE>(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled))
+            done_src++;
     }
     flush_counters(p, ph, relaxed, settled, done_src);
 }
@@ -1061,6 +1083,7 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
                                                           int n_jobs, long long n_items) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][2 * MAXK];
+    __shared__ long long ph_all[8][8];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
@@ -1069,7 +1092,9 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
     const SlotPtrs s = slot_ptrs(base.dense, base.dense_stride, base.compact, (size_t)base.cap, base.P, base.L, slot,
                                  base.g.n_bound);
     long long relaxed = 0, settled = 0, done_src = 0;
-    long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long *ph = ph_all[wib];
+    if (lane < 8) ph[lane] = 0;
+    __syncwarp();
     PrimalParams p;
     int cur_job = -1;
     while (true) {
@@ -1087,7 +1112,7 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
         }
         const int li = (int)(item - jobs[jb].item_begin);
         // failures record the global item index
-        if (run_source<PM>(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled))
+        if (run_source<PM, -1>(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled))
             done_src++;
     }
     flush_counters(base, ph, relaxed, settled, done_src);
@@ -1264,9 +1289,20 @@ int resolve_variant(const cs_plan *plan) {
 }
 
 cudaError_t occupancy_blocks(int P, int variant, int *bpsm) {
-    if (P > 8) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<CS_MAX_DEGREE, 2>, 256, 0);
-    if (variant == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 3>, 256, 0);
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 2>, 256, 0);
+    if (P > 8)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<CS_MAX_DEGREE, 2, 0>, 256, 0);
+    if (variant == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 3, 0>, 256, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 2, 0>, 256, 0);
+}
+
+template <int MODE>
+void launch_primal_mode(const cs::PrimalParams &p, int P, int minb, int blocks, cudaStream_t stream) {
+    if (P <= 8) {
+        if (minb == 3) cs::primal_kernel<8, 3, MODE><<<blocks, 256, 0, stream>>>(p);
+        else cs::primal_kernel<8, 2, MODE><<<blocks, 256, 0, stream>>>(p);
+    } else {
+        cs::primal_kernel<CS_MAX_DEGREE, 2, MODE><<<blocks, 256, 0, stream>>>(p);
+    }
 }
 
 cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, cudaStream_t stream) {
@@ -1275,12 +1311,9 @@ cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, c
     const int blocks = (n_slots + wpb - 1) / wpb;
     p.n_slots = n_slots;
     const int minb = resolve_variant(plan);
-    if (p.P <= 8) {
-        if (minb == 3) cs::primal_kernel<8, 3><<<blocks, tpb, 0, stream>>>(p);
-        else cs::primal_kernel<8, 2><<<blocks, tpb, 0, stream>>>(p);
-    } else {
-        cs::primal_kernel<CS_MAX_DEGREE, 2><<<blocks, tpb, 0, stream>>>(p);
-    }
+    if (p.mode == cs::MODE_SHORTEST) launch_primal_mode<cs::MODE_SHORTEST>(p, p.P, minb, blocks, stream);
+    else if (p.mode == cs::MODE_SEGMENT) launch_primal_mode<cs::MODE_SEGMENT>(p, p.P, minb, blocks, stream);
+    else launch_primal_mode<cs::MODE_TREE>(p, p.P, minb, blocks, stream);
     g_counters[3]++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "primal_kernel launch");
