@@ -474,7 +474,7 @@ __device__ __forceinline__ int load_preds(const SlotPtrs &s, int i, int P, int *
 
 template <int PM>
 CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R, long long *ph,
-                                    int *cnt) {
+                                    int *cnt, int *bw_pl, float *bw_fr) {
     const int lane = lane_id();
     long long tph = clock64();
     const int K = p.k;
@@ -625,13 +625,14 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
                 const float cost = route_cost(s.sd[i], p.speed);
                 const float sw = sig[i];
                 const float pair = __ldg(&p.eligible[v]) ? 0.5f : 1.0f;
-                float fr[PM];
+                // predecessor rows and sigma fractions go to this lane's shared-memory column, so
+                // that the push loop below is a plain (not unrolled) loop over the np predecessors
 #pragma unroll
                 for (int r = 0; r < PM; r++) {
-                    fr[r] = 0.0f;
                     if (r < np) {
                         const float sv = sig[pl[r]];
-                        fr[r] = (sv == sw) ? 1.0f : __fdiv_rn(sv, sw);
+                        bw_pl[r * 32 + lane] = pl[r];
+                        bw_fr[r * 32 + lane] = (sv == sw) ? 1.0f : __fdiv_rn(sv, sw);
                     }
                 }
                 float *dli = dl + (size_t)i * L;
@@ -643,12 +644,13 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
                     const float dep = fadd(seed, __ldcg(&dli[k]));
                     const float depb = fadd(seedb, __ldcg(&dli[K + k]));
                     if (dep == 0.0f && depb == 0.0f) continue;
-#pragma unroll
-                    for (int r = 0; r < PM; r++) {
-                        if (r >= np || fr[r] == 0.0f) continue;
-                        float *pd = dl + (size_t)pl[r] * L;
-                        atomicAdd(&pd[k], fmul(fr[r], dep));
-                        atomicAdd(&pd[K + k], fmul(fr[r], depb));
+#pragma unroll 1
+                    for (int r = 0; r < np; r++) {
+                        const float f = bw_fr[r * 32 + lane];
+                        if (f == 0.0f) continue;
+                        float *pd = dl + (size_t)bw_pl[r * 32 + lane] * L;
+                        atomicAdd(&pd[k], fmul(f, dep));
+                        atomicAdd(&pd[K + k], fmul(f, depb));
                     }
                     if (v == src) continue;
                     const float credit = __fadd_rn(dep, -seed);
@@ -945,7 +947,8 @@ CS_PHASE_INLINE __device__ void tree_rows(const PrimalParams &p, const SlotPtrs 
 // instruction-cache footprint, to what that mode runs); -1 dispatches on p.mode at run time.
 template <int PM, int MODE>
 __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs &s, int li, int src, uint32_t *hist,
-                                           int *cnt, long long *ph, long long &relaxed, long long &settled) {
+                                           int *cnt, int *bw_pl, float *bw_fr, long long *ph, long long &relaxed,
+                                           long long &settled) {
     const int lane = lane_id();
     long long t0 = clock64();
     const int R = warp_search(p, s, src, relaxed);
@@ -972,13 +975,13 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
     __syncwarp();
     phase_mark(ph, 1, t0);
     if constexpr (MODE == MODE_SHORTEST) {
-        shortest_accumulate<PM>(p, s, src, R, ph, cnt);
+        shortest_accumulate<PM>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
     } else if constexpr (MODE == MODE_SEGMENT) {
         segment_accumulate<PM>(p, s, src, R);
     } else if constexpr (MODE == MODE_TREE) {
         tree_rows<PM>(p, s, li, R);
     } else {
-        if (p.mode == MODE_SHORTEST) shortest_accumulate<PM>(p, s, src, R, ph, cnt);
+        if (p.mode == MODE_SHORTEST) shortest_accumulate<PM>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
         else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
         else tree_rows<PM>(p, s, li, R);
     }
@@ -1015,6 +1018,9 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][2 * MAXK];
     __shared__ long long ph_all[8][8];
+    // backward sweep: each lane's predecessor rows and sigma fractions (column-major per warp)
+    __shared__ int bw_pl_all[8][PM * 32];
+    __shared__ float bw_fr_all[8][PM * 32];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
@@ -1031,7 +1037,8 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
         if (idx >= (unsigned long long)p.n_src) break;
         if (__ldcg(&p.hdr->err) != 0u) break;
         const int li = p.remap ? p.remap[idx] : (int)idx;
-        if (run_source<PM, MODE>(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled))
+        if (run_source<PM, MODE>(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], bw_pl_all[wib], bw_fr_all[wib],
+                                 ph, relaxed, settled))
             done_src++;
     }
     flush_counters(p, ph, relaxed, settled, done_src);
@@ -1084,6 +1091,9 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][2 * MAXK];
     __shared__ long long ph_all[8][8];
+    // backward sweep: each lane's predecessor rows and sigma fractions (column-major per warp)
+    __shared__ int bw_pl_all[8][PM * 32];
+    __shared__ float bw_fr_all[8][PM * 32];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
@@ -1112,7 +1122,8 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
         }
         const int li = (int)(item - jobs[jb].item_begin);
         // failures record the global item index
-        if (run_source<PM, -1>(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled))
+        if (run_source<PM, -1>(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], bw_pl_all[wib],
+                               bw_fr_all[wib], ph, relaxed, settled))
             done_src++;
     }
     flush_counters(base, ph, relaxed, settled, done_src);
