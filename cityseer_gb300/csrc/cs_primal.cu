@@ -472,10 +472,14 @@ __device__ __forceinline__ int load_preds(const SlotPtrs &s, int i, int P, int *
     return np;
 }
 
-template <int PM>
+// With SYNC, every warp of the block runs each phase together (a block barrier ends each phase,
+// and a warp without a source runs the phases with R = 0), so at any time a block's warps fetch one
+// phase's code; there is no early return in that form.
+template <int PM, bool SYNC>
 CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R, long long *ph,
                                     int *cnt, int *bw_pl, float *bw_fr) {
     const int lane = lane_id();
+    bool failed = false;
     long long tph = clock64();
     const int K = p.k;
     const int P = p.P;
@@ -519,6 +523,7 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
         if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 1);
     }
     __syncwarp();
+    if constexpr (SYNC) __syncthreads();
     phase_mark(ph, 2, tph);
     // --- closeness (rust/src/centrality.rs:1733-1780).  Density, farness and harmonic terms do not
     // depend on the threshold: they go once into the bucket of the first qualifying threshold and a
@@ -557,8 +562,9 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
             }
         }
     }
+    if constexpr (SYNC) __syncthreads();
     phase_mark(ph, 3, tph);
-    if (!p.betweenness) return;
+    if (!p.betweenness) return;  // uniform over the block
     // --- sigma (f32 path counts) in settle order, chunked: ready once in-chunk preds are done
     float *sig = (float *)s.sig;
     for (int base = 0; base < R; base += 32) {
@@ -589,9 +595,11 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
         }
         if (done != FULL) {
             if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 2);
-            return;
+            failed = true;
+            break;
         }
     }
+    if constexpr (SYNC) __syncthreads();
     phase_mark(ph, 4, tph);
     // --- backward Brandes sweep, all K thresholds in one pass (rust/src/centrality.rs:823-873,
     // 1782-1835).  Dependencies accumulate in f32: for sources whose paths are unique (sigma == 1)
@@ -603,7 +611,7 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     __syncwarp();
     const bool unit_wt = (wt == 1.0f);
     const double wtd = (double)wt;
-    const int nchunks = (R + 31) / 32;
+    const int nchunks = failed ? 0 : (R + 31) / 32;
     for (int ch = nchunks - 1; ch >= 0; ch--) {
         const int base = ch * 32;
         const int i = base + lane;
@@ -668,9 +676,10 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
         }
         if (done != FULL) {
             if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 3);
-            return;
+            break;
         }
     }
+    if constexpr (SYNC) __syncthreads();
     phase_mark(ph, 5, tph);
 }
 
@@ -975,13 +984,13 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
     __syncwarp();
     phase_mark(ph, 1, t0);
     if constexpr (MODE == MODE_SHORTEST) {
-        shortest_accumulate<PM>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
+        shortest_accumulate<PM, false>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
     } else if constexpr (MODE == MODE_SEGMENT) {
         segment_accumulate<PM>(p, s, src, R);
     } else if constexpr (MODE == MODE_TREE) {
         tree_rows<PM>(p, s, li, R);
     } else {
-        if (p.mode == MODE_SHORTEST) shortest_accumulate<PM>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
+        if (p.mode == MODE_SHORTEST) shortest_accumulate<PM, false>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
         else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
         else tree_rows<PM>(p, s, li, R);
     }
@@ -1040,6 +1049,93 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
         if (run_source<PM, MODE>(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], bw_pl_all[wib], bw_fr_all[wib],
                                  ph, relaxed, settled))
             done_src++;
+    }
+    flush_counters(p, ph, relaxed, settled, done_src);
+}
+
+// ------------------------------------------------------------------------------------------
+// Shortest-path form with block-synchronous phases: a block claims one source per warp, and its
+// warps run search, sort, replay, closeness, sigma, backward and reset together, a block barrier
+// between phases.  At any time a block fetches one phase's code, so the SM's instruction caches
+// hold the code of at most one phase per resident block.  Every warp reaches every barrier: a warp
+// without a source (or whose source overflowed) runs the phases with R = 0.
+// ------------------------------------------------------------------------------------------
+template <int PM, int MINB>
+__global__ void __launch_bounds__(256, MINB) primal_sync_kernel(const PrimalParams p) {
+    __shared__ uint32_t hist_all[8][256];
+    __shared__ int cnt_all[8][2 * MAXK];
+    __shared__ long long ph_all[8][8];
+    __shared__ int bw_pl_all[8][PM * 32];
+    __shared__ float bw_fr_all[8][PM * 32];
+    __shared__ long long blk_base;
+    __shared__ unsigned blk_err;
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    const int slot0 = blockIdx.x * (blockDim.x >> 5);
+    const int nw = min((int)(blockDim.x >> 5), p.n_slots - slot0);  // warps of this block with a slot
+    const bool has_slot = wib < nw;
+    const SlotPtrs s = slot_ptrs(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.P, p.L,
+                                 has_slot ? slot0 + wib : 0, p.g.n_bound);
+    long long relaxed = 0, settled = 0, done_src = 0;
+    long long *ph = ph_all[wib];
+    if (lane < 8) ph[lane] = 0;
+    __syncwarp();
+    const long long n = p.n_src;
+    while (true) {
+        if (threadIdx.x == 0) {
+            blk_base = (long long)atomicAdd(p.rerun ? &p.hdr->work_next2 : &p.hdr->work_next,
+                                            (unsigned long long)max(nw, 0));
+            blk_err = __ldcg(&p.hdr->err);
+        }
+        __syncthreads();
+        const long long base = blk_base;
+        const unsigned berr = blk_err;
+        __syncthreads();
+        if (nw <= 0 || base >= n || berr != 0u) break;
+        const long long idx = base + wib;
+        const bool mine = has_slot && idx < n;
+        const int li = mine ? (p.remap ? p.remap[idx] : (int)idx) : 0;
+        const int src = mine ? p.src_list[li] : 0;
+        long long t0 = clock64();
+        int R = 0;
+        if (mine) R = warp_search(p, s, src, relaxed);
+        phase_mark(ph, 0, t0);
+        __syncthreads();
+        const bool ok = mine && R >= 0;
+        if (mine && R < 0) {
+            for (int j = lane; j < p.g.n_bound; j += 32) {
+                s.dist[j] = __int_as_float(INF_BITS);
+                s.aux[j] = 0u;
+            }
+            if (lane == 0) {
+                const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
+                if (f < (unsigned)p.fail_cap) p.failed[f] = li;
+                else raise_err(p.hdr, CS_ERR_CAPACITY, 8);
+            }
+        }
+        if (ok) {
+            warp_sort(s, R, hist_all[wib]);
+            __syncwarp();
+            for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+        }
+        __syncwarp();
+        phase_mark(ph, 1, t0);
+        __syncthreads();
+        shortest_accumulate<PM, true>(p, s, src, ok ? R : 0, ph, cnt_all[wib], bw_pl_all[wib], bw_fr_all[wib]);
+        __syncwarp();
+        t0 = clock64();
+        if (ok) {
+            for (int i = lane; i < R; i += 32) {
+                const int v = s.ord[i];
+                s.dist[v] = __int_as_float(INF_BITS);
+                s.aux[v] = 0u;
+            }
+            settled += R;
+            done_src++;
+        }
+        __syncwarp();
+        phase_mark(ph, 6, t0);
+        __syncthreads();
     }
     flush_counters(p, ph, relaxed, settled, done_src);
 }
@@ -1306,8 +1402,19 @@ cudaError_t occupancy_blocks(int P, int variant, int *bpsm) {
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 2, 0>, 256, 0);
 }
 
+// Block-synchronous phases for the shortest-path mode (CS_PHASE_SYNC=0 selects the per-warp form).
+bool phase_sync() {
+    const char *e = getenv("CS_PHASE_SYNC");
+    return !(e && e[0] == '0');
+}
+
 template <int MODE>
 void launch_primal_mode(const cs::PrimalParams &p, int P, int minb, int blocks, cudaStream_t stream) {
+    if (MODE == cs::MODE_SHORTEST && P <= 8 && phase_sync()) {
+        if (minb == 3) cs::primal_sync_kernel<8, 3><<<blocks, 256, 0, stream>>>(p);
+        else cs::primal_sync_kernel<8, 2><<<blocks, 256, 0, stream>>>(p);
+        return;
+    }
     if (P <= 8) {
         if (minb == 3) cs::primal_kernel<8, 3, MODE><<<blocks, 256, 0, stream>>>(p);
         else cs::primal_kernel<8, 2, MODE><<<blocks, 256, 0, stream>>>(p);
