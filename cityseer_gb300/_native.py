@@ -171,6 +171,8 @@ SIGNATURES = {
             C.c_int32, _ptr, _ptr, _ptr, _ptr, _ptr, _ptr,
         ],
     ),
+    "cs_plan_dual_tree": (C.c_int32, [C.POINTER(DualGraph), C.c_int32, C.c_int32, C.c_int64, C.POINTER(Plan)]),
+    "cs_dual_tree_workspace_init": (C.c_int32, [C.POINTER(Plan), _ptr, C.c_size_t, _ptr]),
     "cs_last_counters": (C.c_int32, [C.POINTER(C.c_int64)] * 4),
     "cs_batch_prepare": (C.c_int32, [C.POINTER(BatchJob), C.c_int32, C.POINTER(C.c_int64)]),
     "cs_batch_plan": (C.c_int32, [C.POINTER(BatchJob), C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.POINTER(Plan)]),

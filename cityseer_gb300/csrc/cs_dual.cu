@@ -880,6 +880,190 @@ __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
     }
 }
 
+// ------------------------------------------------------------------------------------------
+// Simplest-path trees: dijkstra_tree_angular (rust/src/centrality.rs:1202-1332), one query per
+// warp, run by lane 0 in the reference's exact heap order (Rust BinaryHeap restated by
+// heap_sift_up / tree_heap_pop).  This search is heap-order dependent by construction: it accepts
+// tied offers within an absolute epsilon, updates already-visited states, and keeps a node-level
+// best with its own epsilon rule, so it is replayed sequentially rather than label-corrected.
+// Per slot: dense state records [2N] and node positions [N] (zero = untouched), compact rows
+// (node, simpl_dist, agg_seconds, pred) in first-reach order and the heap.
+// ------------------------------------------------------------------------------------------
+struct DTreeState {
+    float route, simpl, agg;
+    uint32_t flags;  // 1: touched, 2: visited
+};
+struct DTreeRow {
+    int32_t node;
+    float simpl, agg;
+    int32_t pred;
+};
+struct DTreeParams {
+    cs_dual_graph g;
+    const int32_t *src;
+    const int32_t *remap;  // retry pass: query indices to run
+    long long n_items;
+    float maxsec;
+    char *dense;
+    size_t dense_stride;
+    int geo_n;
+    char *compact;
+    size_t compact_stride;
+    int cap, hcap;
+    int32_t row_cap;
+    int32_t *t_count, *t_node, *t_pred;
+    float *t_simpl, *t_agg;
+    int32_t *failed;
+    int fail_cap;
+    int final_pass;
+    int n_slots;
+    WsHeader *hdr;
+};
+
+// pop of a Rust BinaryHeap (sift_down_to_bottom, then sift_up): returns the top state
+__device__ __forceinline__ int32_t tree_heap_pop(int32_t *h, int &len) {
+    len--;
+    const int32_t s_top = h[1];
+    if (len > 0) {
+        const int32_t m_last = h[2 * len], s_last = h[2 * len + 1];
+        int pos = 0, child = 1;
+        const int end = len;
+        while (end >= 2 && child <= end - 2) {
+            child += hle(h, child, child + 1) ? 1 : 0;
+            h[2 * pos] = h[2 * child];
+            h[2 * pos + 1] = h[2 * child + 1];
+            pos = child;
+            child = 2 * pos + 1;
+        }
+        if (child == end - 1) {
+            h[2 * pos] = h[2 * child];
+            h[2 * pos + 1] = h[2 * child + 1];
+            pos = child;
+        }
+        h[2 * pos] = m_last;
+        h[2 * pos + 1] = s_last;
+        heap_sift_up(h, 0, pos);
+    }
+    return s_top;
+}
+
+// Returns the number of reached nodes, or -1 when the rows or the heap overflowed.
+__device__ int dual_tree_search(const DTreeParams &p, DTreeState *S, uint32_t *pos, DTreeRow *rows, int32_t *h,
+                                int src) {
+    const float eps = TIE_EPSILON;
+    int n = 0, len = 0;
+    pos[src] = 1u;
+    rows[0] = DTreeRow{src, 0.0f, 0.0f, -1};
+    n = 1;
+    for (int sl = 0; sl < 2; sl++) {
+        const int st = 2 * src + sl;
+        S[st] = DTreeState{0.0f, 0.0f, 0.0f, 1u};
+        h[2 * len] = 0;
+        h[2 * len + 1] = st;
+        len++;
+        heap_sift_up(h, 0, len - 1);
+    }
+    while (len > 0) {
+        const int st = tree_heap_pop(h, len);
+        if (S[st].flags & 2u) continue;
+        S[st].flags |= 2u;
+        const int cur = st >> 1, entry = st & 1;
+        const DTreeState cs0 = S[st];
+        const int beg = __ldg(&p.g.ptr_dev[cur]), end = __ldg(&p.g.ptr_dev[cur + 1]);
+        for (int e = beg; e < end; e++) {
+            if (__ldg(&p.g.exit_slot_dev[e]) != 1 - entry) continue;
+            const int nx = __ldg(&p.g.to_dev[e]);
+            const int nst = 2 * nx + __ldg(&p.g.entry_slot_dev[e]);
+            const float csec = __fadd_rn(cs0.agg, __ldg(&p.g.w_dev[e]));
+            if (csec > p.maxsec) continue;
+            const float csimpl = __fadd_rn(cs0.simpl, __ldg(&p.g.ang_dev[e]));
+            const float cm = __fadd_rn(csimpl, __fmul_rn(ANGULAR_TIE_BREAK, __ldg(&p.g.len_dev[e])));
+            const DTreeState nxs = S[nst];
+            const bool touched = (nxs.flags & 1u) != 0u;
+            const float nroute = touched ? nxs.route : __int_as_float(INF_BITS);
+            const float nagg = touched ? nxs.agg : __int_as_float(INF_BITS);
+            const bool improved = __fadd_rn(cm, eps) < nroute;
+            const bool tied = fabsf(__fadd_rn(cm, -nroute)) <= eps;
+            if (!(improved || (tied && csec < nagg && st != nst))) continue;
+            S[nst] = DTreeState{cm, csimpl, csec, 1u | (nxs.flags & 2u)};
+            if (len >= p.hcap) return -1;
+            h[2 * len] = (int32_t)__float_as_uint(cm);
+            h[2 * len + 1] = nst;
+            len++;
+            heap_sift_up(h, 0, len - 1);
+            uint32_t ps = pos[nx];
+            if (ps == 0u) {
+                if (n >= p.cap) return -1;
+                pos[nx] = (uint32_t)(n + 1);
+                rows[n] = DTreeRow{nx, csimpl, csec, cur};
+                n++;
+                continue;
+            }
+            DTreeRow &r = rows[ps - 1];
+            const bool node_improved = __fadd_rn(csimpl, eps) < r.simpl;
+            const bool node_tied = fabsf(__fadd_rn(csimpl, -r.simpl)) <= eps;
+            if (node_improved || (node_tied && csec < r.agg)) r = DTreeRow{nx, csimpl, csec, cur};
+        }
+    }
+    return n;
+}
+
+__global__ void __launch_bounds__(256) dual_tree_kernel(const DTreeParams p) {
+    const int lane = lane_id();
+    const int slot = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
+    if (slot >= p.n_slots) return;
+    char *d = p.dense + p.dense_stride * (size_t)slot;
+    DTreeState *S = (DTreeState *)d;
+    uint32_t *pos = (uint32_t *)(d + al256((size_t)p.geo_n * 2 * sizeof(DTreeState)));
+    char *c = p.compact + p.compact_stride * (size_t)slot;
+    DTreeRow *rows = (DTreeRow *)c;
+    int32_t *h = (int32_t *)(c + al256((size_t)p.cap * sizeof(DTreeRow)));
+    while (true) {
+        unsigned long long idx = 0;
+        if (lane == 0) idx = atomicAdd(p.remap ? &p.hdr->work_next2 : &p.hdr->work_next, 1ull);
+        idx = __shfl_sync(FULL, idx, 0);
+        if ((long long)idx >= p.n_items) break;
+        const int q = p.remap ? p.remap[idx] : (int)idx;
+        const int src = p.src[q];
+        int n = 0;
+        if (lane == 0) n = dual_tree_search(p, S, pos, rows, h, src);
+        n = __shfl_sync(FULL, n, 0);
+        __syncwarp();
+        if (n < 0) {
+            // rows or heap overflowed: the touched entries are not all listed, so clear the slot
+            for (size_t j = lane; j < (size_t)p.g.n_bound * 2; j += 32) S[j] = DTreeState{0.0f, 0.0f, 0.0f, 0u};
+            for (int j = lane; j < p.g.n_bound; j += 32) pos[j] = 0u;
+            if (lane == 0) {
+                if (p.final_pass) {
+                    raise_err(p.hdr, CS_ERR_CAPACITY, 30);
+                } else {
+                    const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
+                    if (f < (unsigned)p.fail_cap) p.failed[f] = q;
+                    else raise_err(p.hdr, CS_ERR_CAPACITY, 31);
+                }
+            }
+            __syncwarp();
+            continue;
+        }
+        const bool fits = n <= p.row_cap;
+        for (int i = lane; i < n; i += 32) {
+            const DTreeRow r = rows[i];
+            if (fits) {
+                const size_t o = (size_t)q * p.row_cap + i;
+                p.t_node[o] = r.node;
+                p.t_simpl[o] = r.simpl;
+                p.t_agg[o] = r.agg;
+                p.t_pred[o] = r.pred;
+            }
+            S[2 * r.node] = DTreeState{0.0f, 0.0f, 0.0f, 0u};
+            S[2 * r.node + 1] = DTreeState{0.0f, 0.0f, 0.0f, 0u};
+            pos[r.node] = 0u;
+        }
+        if (lane == 0) p.t_count[q] = fits ? n : -n;
+        __syncwarp();
+    }
+}
+
 __global__ void fill_dual_dense(char *dense, size_t stride, int n_bound, int n_slots) {
     const size_t per = 2 * (size_t)n_bound;
     const size_t total = per * (size_t)n_slots;
@@ -945,6 +1129,29 @@ DLayout dlayout(int n_bound, int n_slots, int cap, int K) {
     l.compact_off = l.dense_off + l.dense_stride * (size_t)n_slots;
     l.compact_total = std::max(csd::compact_bytes_d((size_t)cap, K) * (size_t)n_slots,
                                csd::compact_bytes_d(2 * (size_t)n_bound, K));
+    l.total = l.compact_off + l.compact_total;
+    return l;
+}
+
+// Tree workspace: header, failed list, per-slot dense (state records + node positions), per-slot
+// compact (rows + heap of 4 x cap entries; the full-size retry uses cap = N with 8 x N entries).
+struct TLayout {
+    size_t failed_off, dense_off, dense_stride, compact_off, compact_total, total;
+    int fail_cap;
+};
+size_t tcompact_bytes_h(size_t cap, size_t hcap) {
+    return csd::al256(cap * sizeof(csd::DTreeRow)) + csd::al256(hcap * 8);
+}
+size_t tcompact_bytes(size_t cap) { return tcompact_bytes_h(cap, 4 * cap); }
+TLayout tlayout(int n_bound, int n_slots, int cap) {
+    TLayout l;
+    l.fail_cap = std::max(n_slots, 1 << 16);
+    l.failed_off = 256;
+    l.dense_off = csd::al256(l.failed_off + 4 * (size_t)l.fail_cap);
+    l.dense_stride = csd::al256((size_t)n_bound * 2 * sizeof(csd::DTreeState)) + csd::al256((size_t)n_bound * 4);
+    l.compact_off = l.dense_off + l.dense_stride * (size_t)n_slots;
+    l.compact_total = std::max(tcompact_bytes((size_t)cap) * (size_t)n_slots,
+                               tcompact_bytes_h((size_t)n_bound, 8 * (size_t)n_bound));
     l.total = l.compact_off + l.compact_total;
     return l;
 }
@@ -1148,9 +1355,107 @@ cs_status cs_dual_workspace_init(const cs_plan *plan, int32_t n_bound, void *ws,
     return dreset((char *)ws + lay.dense_off, lay.dense_stride, n_bound, plan->n_slots, (cudaStream_t)stream);
 }
 
-cs_status cs_tree_simplest(const cs_dual_graph *, int32_t, const int32_t *, uint32_t, float, const cs_plan *, void *,
-                           size_t, int32_t, int32_t *, int32_t *, float *, float *, int32_t *, void *) {
-    return dfail(CS_ERR_ARG, "dijkstra_tree_simplest is not available on the GPU yet");
+cs_status cs_plan_dual_tree(const cs_dual_graph *g, int32_t cap, int32_t max_slots, int64_t mem_budget_bytes,
+                            cs_plan *plan) {
+    cs_status st = dvalidate(g);
+    if (st != CS_OK) return st;
+    if (!plan) return dfail(CS_ERR_ARG, "plan is NULL");
+    const int sms = dsm_count();
+    if (sms <= 0) return dfail(CS_ERR_CUDA, "no CUDA device");
+    int slots = sms * 8;
+    if (max_slots > 0) slots = std::min(slots, max_slots);
+    if (cap <= 0) cap = std::min(g->n_bound, 16384);
+    cap = std::max(64, std::min(cap, g->n_bound));
+    if (mem_budget_bytes > 0)
+        while (slots > 8 && (int64_t)tlayout(g->n_bound, slots, cap).total > mem_budget_bytes) slots = slots * 7 / 8;
+    plan->n_slots = std::max(1, slots);
+    plan->cap = cap;
+    plan->threads_per_block = 256;
+    plan->blocks = (plan->n_slots + 7) / 8;
+    plan->lanes = 1;
+    plan->n_bound = g->n_bound;
+    plan->workspace_bytes = tlayout(g->n_bound, plan->n_slots, cap).total;
+    return CS_OK;
+}
+
+cs_status cs_dual_tree_workspace_init(const cs_plan *plan, void *ws, size_t ws_bytes, void *stream) {
+    if (!plan || !ws) return dfail(CS_ERR_ARG, "plan/workspace is NULL");
+    if (ws_bytes < plan->workspace_bytes) return dfail(CS_ERR_ARG, "workspace smaller than plan");
+    const TLayout lay = tlayout(plan->n_bound, plan->n_slots, plan->cap);
+    cudaError_t e = cudaMemsetAsync(ws, 0, lay.compact_off, (cudaStream_t)stream);  // header, lists, dense
+    return e == cudaSuccess ? CS_OK : dcuda(e, "tree workspace init");
+}
+
+cs_status cs_tree_simplest(const cs_dual_graph *g, int32_t n_queries, const int32_t *src_dev, uint32_t max_seconds,
+                           float speed_m_s, const cs_plan *plan, void *ws, size_t ws_bytes, int32_t row_cap,
+                           int32_t *count_dev, int32_t *node_dev, float *simpl_dev, float *agg_seconds_dev,
+                           int32_t *pred_dev, void *stream_v) {
+    cs_status st = dvalidate(g);
+    if (st != CS_OK) return st;
+    if (!plan || !ws) return dfail(CS_ERR_ARG, "plan/workspace is NULL");
+    if (n_queries < 0 || (n_queries > 0 && !src_dev)) return dfail(CS_ERR_ARG, "bad query list");
+    if (!count_dev || !node_dev || !simpl_dev || !agg_seconds_dev || !pred_dev || row_cap <= 0)
+        return dfail(CS_ERR_ARG, "tree outputs missing");
+    if (!(speed_m_s > 0.0f)) return dfail(CS_ERR_ARG, "speed_m_s must be finite and positive");
+    const int geo_n = plan->n_bound > 0 ? plan->n_bound : g->n_bound;
+    if (geo_n < g->n_bound) return dfail(CS_ERR_ARG, "plan was made for a smaller graph");
+    const TLayout lay = tlayout(geo_n, plan->n_slots, plan->cap);
+    if (ws_bytes < lay.total) return dfail(CS_ERR_ARG, "workspace too small for this plan");
+    if (n_queries == 0) return CS_OK;
+    cudaStream_t s = (cudaStream_t)stream_v;
+    char *base = (char *)ws;
+    csd::DTreeParams p;
+    memset(&p, 0, sizeof(p));
+    p.g = *g;
+    p.src = src_dev;
+    p.n_items = n_queries;
+    p.maxsec = (float)max_seconds;
+    p.dense = base + lay.dense_off;
+    p.dense_stride = lay.dense_stride;
+    p.geo_n = geo_n;
+    p.compact = base + lay.compact_off;
+    p.compact_stride = tcompact_bytes(plan->cap);
+    p.cap = plan->cap;
+    p.hcap = 4 * plan->cap;
+    p.row_cap = row_cap;
+    p.t_count = count_dev;
+    p.t_node = node_dev;
+    p.t_pred = pred_dev;
+    p.t_simpl = simpl_dev;
+    p.t_agg = agg_seconds_dev;
+    p.failed = (int32_t *)(base + lay.failed_off);
+    p.fail_cap = lay.fail_cap;
+    p.hdr = (cs::WsHeader *)base;
+    p.n_slots = std::max(1, std::min(plan->n_slots, n_queries));
+    cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), s);
+    if (e != cudaSuccess) return dcuda(e, "tree header reset");
+    csd::dual_tree_kernel<<<(p.n_slots + 7) / 8, 256, 0, s>>>(p);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return dcuda(e, "dual_tree_kernel launch");
+    cs::WsHeader h;
+    st = dsync_header(p.hdr, h, s);
+    if (st != CS_OK) return st;
+    if (h.n_failed > 0u) {
+        // queries whose rows or heap overflowed: again with every node's row and a larger heap, on as
+        // many slots as the compact region holds at that size
+        csd::DTreeParams p2 = p;
+        p2.cap = g->n_bound;
+        p2.hcap = 8 * g->n_bound;
+        p2.compact_stride = tcompact_bytes_h(p2.cap, p2.hcap);
+        p2.remap = p.failed;
+        p2.n_items = std::min<unsigned>(h.n_failed, (unsigned)lay.fail_cap);
+        p2.final_pass = 1;
+        p2.n_slots = (int)std::max<size_t>(1, std::min<size_t>(lay.compact_total / p2.compact_stride,
+                                                                 (size_t)std::min<long long>(p2.n_items, p.n_slots)));
+        if (lay.compact_total < p2.compact_stride)
+            return dfail(CS_ERR_CAPACITY, "tree workspace cannot hold one full-size search");
+        csd::dual_tree_kernel<<<(p2.n_slots + 7) / 8, 256, 0, s>>>(p2);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return dcuda(e, "dual_tree_kernel launch");
+        st = dsync_header(p.hdr, h, s);
+        if (st != CS_OK) return st;
+    }
+    return CS_OK;
 }
 
 }  // extern "C"

@@ -224,5 +224,75 @@ def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, between
     return res
 
 
+class DualTreeWorkspace(device.Workspace):
+    def init(self, stream=None):
+        lib = _native.load()
+        _native.check(lib.cs_dual_tree_workspace_init(C.byref(self.plan), self.ptr, self.nbytes, stream),
+                      "cs_dual_tree_workspace_init")
+
+
+def tree_workspace(ns, csr: DualCSR, n_queries: int, speed: float):
+    """The dual graph's simplest-path tree workspace (capacity from the dual's metric reach)."""
+    from .centrality import _mem_budget
+
+    ws = ns._cache.get("wsdt")
+    if ws is None:
+        lib = _native.load()
+        plan = _native.Plan()
+        _native.check(lib.cs_plan_dual_tree(C.byref(csr.struct(speed)), 0, 0, _mem_budget(csr.device) // 4,
+                                            C.byref(plan)), "cs_plan_dual_tree")
+        ws = DualTreeWorkspace(plan, csr.n_bound, csr.device)
+        ns._cache["wsdt"] = ws
+    return ws
+
+
+def tree_simplest_raw(ns, sources, max_seconds: int, speed: float, row_cap: int | None = None):
+    """Batched simplest-path trees on the GPU: (counts, nodes, simpl_dist, agg_seconds, preds), rows
+    in first-reach order, row_cap wide."""
+    from .centrality import _stream_ptr
+
+    csr = dual_csr(ns)
+    dev = csr.device
+    nq = len(sources)
+    nb = csr.n_bound
+    if row_cap is None:
+        row_cap = nb
+    ws = tree_workspace(ns, csr, nq, speed)
+    lib = _native.load()
+    src_t = torch.tensor(list(sources), dtype=torch.int32, device=dev)
+    count = torch.zeros(max(nq, 1), dtype=torch.int32, device=dev)
+    node = torch.empty((max(nq, 1), row_cap), dtype=torch.int32, device=dev)
+    simpl = torch.empty((max(nq, 1), row_cap), dtype=torch.float32, device=dev)
+    agg = torch.empty((max(nq, 1), row_cap), dtype=torch.float32, device=dev)
+    pred = torch.empty((max(nq, 1), row_cap), dtype=torch.int32, device=dev)
+    rc = lib.cs_tree_simplest(C.byref(csr.struct(speed)), nq, src_t.data_ptr() if nq else None, int(max_seconds),
+                              C.c_float(speed), C.byref(ws.plan), ws.ptr, ws.nbytes, row_cap, count.data_ptr(),
+                              node.data_ptr(), simpl.data_ptr(), agg.data_ptr(), pred.data_ptr(), _stream_ptr())
+    if rc != _native.CS_OK:
+        ws.init(_stream_ptr())
+    _native.check(rc, "cs_tree_simplest")
+    return (count.cpu().numpy()[:nq], node.cpu().numpy()[:nq], simpl.cpu().numpy()[:nq], agg.cpu().numpy()[:nq],
+            pred.cpu().numpy()[:nq])
+
+
 def tree_simplest(ns, sources, max_seconds, speed):
-    raise NotImplementedError("dijkstra_tree_simplest is not available on the GPU yet")
+    """Per source: (visited_nodes, list[NodeVisit]) exactly as dijkstra_tree_simplest returns."""
+    from .graph import NodeVisit
+
+    counts, nodes, simpl, agg, preds = tree_simplest_raw(ns, sources, max_seconds, speed)
+    nb = ns.node_bound()
+    out = []
+    for q in range(len(sources)):
+        n = int(counts[q])
+        tree = [NodeVisit() for _ in range(nb)]
+        visited = nodes[q, :n].tolist()
+        for i in range(n):
+            t = tree[int(nodes[q, i])]
+            t.visited = True
+            t.discovered = True
+            t.simpl_dist = float(simpl[q, i])
+            t.agg_seconds = float(agg[q, i])
+            p = int(preds[q, i])
+            t.pred = None if p < 0 else p
+        out.append((visited, tree))
+    return out

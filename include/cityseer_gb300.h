@@ -213,7 +213,14 @@ cs_status cs_tree_shortest(const cs_primal_graph *g, int32_t n_queries, const in
                            int32_t *pred_dev, void *stream);
 
 /* Same for dijkstra_tree_simplest (rust/src/centrality.rs:1202-1332, 1510-1521) on a dual graph:
- * per query, reached dual nodes with simpl_dist, agg_seconds and node-level predecessor. */
+ * per query, reached dual nodes in first-reach order with their final simpl_dist, agg_seconds and
+ * node-level predecessor (-1 for the source).  count_dev[q] = number reached, or minus that number
+ * when it exceeds row_cap.  The plan and workspace come from cs_plan_dual_tree /
+ * cs_dual_tree_workspace_init; queries whose search outgrows the plan's capacity are redone in the
+ * call at full size. */
+cs_status cs_plan_dual_tree(const cs_dual_graph *g, int32_t cap, int32_t max_slots, int64_t mem_budget_bytes,
+                            cs_plan *plan);
+cs_status cs_dual_tree_workspace_init(const cs_plan *plan, void *workspace_dev, size_t workspace_bytes, void *stream);
 cs_status cs_tree_simplest(const cs_dual_graph *g, int32_t n_queries, const int32_t *src_dev, uint32_t max_seconds,
                            float speed_m_s, const cs_plan *plan, void *workspace_dev, size_t workspace_bytes,
                            int32_t row_cap, int32_t *count_dev, int32_t *node_dev, float *simpl_dev,

@@ -48,3 +48,61 @@ def test_trees_bit_exact():
                 dref = t_ref["agg_seconds"][vis_ref]
                 if len(np.unique(dref)) == len(dref):
                     assert visited == vis_ref.tolist()
+
+
+def _simplest_trees_match(ns, srcs, max_seconds, row_cap=None):
+    from cityseer_gb300 import dual
+
+    og = oracle.OracleGraph(ns)
+    counts, nodes, simpl, agg, preds = dual.tree_simplest_raw(ns, srcs, max_seconds, 1.33333, row_cap=row_cap)
+    for q, src in enumerate(srcs):
+        vis_ref, t_ref = oracle.tree_simplest(og, src, max_seconds, 1.33333)
+        n = int(counts[q])
+        assert n == len(vis_ref), (src, max_seconds, n, len(vis_ref))
+        np.testing.assert_array_equal(nodes[q, :n], vis_ref, err_msg=f"reach order src {src}")
+        np.testing.assert_array_equal(simpl[q, :n], t_ref["simpl_dist"][vis_ref], err_msg=f"simpl src {src}")
+        np.testing.assert_array_equal(agg[q, :n], t_ref["agg_seconds"][vis_ref], err_msg=f"agg src {src}")
+        np.testing.assert_array_equal(preds[q, :n], t_ref["pred"][vis_ref], err_msg=f"pred src {src}")
+
+
+@pytest.mark.gpu
+def test_simplest_trees_bit_exact():
+    """dijkstra_tree_simplest on dual graphs: reach order, simpl_dist, agg_seconds and node-level
+    predecessor bit-exact against the oracle (heap-order restatement of dijkstra_tree_angular)."""
+    from cityseer_gb300.tools import graphs, io
+
+    mock_dual = io.network_structure_from_nx(graphs.nx_to_dual(mock_graph()))[2]
+    p, _ = synth.lattice_config("c3", side=14)
+    for ns in (mock_dual, synth.dual_structure(p)):
+        srcs = ns.node_indices()[::5]
+        for max_seconds in (0, 375, 1500, 3750):
+            _simplest_trees_match(ns, srcs, max_seconds)
+    # the public method and a plan smaller than the reach (queries redone at full size)
+    ns = synth.dual_structure(p)
+    visited, tree = ns.dijkstra_tree_simplest(ns.node_indices()[3], 1500, 1.33333)
+    vis_ref, t_ref = oracle.tree_simplest(oracle.OracleGraph(ns), ns.node_indices()[3], 1500, 1.33333)
+    assert visited == vis_ref.tolist()
+    assert all(np.float32(tree[v].simpl_dist) == t_ref["simpl_dist"][v] for v in vis_ref)
+
+
+@pytest.mark.gpu
+def test_simplest_trees_small_capacity():
+    import ctypes as C
+
+    import torch
+
+    from cityseer_gb300 import _native, dual
+
+    p, _ = synth.lattice_config("c3", side=12)
+    ns = synth.dual_structure(p)
+    csr = dual.dual_csr(ns)
+    lib = _native.load()
+    plan = _native.Plan()
+    _native.check(lib.cs_plan_dual_tree(C.byref(csr.struct(1.33333)), 64, 16, 0, C.byref(plan)), "plan")
+    ns._cache["wsdt"] = dual.DualTreeWorkspace(plan, csr.n_bound, csr.device)
+    srcs = ns.node_indices()[::9]
+    _simplest_trees_match(ns, srcs, 3750)
+    # rows narrower than the reach: counts come back negative
+    counts = dual.tree_simplest_raw(ns, srcs[:3], 3750, 1.33333, row_cap=8)[0]
+    assert (counts < 0).all()
+    torch.cuda.synchronize()
