@@ -471,6 +471,65 @@ def tree_shortest(ns, sources: list[int], max_seconds: int, speed: float):
     return out
 
 
+def tree_segment(ns, src: int, max_seconds: int, speed: float):
+    """dijkstra_tree_segment (rust/src/centrality.rs:1524-1611): (visited_nodes, visited_edges,
+    list[NodeVisit], list[EdgeVisit]).  The search (settle order, agg_seconds, strict-< first
+    predecessor) runs on the GPU tree kernel; the edge bookkeeping follows from it on the host: a
+    settled node lists its incoming edges from nodes not yet settled (self loops too), and a node's
+    last segment is the cheapest edge to its predecessor (first in that node's incoming order on ties).
+    """
+    from .graph import EdgeVisit, NodeVisit
+
+    counts, nodes, agg, preds = tree_shortest_raw(ns, [src], max_seconds, speed)
+    n = int(counts[0])
+    host = _primal_host(ns)
+    nb = ns.node_bound()
+    a = ns.arrays()
+    order = nodes[0, :n].astype(np.int64)
+    pos = np.full(nb, -1, np.int64)
+    pos[order] = np.arange(n)
+    in_ptr = host.h["in_ptr"].astype(np.int64)
+    in_nb = host.h["in_nb"].astype(np.int64)
+    in_slot = host.ex[host.in_order]
+    win = host.weights(speed)[0]
+    # visited edges, in settle order then incoming order
+    cnt = in_ptr[order + 1] - in_ptr[order]
+    rows = np.repeat(np.arange(n), cnt)
+    offs = np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+    ei = in_ptr[order][rows] + offs
+    u = order[rows]
+    v = in_nb[ei]
+    keep = (v == u) | (pos[v] < 0) | (pos[v] > rows)
+    visited_edges = in_slot[ei[keep]].tolist()
+    edge_map = [EdgeVisit() for _ in range(len(a["e_src"]))]
+    for e, uu, vv in zip(in_slot[ei[keep]].tolist(), u[keep].tolist(), v[keep].tolist()):
+        ev = edge_map[e]
+        ev.visited = True
+        ev.start_nd_idx = uu
+        ev.end_nd_idx = vv
+        ev.edge_idx = int(a["e_idx"][e])
+    tree = [NodeVisit() for _ in range(nb)]
+    sp32 = np.float32(speed)
+    for i in range(n):
+        x = int(order[i])
+        t = tree[x]
+        t.visited = True
+        t.discovered = True
+        t.agg_seconds = float(agg[0, i])
+        t.short_dist = float(np.float32(agg[0, i]) * sp32)
+        p = int(preds[0, i])
+        if p < 0:
+            continue
+        t.pred = p
+        # cheapest edge x -> p among the predecessor's incoming edges (first on ties)
+        lo, hi = int(in_ptr[p]), int(in_ptr[p + 1])
+        cand = [j for j in range(lo, hi) if in_nb[j] == x]
+        best = min(cand, key=lambda j: (win[j], j - lo))
+        t.last_seg = int(in_slot[best])
+        t.origin_seg = t.last_seg if p == src else tree[p].origin_seg
+    return order.tolist(), visited_edges, tree, edge_map
+
+
 def tree_simplest(ns, sources: list[int], max_seconds: int, speed: float):
     from . import dual
 

@@ -565,6 +565,13 @@ class NetworkStructure:
             self._validate_src(int(s), speed_m_s)
         return centrality.tree_shortest(self, list(src_indices), max_seconds, speed_m_s)
 
+    def dijkstra_tree_segment(self, src_idx: int, max_seconds: int, speed_m_s: float):
+        """(visited_nodes, visited_edges, tree_map, edge_map) as rust/src/centrality.rs:1524-1611."""
+        from . import centrality
+
+        self._validate_src(src_idx, speed_m_s)
+        return centrality.tree_segment(self, src_idx, max_seconds, speed_m_s)
+
     def dijkstra_tree_simplest(self, src_idx: int, max_seconds: int, speed_m_s: float):
         from . import centrality
 

@@ -106,3 +106,29 @@ def test_simplest_trees_small_capacity():
     counts = dual.tree_simplest_raw(ns, srcs[:3], 3750, 1.33333, row_cap=8)[0]
     assert (counts < 0).all()
     torch.cuda.synchronize()
+
+
+@pytest.mark.gpu
+def test_segment_trees_match_oracle():
+    """dijkstra_tree_segment: visited nodes and edges in order, agg_seconds, pred, origin and last
+    segments bit-exact against the oracle."""
+    for ns in (synth.primal_structure(synth.lattice_config("c1", side=12)[0]), structure(mock_graph())[2],
+               structure(diamond_graph())[2]):
+        og = oracle.OracleGraph(ns)
+        for src in ns.node_indices()[::5]:
+            for max_seconds in (0, 300, 1500):
+                vis, vedges, tree, emap = ns.dijkstra_tree_segment(src, max_seconds, 1.33333)
+                vis_ref, ve_ref, t_ref = oracle.tree_segment(og, src, max_seconds, 1.33333)
+                assert sorted(vis) == sorted(vis_ref.tolist())
+                dref = t_ref["agg_seconds"][vis_ref]
+                if len(np.unique(dref)) < len(dref):
+                    continue  # equal-distance settle ties follow the heap's internal order there
+                assert vis == vis_ref.tolist()
+                assert vedges == ve_ref.tolist()
+                for v in vis_ref:
+                    assert np.float32(tree[v].agg_seconds) == t_ref["agg_seconds"][v]
+                    assert (tree[v].pred if tree[v].pred is not None else -1) == t_ref["pred"][v]
+                    assert (tree[v].last_seg if tree[v].last_seg is not None else -1) == t_ref["last_seg"][v]
+                    assert (tree[v].origin_seg if tree[v].origin_seg is not None else -1) == t_ref["origin_seg"][v]
+                for e in ve_ref:
+                    assert emap[e].visited
