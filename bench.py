@@ -602,7 +602,7 @@ def run_serve(args):
             saturated = True
             srv.cancel()
             srv.drain(timeout=900)
-        ok = [t for t in tickets if t.error is None]
+        ok = [t for t in tickets if t.done and t.error is None]
         end = max(t.t_done for t in ok) if ok else start
         n_src = sum(len(t.query.sources) for t in ok)
         errs = [t.error for t in tickets if t.error is not None and "cancelled" not in str(t.error)]
@@ -620,9 +620,15 @@ def run_serve(args):
     clk = clocks.stop()
     st = srv.stats()
     srv.stop()
-    dws = srv.dws
     del srv
     torch.cuda.empty_cache()
+    # plain simplest-path calls share one dual workspace sized for the largest dual graph
+    big = max(duals, key=lambda g: duals[g].node_bound())
+    dcap = max(dual.estimate_states(ns, 1.33333, 3751) for ns in duals.values())
+    dplan = _native.Plan()
+    _native.check(_native.load().cs_plan_dual(C.byref(dual.dual_csr(duals[big]).struct(1.33333)), 0, 4, dcap, 0,
+                                              centrality._mem_budget(dev) // 3, C.byref(dplan)), "cs_plan_dual")
+    dws = dual.DualWorkspace(dplan, dplan.n_bound, dev)
     # ---- serial loop of plain calls on the 500 req/s stream (or the nearest rate)
     rate_ser = min(streams, key=lambda r: abs(r - 500.0))
     reqs = streams[rate_ser]

@@ -120,6 +120,26 @@ class BatchJob(C.Structure):
     ]
 
 
+class DualBatchJob(C.Structure):
+    _fields_ = [
+        ("g", DualGraph),
+        ("k", C.c_int32),
+        ("seconds", C.c_uint32 * MAX_K),
+        ("tolerance", C.c_float),
+        ("angular_scaling_unit", C.c_float),
+        ("farness_scaling_offset", C.c_float),
+        ("compute_closeness", C.c_int32),
+        ("compute_betweenness", C.c_int32),
+        ("n_sources", C.c_int32),
+        ("sources", _ptr),
+        ("src_wt", _ptr),
+        ("eligible", _ptr),
+        ("out", _ptr),
+        ("bucket", _ptr),
+        ("item_begin", C.c_int64),
+    ]
+
+
 class Outputs(C.Structure):
     _fields_ = [("out", _ptr), ("reach", _ptr)]
 
@@ -185,6 +205,13 @@ SIGNATURES = {
                                     _ptr]),
     "cs_abi_sizes": (C.c_int32, [_ptr, C.c_int32]),
     "cs_last_retries": (C.c_int32, [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "cs_dual_batch_prepare": (C.c_int32, [C.POINTER(DualBatchJob), C.c_int32, C.POINTER(C.c_int64)]),
+    "cs_dual_batch_plan": (C.c_int32, [C.POINTER(DualBatchJob), C.c_int32, C.c_int32, C.c_int32, C.c_int64,
+                                       C.POINTER(Plan)]),
+    "cs_dual_batch_run": (C.c_int32, [C.POINTER(DualBatchJob), _ptr, C.c_int32, C.POINTER(Plan), _ptr, C.c_size_t,
+                                      C.c_int32, _ptr]),
+    "cs_dual_batch_failed": (C.c_int32, [_ptr, C.POINTER(Plan), C.POINTER(C.c_int32), C.c_int32,
+                                         C.POINTER(C.c_int64), _ptr]),
     "cs_source_weights": (C.c_int32, [_ptr, C.c_int64, _ptr, C.c_int32, _ptr, _ptr, _ptr]),
     "cs_device_sm_count": (C.c_int32, []),
     "cs_last_phase_cycles": (C.c_int32, [_ptr, C.c_int32]),
@@ -227,9 +254,9 @@ def load(auto_build: bool = True) -> C.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        sizes = (C.c_int32 * 6)()
-        lib.cs_abi_sizes(sizes, 6)
-        want = [C.sizeof(t) for t in (PrimalGraph, DualGraph, Query, Plan, Outputs, BatchJob)]
+        sizes = (C.c_int32 * 7)()
+        lib.cs_abi_sizes(sizes, 7)
+        want = [C.sizeof(t) for t in (PrimalGraph, DualGraph, Query, Plan, Outputs, BatchJob, DualBatchJob)]
         if list(sizes) != want:
             raise RuntimeError(f"libcsgpu.so struct layouts {list(sizes)} differ from the binding's {want}")
         _lib = lib

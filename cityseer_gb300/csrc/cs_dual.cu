@@ -131,6 +131,7 @@ struct DualParams {
     const int32_t *remap;
     int32_t mode;
     int32_t fail_final;  // an overflow at this capacity is an error (capacity = every state)
+    int32_t replay_rounds;  // replay / re-sort rounds before a source falls back to the exact search
     int32_t force_exact;
     int32_t row_cap;
     int32_t *t_count, *t_node, *t_pred;
@@ -793,6 +794,86 @@ __device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, in
 // ------------------------------------------------------------------------------------------
 // Persistent kernel.
 // ------------------------------------------------------------------------------------------
+// One source on this warp's slot: search, settle order, replay, accumulation, scratch reset.
+// Returns true when the source was accumulated; false when it was listed (overflow or a replay
+// that disagreed) for a later pass.  li is what the lists record.
+__device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot &s, int li, int src, uint32_t *hist,
+                                                int *cnt, long long &relaxed, long long &settled) {
+    const int lane = lane_id();
+    const int N2 = 2 * p.g.n_bound;
+    const bool exact = (p.pass == 2) || p.force_exact;
+    int R;
+    if (exact) {
+        R = dual_exact_search(p, s, src);
+    } else {
+        R = dual_search(p, s, src, relaxed);
+    }
+    if (R < 0) {
+        for (int j = lane; j < N2; j += 32) {
+            s.key[j] = KEY_INF;
+            s.aux[j] = 0u;
+        }
+        if (lane == 0) {
+            if (p.fail_final) {
+                raise_err(p.hdr, CS_ERR_CAPACITY, 27);  // full-capacity passes must not overflow
+            } else {
+                const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
+                if (f < (unsigned)p.fail_cap) p.failed[f] = li;
+                else raise_err(p.hdr, CS_ERR_CAPACITY, 23);
+            }
+        }
+        __syncwarp();
+        return false;
+    }
+    // Replay in settle order.  A search key can hold a route from an offer its offering state
+    // later withdrew (that state improved its route but its new seconds crossed the cutoff), so
+    // the first order is an estimate: replay, re-sort by the replayed routes, and replay again
+    // until the order is consistent (the reference's), else fall back to the exact search.
+    bool bad = false;
+    int rr = 1;
+    const int rounds = exact ? 1 : max(1, p.replay_rounds);
+    for (int it = 0; it < rounds && rr == 1; it++) {
+        if (!exact) warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb,
+                                    s.vb, s.rk, s.ord, hist);
+        __syncwarp();
+        for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+        __syncwarp();
+        rr = dual_replay(p, s, src, R, bad, !exact);
+        __syncwarp();
+    }
+    const bool ok = rr == 0;
+    if (ok) {
+        dual_accumulate(p, s, src, R, cnt, bad);
+    } else if (lane == 0) {
+        if (exact) raise_err(p.hdr, CS_ERR_INTERNAL, 24);  // the exact pass must replay cleanly
+        else {
+            const unsigned f = atomicAdd(&p.hdr->n_inexact, 1u);
+            if (f < (unsigned)p.inexact_cap) p.inexact[f] = li;
+            else raise_err(p.hdr, CS_ERR_CAPACITY, 25);
+        }
+    }
+    if (__any_sync(FULL, bad) && lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 26);
+    __syncwarp();
+    for (int i = lane; i < R; i += 32) {
+        const int S = s.ord[i];
+        s.key[S] = KEY_INF;
+        s.aux[S] = 0u;
+    }
+    __syncwarp();
+    settled += R;
+    return ok;
+}
+
+__device__ __forceinline__ void flush_dual_counters(const DualParams &p, long long relaxed, long long settled,
+                                                    long long done_src) {
+    const long long rsum = warp_sum_ll(relaxed);
+    if (lane_id() == 0) {
+        atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
+        atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
+        atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
+    }
+}
+
 __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][MAXK];
@@ -802,7 +883,6 @@ __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
     if (slot >= p.n_slots) return;
     const DSlot s = dslot(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.k, slot, p.geo_n);
     long long relaxed = 0, settled = 0, done_src = 0;
-    const int N2 = 2 * p.g.n_bound;
     while (true) {
         unsigned long long idx = 0;
         if (lane == 0) idx = atomicAdd(p.pass ? &p.hdr->work_next2 : &p.hdr->work_next, 1ull);
@@ -810,73 +890,101 @@ __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
         if (idx >= (unsigned long long)p.n_src) break;
         if (__ldcg(&p.hdr->err) != 0u) break;
         const int li = p.remap ? p.remap[idx] : (int)idx;
-        const int src = p.src_list[li];
-        const bool exact = (p.pass == 2) || p.force_exact;
-        int R;
-        if (exact) {
-            R = dual_exact_search(p, s, src);
-        } else {
-            R = dual_search(p, s, src, relaxed);
+        if (run_dual_source(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], relaxed, settled)) done_src++;
+    }
+    flush_dual_counters(p, relaxed, settled, done_src);
+}
+
+// Batched form: the (job, source) items of many simplest-path queries (graphs, thresholds, source
+// subsets) in one persistent launch.  Slot geometry comes from the base parameters (largest graph,
+// threshold count and capacity of the batch); an item's job is the one whose item_begin is the
+// largest <= the item.  Lists record global item indices.
+__device__ __forceinline__ int djob_of(const cs_dual_batch_job *jobs, int n_jobs, long long item) {
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].item_begin <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void djob_params(const DualParams &base, const cs_dual_batch_job &j, DualParams &p) {
+    p = base;
+    p.g = j.g;
+    p.k = j.k;
+    uint32_t maxs = 0;
+    for (int i = 0; i < MAXK; i++) {
+        p.sk[i] = i < j.k ? (float)j.seconds[i] : 0.0f;
+        if (i < j.k) maxs = max(maxs, j.seconds[i]);
+    }
+    p.maxsec = (float)maxs;
+    p.tol = j.tolerance;
+    p.asu = j.angular_scaling_unit;
+    p.fso = j.farness_scaling_offset;
+    p.closeness = j.compute_closeness;
+    p.betweenness = j.compute_betweenness;
+    p.track_reach = 0;
+    p.reach = nullptr;
+    p.src_list = j.sources_dev;
+    p.n_src = j.n_sources;
+    p.src_wt = j.src_wt_dev;
+    p.eligible = j.eligible_dev;
+    p.out = j.out_dev;
+    p.bucket = j.bucket_dev;
+}
+
+__global__ void __launch_bounds__(256, 2) dual_batch_kernel(const DualParams base, const cs_dual_batch_job *jobs,
+                                                            int n_jobs, long long n_items) {
+    __shared__ uint32_t hist_all[8][256];
+    __shared__ int cnt_all[8][MAXK];
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
+    if (slot >= base.n_slots) return;
+    const DSlot s = dslot(base.dense, base.dense_stride, base.compact, (size_t)base.cap, base.k, slot, base.geo_n);
+    long long relaxed = 0, settled = 0, done_src = 0;
+    DualParams p;
+    int cur_job = -1;
+    while (true) {
+        unsigned long long idx = 0;
+        if (lane == 0) idx = atomicAdd(base.pass ? &base.hdr->work_next2 : &base.hdr->work_next, 1ull);
+        idx = __shfl_sync(FULL, idx, 0);
+        const long long n = base.pass ? base.n_src : n_items;
+        if ((long long)idx >= n) break;
+        if (__ldcg(&base.hdr->err) != 0u) break;
+        const long long item = base.remap ? (long long)base.remap[idx] : (long long)idx;
+        const int jb = djob_of(jobs, n_jobs, item);
+        if (jb != cur_job) {
+            djob_params(base, jobs[jb], p);
+            cur_job = jb;
         }
-        if (R < 0) {
-            for (int j = lane; j < N2; j += 32) {
-                s.key[j] = KEY_INF;
-                s.aux[j] = 0u;
-            }
-            if (lane == 0) {
-                if (p.fail_final) {
-                    raise_err(p.hdr, CS_ERR_CAPACITY, 27);  // full-capacity passes must not overflow
-                } else {
-                    const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
-                    if (f < (unsigned)p.fail_cap) p.failed[f] = li;
-                    else raise_err(p.hdr, CS_ERR_CAPACITY, 23);
+        const int li = (int)(item - jobs[jb].item_begin);
+        if (run_dual_source(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], relaxed, settled))
+            done_src++;
+    }
+    flush_dual_counters(base, relaxed, settled, done_src);
+}
+
+// Closeness prefixes of every job with closeness (blockIdx.y strides the jobs); the bucket is
+// zeroed as it is read, so buckets are zero between runs.
+__global__ void dual_batch_prefix(const cs_dual_batch_job *jobs, int n_jobs) {
+    for (int j = blockIdx.y; j < n_jobs; j += gridDim.y) {
+        const cs_dual_batch_job &jb = jobs[j];
+        if (!jb.compute_closeness || jb.n_sources <= 0) continue;
+        const int K = jb.k, N = jb.g.n_bound;
+        const size_t KN = (size_t)K * N;
+        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+            for (int m = 0; m < 3; m++) {
+                double acc = 0.0;
+                for (int k = 0; k < K; k++) {
+                    const size_t o = (size_t)m * KN + (size_t)k * N + t;
+                    acc += jb.bucket_dev[o];
+                    jb.bucket_dev[o] = 0.0;
+                    jb.out_dev[o] += acc;
                 }
             }
-            __syncwarp();
-            continue;
         }
-        // Replay in settle order.  A search key can hold a route from an offer its offering state
-        // later withdrew (that state improved its route but its new seconds crossed the cutoff), so
-        // the first order is an estimate: replay, re-sort by the replayed routes, and replay again
-        // until the order is consistent (the reference's), else fall back to the exact search.
-        bool bad = false;
-        int rr = 1;
-        for (int it = 0; it < (exact ? 1 : 4) && rr == 1; it++) {
-            if (!exact) warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb,
-                                        s.vb, s.rk, s.ord, hist_all[wib]);
-            __syncwarp();
-            for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
-            __syncwarp();
-            rr = dual_replay(p, s, src, R, bad, !exact);
-            __syncwarp();
-        }
-        const bool ok = rr == 0;
-        if (ok) {
-            dual_accumulate(p, s, src, R, cnt_all[wib], bad);
-        } else if (lane == 0) {
-            if (exact) raise_err(p.hdr, CS_ERR_INTERNAL, 24);  // the exact pass must replay cleanly
-            else {
-                const unsigned f = atomicAdd(&p.hdr->n_inexact, 1u);
-                if (f < (unsigned)p.inexact_cap) p.inexact[f] = li;
-                else raise_err(p.hdr, CS_ERR_CAPACITY, 25);
-            }
-        }
-        if (__any_sync(FULL, bad) && lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 26);
-        __syncwarp();
-        for (int i = lane; i < R; i += 32) {
-            const int S = s.ord[i];
-            s.key[S] = KEY_INF;
-            s.aux[S] = 0u;
-        }
-        __syncwarp();
-        settled += R;
-        if (ok) done_src += 1;
-    }
-    const long long rsum = warp_sum_ll(relaxed);
-    if (lane == 0) {
-        atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
-        atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
-        atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
     }
 }
 
@@ -1173,6 +1281,13 @@ cs_status dreset(char *dense, size_t stride, int n_bound, int n_slots, cudaStrea
     return e == cudaSuccess ? CS_OK : dcuda(e, "fill_dual_dense launch");
 }
 
+// Replay / re-sort rounds per source (CS_DUAL_REPLAY_ROUNDS overrides the default of 4).
+int replay_rounds() {
+    const char *e = getenv("CS_DUAL_REPLAY_ROUNDS");
+    const int r = e ? atoi(e) : 0;
+    return (r >= 1 && r <= 64) ? r : 4;
+}
+
 cs_status dlaunch(csd::DualParams &p, int n_slots, cudaStream_t s) {
     p.n_slots = n_slots;
     csd::dual_kernel<<<(n_slots + 7) / 8, 256, 0, s>>>(p);
@@ -1276,6 +1391,7 @@ cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, cons
     p.cap = plan->cap;
     const char *fe = getenv("CS_DUAL_FORCE_EXACT");
     p.force_exact = (fe && fe[0] == '1') ? 1 : 0;
+    p.replay_rounds = replay_rounds();
     if (p.n_src <= 0) return CS_OK;
     cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), s);
     if (e == cudaSuccess && p.closeness)
@@ -1353,6 +1469,197 @@ cs_status cs_dual_workspace_init(const cs_plan *plan, int32_t n_bound, void *ws,
     cudaError_t e = cudaMemsetAsync(ws, 0, 256, (cudaStream_t)stream);
     if (e != cudaSuccess) return dcuda(e, "workspace init");
     return dreset((char *)ws + lay.dense_off, lay.dense_stride, n_bound, plan->n_slots, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------------------------------------
+// Batched simplest-path form.
+// ------------------------------------------------------------------------------------------
+}  // extern "C"
+namespace {
+struct DBatchShape {
+    int max_n, max_k;
+};
+
+cs_status dbatch_shape(const cs_dual_batch_job *jobs, int n_jobs, DBatchShape &b) {
+    if (!jobs || n_jobs <= 0) return dfail(CS_ERR_ARG, "empty batch");
+    b.max_n = 1;
+    b.max_k = 1;
+    for (int j = 0; j < n_jobs; j++) {
+        cs_status st = dvalidate(&jobs[j].g);
+        if (st != CS_OK) return st;
+        if (jobs[j].k < 1 || jobs[j].k > CS_MAX_THRESHOLDS) return dfail(CS_ERR_ARG, "threshold count out of range");
+        if (!jobs[j].out_dev) return dfail(CS_ERR_ARG, "job without out_dev");
+        if (jobs[j].compute_closeness && !jobs[j].bucket_dev)
+            return dfail(CS_ERR_ARG, "job with closeness needs bucket_dev");
+        b.max_n = std::max(b.max_n, jobs[j].g.n_bound);
+        b.max_k = std::max(b.max_k, jobs[j].k);
+    }
+    return CS_OK;
+}
+
+cs_status dbatch_launch(csd::DualParams &p, const cs_dual_batch_job *jobs_dev, int n_jobs, long long n_items, int slots,
+                        cudaStream_t s) {
+    p.n_slots = slots;
+    csd::dual_batch_kernel<<<(slots + 7) / 8, 256, 0, s>>>(p, jobs_dev, n_jobs, n_items);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CS_OK : dcuda(e, "dual_batch_kernel launch");
+}
+}  // namespace
+extern "C" {
+
+cs_status cs_dual_batch_prepare(cs_dual_batch_job *jobs_host, int32_t n_jobs, int64_t *n_items) {
+    if (!jobs_host || n_jobs <= 0 || !n_items) return dfail(CS_ERR_ARG, "empty batch");
+    int64_t acc = 0;
+    for (int j = 0; j < n_jobs; j++) {
+        jobs_host[j].item_begin = acc;
+        acc += std::max(0, jobs_host[j].n_sources);
+    }
+    *n_items = acc;
+    return CS_OK;
+}
+
+cs_status cs_dual_batch_plan(const cs_dual_batch_job *jobs_host, int32_t n_jobs, int32_t cap, int32_t max_slots,
+                             int64_t mem_budget_bytes, cs_plan *plan) {
+    DBatchShape b;
+    cs_status st = dbatch_shape(jobs_host, n_jobs, b);
+    if (st != CS_OK) return st;
+    // the largest job graph with the largest threshold count sizes the slots
+    int big = 0;
+    for (int j = 1; j < n_jobs; j++)
+        if (jobs_host[j].g.n_bound > jobs_host[big].g.n_bound) big = j;
+    return cs_plan_dual(&jobs_host[big].g, 0, b.max_k, cap, max_slots, mem_budget_bytes, plan);
+}
+
+cs_status cs_dual_batch_run(const cs_dual_batch_job *jobs_host, const cs_dual_batch_job *jobs_dev, int32_t n_jobs,
+                            const cs_plan *plan, void *ws, size_t ws_bytes, int32_t flags, void *stream_v) {
+    DBatchShape b;
+    cs_status st = dbatch_shape(jobs_host, n_jobs, b);
+    if (st != CS_OK) return st;
+    if (!plan || !ws || !jobs_dev) return dfail(CS_ERR_ARG, "plan/workspace/jobs_dev is NULL");
+    if (plan->lanes < b.max_k) return dfail(CS_ERR_ARG, "plan was made for fewer thresholds");
+    const int geo_n = plan->n_bound > 0 ? plan->n_bound : b.max_n;
+    if (geo_n < b.max_n) return dfail(CS_ERR_ARG, "plan was made for a smaller graph");
+    const int L = plan->lanes;
+    const DLayout lay = dlayout(geo_n, plan->n_slots, plan->cap, L);
+    if (ws_bytes < lay.total) return dfail(CS_ERR_ARG, "workspace too small for this plan");
+    long long n_items = 0;
+    for (int j = 0; j < n_jobs; j++) {
+        if (jobs_host[j].item_begin != n_items) return dfail(CS_ERR_ARG, "jobs not prepared (cs_dual_batch_prepare)");
+        n_items += std::max(0, jobs_host[j].n_sources);
+    }
+    cudaStream_t s = (cudaStream_t)stream_v;
+    char *base = (char *)ws;
+    csd::DualParams p;
+    memset(&p, 0, sizeof(p));
+    p.g.n_bound = geo_n;
+    p.geo_n = geo_n;
+    p.k = L;  // slot geometry; each job brings its own k
+    p.replay_rounds = replay_rounds();
+    p.delta = plan->delta_seconds > 0.0f ? plan->delta_seconds : 30.0f;
+    p.hdr = (cs::WsHeader *)base;
+    p.failed = (int32_t *)(base + lay.failed_off);
+    p.fail_cap = lay.fail_cap;
+    p.inexact = (int32_t *)(base + lay.inexact_off);
+    p.inexact_cap = lay.fail_cap;
+    p.dense = base + lay.dense_off;
+    p.dense_stride = lay.dense_stride;
+    p.compact = base + lay.compact_off;
+    p.cap = plan->cap;
+    cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), s);
+    if (e != cudaSuccess) return dcuda(e, "batch reset");
+    if (n_items > 0) {
+        st = dbatch_launch(p, jobs_dev, n_jobs, n_items, plan->n_slots, s);
+        if (st != CS_OK) return st;
+    }
+    if (!(flags & CS_BATCH_ASYNC) && n_items > 0) {
+        cs::WsHeader h;
+        st = dsync_header(p.hdr, h, s);
+        if (st != CS_OK) return st;
+        // overflowed items at growing capacities, then items whose replay disagreed with the exact
+        // heap search (as cs_centrality_simplest)
+        const int N2 = 2 * b.max_n;
+        int32_t *listA = p.failed;
+        int32_t *listB = (int32_t *)(base + lay.failed2_off);
+        auto chain = [&](int pass, const int32_t *in, unsigned n_in, int cap0) -> cs_status {
+            int cap_l = std::min(N2, cap0);
+            const int32_t *list = in;
+            while (n_in > 0u) {
+                const bool final = cap_l >= N2;
+                int32_t *out_l = (list == listA) ? listB : listA;
+                csd::DualParams p2 = p;
+                p2.pass = pass;
+                p2.cap = cap_l;
+                p2.remap = list;
+                p2.n_src = std::min<unsigned>(n_in, (unsigned)lay.fail_cap);
+                p2.failed = out_l;
+                p2.fail_final = final ? 1 : 0;
+                cudaError_t e2 = cudaMemsetAsync(&p.hdr->work_next2, 0, sizeof(unsigned long long), s);
+                if (e2 == cudaSuccess) e2 = cudaMemsetAsync(&p.hdr->n_failed, 0, sizeof(unsigned), s);
+                if (e2 != cudaSuccess) return dcuda(e2, "retry counter reset");
+                const size_t per = csd::compact_bytes_d((size_t)cap_l, L);
+                int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
+                slots2 = std::max(1, std::min<int>(slots2, (int)p2.n_src));
+                cs_status st2 = dbatch_launch(p2, jobs_dev, n_jobs, n_items, slots2, s);
+                if (st2 != CS_OK) return st2;
+                cs::WsHeader h2;
+                st2 = dsync_header(p.hdr, h2, s);
+                if (st2 != CS_OK) return st2;
+                h.n_inexact = h2.n_inexact;
+                n_in = final ? 0u : h2.n_failed;
+                list = out_l;
+                cap_l = (int)std::min<long long>(N2, 4ll * cap_l);
+            }
+            return CS_OK;
+        };
+        const long long n_over = h.n_failed;
+        if (h.n_failed > 0u) {
+            st = chain(1, listA, h.n_failed, 4 * std::max(plan->cap, 16));
+            if (st != CS_OK) return st;
+        }
+        const long long n_inexact = h.n_inexact;
+        if (h.n_inexact > 0u) {
+            st = chain(2, p.inexact, std::min<unsigned>(h.n_inexact, (unsigned)lay.fail_cap), plan->cap);
+            if (st != CS_OK) return st;
+        }
+        cs_set_retries_internal(n_over, n_inexact);
+    }
+    int max_n = 0, n_pref = 0;
+    for (int j = 0; j < n_jobs; j++)
+        if (jobs_host[j].compute_closeness && jobs_host[j].n_sources > 0) {
+            max_n = std::max(max_n, jobs_host[j].g.n_bound);
+            n_pref++;
+        }
+    if (n_pref > 0) {
+        const int gy = std::min(n_pref, 65535);
+        const int gx = std::max(1, std::min((max_n + 255) / 256, std::max(1, dsm_count() * 8 / gy)));
+        csd::dual_batch_prefix<<<dim3(gx, gy), 256, 0, s>>>(jobs_dev, n_jobs);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return dcuda(e, "dual_batch_prefix launch");
+    }
+    return CS_OK;
+}
+
+cs_status cs_dual_batch_failed(void *ws, const cs_plan *plan, int32_t *items_host, int32_t max_items, int64_t *n_items,
+                               void *stream) {
+    // overflowed items first, then items whose replay disagreed
+    if (!ws || !plan || !n_items) return dfail(CS_ERR_ARG, "workspace/plan/n_items is NULL");
+    cs::WsHeader h;
+    cudaStream_t st = (cudaStream_t)stream;
+    cs_status rc = dsync_header((cs::WsHeader *)ws, h, st);
+    if (rc != CS_OK) return rc;
+    const DLayout lay = dlayout(std::max(1, plan->n_bound), plan->n_slots, plan->cap, plan->lanes);
+    if (h.n_failed > (unsigned)lay.fail_cap || h.n_inexact > (unsigned)lay.fail_cap)
+        return dfail(CS_ERR_CAPACITY, "more listed items than the lists hold");
+    *n_items = (int64_t)h.n_failed + (int64_t)h.n_inexact;
+    const int64_t c1 = std::min<int64_t>(h.n_failed, std::max(0, max_items));
+    const int64_t c2 = std::min<int64_t>(h.n_inexact, std::max<int64_t>(0, max_items - c1));
+    cudaError_t e = cudaSuccess;
+    if (c1 > 0 && items_host)
+        e = cudaMemcpyAsync(items_host, (char *)ws + lay.failed_off, 4 * (size_t)c1, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && c2 > 0 && items_host)
+        e = cudaMemcpyAsync(items_host + c1, (char *)ws + lay.inexact_off, 4 * (size_t)c2, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? CS_OK : dcuda(e, "dual batch lists");
 }
 
 cs_status cs_plan_dual_tree(const cs_dual_graph *g, int32_t cap, int32_t max_slots, int64_t mem_budget_bytes,

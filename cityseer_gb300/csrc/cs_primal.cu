@@ -1976,9 +1976,10 @@ extern "C" cs_status cs_source_weights(const int32_t *sources_dev, int64_t n_sou
 
 extern "C" cs_status cs_abi_sizes(int32_t *out, int32_t n) {
     // sizes of the public structs, for bindings to check their layouts against
-    const int32_t v[6] = {(int32_t)sizeof(cs_primal_graph), (int32_t)sizeof(cs_dual_graph), (int32_t)sizeof(cs_query),
-                          (int32_t)sizeof(cs_plan), (int32_t)sizeof(cs_outputs), (int32_t)sizeof(cs_batch_job)};
+    const int32_t v[7] = {(int32_t)sizeof(cs_primal_graph), (int32_t)sizeof(cs_dual_graph), (int32_t)sizeof(cs_query),
+                          (int32_t)sizeof(cs_plan),         (int32_t)sizeof(cs_outputs),    (int32_t)sizeof(cs_batch_job),
+                          (int32_t)sizeof(cs_dual_batch_job)};
     if (!out) return fail(CS_ERR_ARG, "out is NULL");
-    for (int i = 0; i < n && i < 6; i++) out[i] = v[i];
+    for (int i = 0; i < n && i < 7; i++) out[i] = v[i];
     return CS_OK;
 }

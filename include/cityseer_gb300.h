@@ -133,6 +133,27 @@ typedef struct {
     int64_t item_begin;       /* first queue item of this job (set by cs_batch_prepare) */
 } cs_batch_job;
 
+/* One simplest-path (dual graph) job of a batched launch: outputs [4][k][n_bound] as
+ * cs_centrality_simplest writes them (density, farness, harmonic, betweenness). */
+typedef struct {
+    cs_dual_graph g;
+    int32_t k;
+    uint32_t seconds[CS_MAX_THRESHOLDS];
+    float tolerance;
+    float angular_scaling_unit;
+    float farness_scaling_offset;
+    int32_t compute_closeness;
+    int32_t compute_betweenness;
+    int32_t n_sources;
+    const int32_t *sources_dev;
+    const float *src_wt_dev;
+    const uint8_t *eligible_dev;
+    double *out_dev;
+    double *bucket_dev;       /* [3][k][n_bound] when compute_closeness: zero before the first run; every
+                                 successful run leaves it zero */
+    int64_t item_begin;       /* first queue item of this job (set by cs_dual_batch_prepare) */
+} cs_dual_batch_job;
+
 /* Outputs: f64 rows [metric][k][n_bound]; reach_dev: u32[k] (may be NULL when !track_reach). */
 typedef struct {
     double *out_dev;
@@ -263,12 +284,27 @@ cs_status cs_last_phase_cycles(int64_t *cycles, int32_t n);
 cs_status cs_source_weights(const int32_t *sources_dev, int64_t n_sources, const float *node_w_dev, int32_t n_bound,
                             float *src_wt_dev, uint8_t *eligible_dev, void *stream);
 
+/* Batched simplest-path form: many queries on many dual graphs in one persistent launch, as
+ * cs_batch_* does for the primal.  cs_dual_batch_run with CS_BATCH_ASYNC neither synchronises nor
+ * redoes anything; cs_dual_batch_failed then lists the items that overflowed or whose replay
+ * disagreed (they contributed nothing; run them again as a synchronous batch, which redoes them at
+ * growing capacities and with the exact heap search). */
+cs_status cs_dual_batch_prepare(cs_dual_batch_job *jobs_host, int32_t n_jobs, int64_t *n_items);
+cs_status cs_dual_batch_plan(const cs_dual_batch_job *jobs_host, int32_t n_jobs, int32_t cap, int32_t max_slots,
+                             int64_t mem_budget_bytes, cs_plan *plan);
+cs_status cs_dual_batch_run(const cs_dual_batch_job *jobs_host, const cs_dual_batch_job *jobs_dev, int32_t n_jobs,
+                            const cs_plan *plan, void *workspace_dev, size_t workspace_bytes, int32_t flags,
+                            void *stream);
+cs_status cs_dual_batch_failed(void *workspace_dev, const cs_plan *plan, int32_t *items_host, int32_t max_items,
+                               int64_t *n_items, void *stream);
+
 /* Sources of the last call on this thread that overflowed their slot's capacity (and were run again
  * at a larger one) and, for simplest-path calls, whose replay disagreed with the label-correcting
  * search (and were run again with the exact heap search). */
 cs_status cs_last_retries(int64_t *overflowed, int64_t *inexact);
 
-/* sizeof of cs_primal_graph, cs_dual_graph, cs_query, cs_plan, cs_outputs, cs_batch_job (first n). */
+/* sizeof of cs_primal_graph, cs_dual_graph, cs_query, cs_plan, cs_outputs, cs_batch_job,
+ * cs_dual_batch_job (first n). */
 cs_status cs_abi_sizes(int32_t *out, int32_t n);
 
 /* Number of SMs of the current device (0 on failure). */
