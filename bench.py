@@ -481,7 +481,7 @@ def run_batch(args):
             assert torch.equal(a[0], c[0]), "batched density differs from the plain call"
         worst = max(worst, float(((a - c).abs() / c.abs().clamp_min(1e-3)).max()))
     assert worst < 1e-6, f"batched rows differ from plain rows (rel {worst})"
-    n_items = b.n_items
+    n_items = sum(len(jb["proc"]) for jb in b.jobs)  # (job, source) pairs: a fused item serves two
     n_nodes = sum(ns.node_count() for ns, _ in graphs)
     line = {
         "metric": BATCH_METRIC,
@@ -502,6 +502,8 @@ def run_batch(args):
             "jobs": len(jobs),
             "nodes_total": n_nodes,
             "items_per_step": n_items,
+            "launch_items_per_step": b.n_items,
+            "fused_jobs": b.n_fused,
             "l2": "inputs larger than L2 (workspace + 96 graphs)",
             "slots": int(b.plan.n_slots),
             "cap": int(b.plan.cap),
@@ -514,7 +516,7 @@ def run_batch(args):
         "edges_relaxed_per_s": counters[1] / t_batch,
         "parity_max_rel": worst,
         "setup_s": {"graphs": round(t_build, 2), "batch": round(t_setup, 2)},
-        "gpu_launches": 1 + sum(1 for jb in b.jobs if jb["mode"] == 0 and jb["closeness"]),
+        "gpu_launches": 2,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

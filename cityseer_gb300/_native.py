@@ -116,6 +116,7 @@ class BatchJob(C.Structure):
         ("eligible", _ptr),
         ("out", _ptr),
         ("bucket", _ptr),
+        ("out2", _ptr),
         ("item_begin", C.c_int64),
     ]
 

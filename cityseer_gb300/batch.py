@@ -24,10 +24,15 @@ class Batch:
     """jobs: sequence of dicts with keys ns, mode ('shortest' | 'segment'), distances, and optional
     speed_m_s, tolerance, compute_closeness, compute_betweenness, source_indices."""
 
-    def __init__(self, jobs, cap: int = 0, max_slots: int = 0, tune: bool = False):
+    def __init__(self, jobs, cap: int = 0, max_slots: int = 0, tune: bool = False, fuse: bool = False):
+        """fuse: a shortest-path job and a segment job on the same graph, thresholds, flags and
+        sources become one job of mode 3 (one search per source feeds both).  Off by default: on
+        the 96-graph workload the fused job ran slower than the two jobs apart, since the fused
+        per-source code (both accumulations) misses the instruction caches more than it saves in
+        searches.  Jobs run grouped by mode, one launch of that mode's kernel per group."""
         self.lib = _native.load()
         self.jobs = []
-        self.table = (_native.BatchJob * len(jobs))()
+        structs = [_native.BatchJob() for _ in jobs]
         variants = []
         max_reach = 1
         for j, spec in enumerate(jobs):
@@ -64,7 +69,7 @@ class Batch:
                 if (mode == 0 and closeness) else None
             keep = [torch.from_numpy(np.ascontiguousarray(proc)).to(dev), torch.from_numpy(wt).to(dev),
                     torch.from_numpy(el).to(dev)]
-            jb = self.table[j]
+            jb = structs[j]
             jb.g = csr.struct(speed)
             jb.mode = mode
             jb.k = len(d)
@@ -84,9 +89,37 @@ class Batch:
             jb.out = out.data_ptr()
             jb.bucket = bucket.data_ptr() if bucket is not None else None
             self.jobs.append(dict(ns=ns, csr=csr, mode=mode, d=d, out=out, bucket=bucket, keep=keep, sp=sp,
-                                  closeness=closeness, betweenness=betweenness))
+                                  closeness=closeness, betweenness=betweenness, proc=np.asarray(proc),
+                                  speed=speed, tol=jb.tolerance))
+        # fusion: pair each segment job with a matching shortest-path job
+        table = []
+        used = set()
+        if fuse:
+            short = {}
+            for j, jb in enumerate(self.jobs):
+                if jb["mode"] == 0:
+                    short.setdefault(self._fuse_key(jb), []).append(j)
+            for j, jb in enumerate(self.jobs):
+                if jb["mode"] != 1:
+                    continue
+                for cand in short.get(self._fuse_key(jb), []):
+                    if cand in used or not np.array_equal(self.jobs[cand]["proc"], jb["proc"]):
+                        continue
+                    st = structs[cand]
+                    st.mode = 3
+                    st.out2 = jb["out"].data_ptr()
+                    used.update((cand, j))
+                    jb["fused_with"] = cand
+                    break
+        for j, st in enumerate(structs):
+            if j in used and self.jobs[j]["mode"] == 1:
+                continue
+            table.append(st)
+        table.sort(key=lambda st: {0: 0, 1: 1, 3: 2}[st.mode])  # one launch per mode group
+        self.n_fused = sum(1 for jb in self.jobs if "fused_with" in jb)
+        self.table = (_native.BatchJob * len(table))(*table)
         n = C.c_int64()
-        _native.check(self.lib.cs_batch_prepare(self.table, len(jobs), C.byref(n)), "cs_batch_prepare")
+        _native.check(self.lib.cs_batch_prepare(self.table, len(table), C.byref(n)), "cs_batch_prepare")
         self.n_items = n.value
         dev = self.jobs[0]["csr"].device
         raw = bytes(memoryview(self.table).cast("B"))
@@ -95,18 +128,22 @@ class Batch:
         plan.variant = max(set(variants), key=variants.count)
         if cap <= 0:
             cap = int(max(1024, -(-int(max_reach * 1.3) // 256) * 256))
-        _native.check(self.lib.cs_batch_plan(self.table, len(jobs), cap, max_slots, centrality._mem_budget(dev),
-                                             C.byref(plan)), "cs_batch_plan")
+        _native.check(self.lib.cs_batch_plan(self.table, len(self.table), cap, max_slots,
+                                             centrality._mem_budget(dev), C.byref(plan)), "cs_batch_plan")
         self.plan = plan
         from .device import Workspace
 
         self.ws = Workspace(plan, plan.n_bound, dev)
         self.graph = None
 
+    @staticmethod
+    def _fuse_key(jb):
+        return (id(jb["ns"]), tuple(jb["d"]), jb["speed"], jb["tol"], jb["closeness"], jb["betweenness"])
+
     def run(self, async_: bool = False, stream=None) -> None:
         """Enqueues the whole batch; outputs must be zero (fresh Batch, or zero_outputs())."""
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        rc = self.lib.cs_batch_run(self.table, self.table_dev.data_ptr(), len(self.jobs), C.byref(self.plan),
+        rc = self.lib.cs_batch_run(self.table, self.table_dev.data_ptr(), len(self.table), C.byref(self.plan),
                                    self.ws.ptr, self.ws.nbytes, _native.CS_BATCH_ASYNC if async_ else 0, st)
         if rc != _native.CS_OK:
             self.ws.init(st)

@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <vector>
 
 #include "cs_common.cuh"
 #include "cs_sort.cuh"
@@ -95,7 +96,7 @@ __host__ __device__ inline SlotPtrs slot_ptrs(char *dense, size_t dense_stride, 
     return s;
 }
 
-enum Mode { MODE_SHORTEST = 0, MODE_SEGMENT = 1, MODE_TREE = 2 };
+enum Mode { MODE_SHORTEST = 0, MODE_SEGMENT = 1, MODE_TREE = 2, MODE_BOTH = 3 };  // BOTH: batched jobs only
 
 struct PrimalParams {
     cs_primal_graph g;
@@ -113,6 +114,7 @@ struct PrimalParams {
     const uint8_t *eligible;
     double *out;
     double *bucket;  // [3][K][N] threshold-bucketed closeness terms (density, farness, harmonic)
+    double *out2;    // MODE_BOTH: segment rows [4][K][N] (out holds the shortest rows)
     uint32_t *reach;
     WsHeader *hdr;
     int32_t *failed;  // [fail_cap] indices (into src_list) of sources that overflowed
@@ -704,7 +706,8 @@ __global__ void bucket_prefix_kernel(const double *bucket, double *out, int K, i
 __global__ void batch_prefix_kernel(const cs_batch_job *jobs, int n_jobs) {
     for (int j = blockIdx.y; j < n_jobs; j += gridDim.y) {
         const cs_batch_job &jb = jobs[j];
-        if (jb.mode != MODE_SHORTEST || !jb.compute_closeness || jb.n_sources <= 0) continue;
+        if ((jb.mode != MODE_SHORTEST && jb.mode != MODE_BOTH) || !jb.compute_closeness || jb.n_sources <= 0)
+            continue;
         const int K = jb.k, N = jb.g.n_bound;
         const size_t KN = (size_t)K * N;
         double *bucket = jb.bucket_dev;
@@ -732,6 +735,7 @@ CS_PHASE_INLINE __device__ void segment_accumulate(const PrimalParams &p, const 
     const int lane = lane_id();
     const int K = p.k;
     const int N = p.g.n_bound;
+    double *const out = (p.mode == MODE_BOTH) ? p.out2 : p.out;  // segment rows
     bool bad = false;
     // single predecessor (strict <) with its last segment length; pred position in pr[i*P]
     for (int i = lane; i < R; i += 32) {
@@ -845,9 +849,9 @@ CS_PHASE_INLINE __device__ void segment_accumulate(const PrimalParams &p, const 
             const double a1 = warp_sum_d(acc[MAXK + k]);
             const double a2 = warp_sum_d(acc[2 * MAXK + k]);
             if (lane == 0) {
-                atomicAdd(p.out + ((size_t)0 * K + k) * N + src, a0);
-                atomicAdd(p.out + ((size_t)1 * K + k) * N + src, a1);
-                atomicAdd(p.out + ((size_t)2 * K + k) * N + src, a2);
+                atomicAdd(out + ((size_t)0 * K + k) * N + src, a0);
+                atomicAdd(out + ((size_t)1 * K + k) * N + src, a1);
+                atomicAdd(out + ((size_t)2 * K + k) * N + src, a2);
             }
         }
     }
@@ -896,7 +900,7 @@ CS_PHASE_INLINE __device__ void segment_accumulate(const PrimalParams &p, const 
                             if (isfinite(auc) && auc >= 0.0f) total += (double)auc;
                         }
                     }
-                    if (i > 0 && v != src && below > 0.0) atomicAdd(p.out + ((size_t)3 * K + k) * N + v, below);
+                    if (i > 0 && v != src && below > 0.0) atomicAdd(out + ((size_t)3 * K + k) * N + v, below);
                     if (pp >= 0 && total != 0.0) atomicAdd(&acc[(size_t)pp * K + k], total);
                 }
                 mine = true;
@@ -992,7 +996,13 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
     } else {
         if (p.mode == MODE_SHORTEST) shortest_accumulate<PM, false>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
         else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
-        else tree_rows<PM>(p, s, li, R);
+        else if (p.mode == MODE_BOTH) {
+            // one search and settle order serve both: shortest rows, then segment rows (its own
+            // single-predecessor replay over the same positions)
+            shortest_accumulate<PM, false>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
+            __syncwarp();
+            segment_accumulate<PM>(p, s, src, R);
+        } else tree_rows<PM>(p, s, li, R);
     }
     __syncwarp();
     t0 = clock64();
@@ -1178,12 +1188,15 @@ __device__ __forceinline__ void job_params(const PrimalParams &base, const cs_ba
     p.eligible = j.eligible_dev;
     p.out = j.out_dev;
     p.bucket = j.bucket_dev;
+    p.out2 = j.out2_dev;
     p.mode = j.mode;
 }
 
-template <int PM, int MINB>
+// MODE: the accumulation compiled in (0 shortest, 1 segment), or -1 to dispatch on each job's
+// mode; a launch covers items [item_lo, item_hi) (or, in a re-run, the listed items).
+template <int PM, int MINB, int MODE>
 __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams base, const cs_batch_job *jobs,
-                                                          int n_jobs, long long n_items) {
+                                                          int n_jobs, long long item_lo, long long item_hi) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][2 * MAXK];
     __shared__ long long ph_all[8][8];
@@ -1207,10 +1220,10 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
         unsigned long long idx = 0;
         if (lane == 0) idx = atomicAdd(base.rerun ? &base.hdr->work_next2 : &base.hdr->work_next, 1ull);
         idx = __shfl_sync(FULL, idx, 0);
-        const long long n = base.rerun ? base.n_src : n_items;
+        const long long n = base.rerun ? base.n_src : item_hi - item_lo;
         if ((long long)idx >= n) break;
         if (__ldcg(&base.hdr->err) != 0u) break;
-        const long long item = base.remap ? (long long)base.remap[idx] : (long long)idx;
+        const long long item = base.remap ? (long long)base.remap[idx] : item_lo + (long long)idx;
         const int jb = job_of(jobs, n_jobs, item);
         if (jb != cur_job) {
             job_params(base, jobs[jb], p);
@@ -1218,8 +1231,8 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
         }
         const int li = (int)(item - jobs[jb].item_begin);
         // failures record the global item index
-        if (run_source<PM, -1>(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], bw_pl_all[wib],
-                               bw_fr_all[wib], ph, relaxed, settled))
+        if (run_source<PM, MODE>(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], bw_pl_all[wib],
+                                 bw_fr_all[wib], ph, relaxed, settled))
             done_src++;
     }
     flush_counters(base, ph, relaxed, settled, done_src);
@@ -1376,7 +1389,9 @@ cs_status retry_chain(const cs::PrimalParams &p, const cs_plan *plan, const Layo
     return CS_OK;
 }
 
-int lanes_for(int mode, int k) { return mode == cs::MODE_SHORTEST ? 2 * k : (mode == cs::MODE_SEGMENT ? k : 1); }
+int lanes_for(int mode, int k) {
+    return (mode == cs::MODE_SHORTEST || mode == cs::MODE_BOTH) ? 2 * k : (mode == cs::MODE_SEGMENT ? k : 1);
+}
 
 cs_status validate_primal(const cs_primal_graph *g) {
     if (!g) return fail(CS_ERR_ARG, "graph is NULL");
@@ -1439,17 +1454,29 @@ cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, c
     return CS_OK;
 }
 
+template <int MODE>
+void launch_batch_mode(const cs::PrimalParams &p, int minb, int blocks, const cs_batch_job *jobs_dev, int n_jobs,
+                       long long lo, long long hi, cudaStream_t stream) {
+    if (p.P <= 8) {
+        if (minb == 3) cs::batch_kernel<8, 3, MODE><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, lo, hi);
+        else cs::batch_kernel<8, 2, MODE><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, lo, hi);
+    } else {
+        cs::batch_kernel<CS_MAX_DEGREE, 2, MODE><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, lo, hi);
+    }
+}
+
+// mode: the jobs' common mode (0 or 1) for a mode-specialised kernel, else -1
 cs_status launch_batch(cs::PrimalParams &p, const cs_plan *plan, const cs_batch_job *jobs_dev, int n_jobs,
-                       long long n_items, int n_slots, cudaStream_t stream) {
+                       long long item_lo, long long item_hi, int n_slots, int mode, cudaStream_t stream) {
     const int blocks = (n_slots + 7) / 8;
     p.n_slots = n_slots;
     const int minb = resolve_variant(plan);
-    if (p.P <= 8) {
-        if (minb == 3) cs::batch_kernel<8, 3><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, n_items);
-        else cs::batch_kernel<8, 2><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, n_items);
-    } else {
-        cs::batch_kernel<CS_MAX_DEGREE, 2><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, n_items);
-    }
+    if (mode == cs::MODE_SHORTEST)
+        launch_batch_mode<cs::MODE_SHORTEST>(p, minb, blocks, jobs_dev, n_jobs, item_lo, item_hi, stream);
+    else if (mode == cs::MODE_SEGMENT)
+        launch_batch_mode<cs::MODE_SEGMENT>(p, minb, blocks, jobs_dev, n_jobs, item_lo, item_hi, stream);
+    else
+        launch_batch_mode<-1>(p, minb, blocks, jobs_dev, n_jobs, item_lo, item_hi, stream);
     g_counters[3]++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "batch_kernel launch");
@@ -1807,12 +1834,14 @@ cs_status batch_shape(const cs_batch_job *jobs, int n_jobs, BatchShape &b) {
     for (int j = 0; j < n_jobs; j++) {
         cs_status st = validate_primal(&jobs[j].g);
         if (st != CS_OK) return st;
-        if (jobs[j].mode != cs::MODE_SHORTEST && jobs[j].mode != cs::MODE_SEGMENT)
-            return fail(CS_ERR_ARG, "batch job mode must be 0 (shortest) or 1 (segment)");
+        if (jobs[j].mode != cs::MODE_SHORTEST && jobs[j].mode != cs::MODE_SEGMENT && jobs[j].mode != cs::MODE_BOTH)
+            return fail(CS_ERR_ARG, "batch job mode must be 0 (shortest), 1 (segment) or 3 (both)");
+        if (jobs[j].mode == cs::MODE_BOTH && !jobs[j].out2_dev) return fail(CS_ERR_ARG, "mode 3 job without out2_dev");
         if (jobs[j].k < 1 || jobs[j].k > CS_MAX_THRESHOLDS) return fail(CS_ERR_ARG, "threshold count out of range");
         if (!(jobs[j].speed_m_s > 0.0f)) return fail(CS_ERR_ARG, "speed_m_s must be finite and positive");
         if (!jobs[j].out_dev) return fail(CS_ERR_ARG, "job without out_dev");
-        if (jobs[j].mode == cs::MODE_SHORTEST && jobs[j].compute_closeness && !jobs[j].bucket_dev)
+        if ((jobs[j].mode == cs::MODE_SHORTEST || jobs[j].mode == cs::MODE_BOTH) && jobs[j].compute_closeness &&
+            !jobs[j].bucket_dev)
             return fail(CS_ERR_ARG, "shortest job with closeness needs bucket_dev");
         b.max_n = std::max(b.max_n, jobs[j].g.n_bound);
         b.P = std::max(b.P, jobs[j].g.max_out_degree);
@@ -1880,8 +1909,28 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
     cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), stream);
     if (e != cudaSuccess) return cuda_fail(e, "batch reset");
     if (n_items == 0) return CS_OK;
-    st = launch_batch(p, plan, jobs_dev, n_jobs, n_items, plan->n_slots, stream);
-    if (st != CS_OK) return st;
+    // consecutive jobs of one mode run as one launch of that mode's kernel (a smaller instruction
+    // footprint than the all-mode kernel); more than four such runs use the all-mode kernel once
+    struct Run {
+        long long lo, hi;
+        int mode;
+    };
+    std::vector<Run> runs;
+    for (int j = 0; j < n_jobs; j++) {
+        const int m = (jobs_host[j].mode == cs::MODE_SHORTEST || jobs_host[j].mode == cs::MODE_SEGMENT)
+                          ? jobs_host[j].mode : -1;
+        const long long lo = jobs_host[j].item_begin, hi = lo + std::max(0, jobs_host[j].n_sources);
+        if (!runs.empty() && runs.back().mode == m) runs.back().hi = hi;
+        else runs.push_back({lo, hi, m});
+    }
+    if (runs.size() > 4) runs.assign(1, Run{0, n_items, -1});
+    for (const Run &r : runs) {
+        if (r.hi <= r.lo) continue;
+        e = cudaMemsetAsync(&p.hdr->work_next, 0, sizeof(unsigned long long), stream);
+        if (e != cudaSuccess) return cuda_fail(e, "batch counter reset");
+        st = launch_batch(p, plan, jobs_dev, n_jobs, r.lo, r.hi, plan->n_slots, r.mode, stream);
+        if (st != CS_OK) return st;
+    }
     if (!(flags & CS_BATCH_ASYNC)) {
         cs::WsHeader h;
         e = cs::read_header(p.hdr, h, stream, true);
@@ -1890,7 +1939,7 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
         const long long n_over = h.n_failed;
         if (h.n_failed > 0u) {
             st = retry_chain(p, plan, lay, base, b.max_n, P, h, stream, true, [&](cs::PrimalParams &p2, int slots2) {
-                return launch_batch(p2, plan, jobs_dev, n_jobs, n_items, slots2, stream);
+                return launch_batch(p2, plan, jobs_dev, n_jobs, 0, n_items, slots2, -1, stream);
             });
             if (st != CS_OK) return st;
         }
@@ -1902,7 +1951,7 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
     int max_n = 0, n_pref = 0;
     for (int j = 0; j < n_jobs; j++) {
         const cs_batch_job &jb = jobs_host[j];
-        if (jb.mode == cs::MODE_SHORTEST && jb.compute_closeness && jb.n_sources > 0) {
+        if ((jb.mode == cs::MODE_SHORTEST || jb.mode == cs::MODE_BOTH) && jb.compute_closeness && jb.n_sources > 0) {
             max_n = std::max(max_n, jb.g.n_bound);
             n_pref++;
         }

@@ -591,6 +591,8 @@ class Server:
             n = min(t.total - t.next_off, max(1, int(budget / c)))
             chunks.append((t, t.next_off, n))
             budget -= n * c
+        if kd.name == "primal":
+            chunks.sort(key=lambda c: c[0]._job.mode)  # one launch per mode group
         table = (kd.job_cls * len(chunks))()
         for j, (t, off, n) in enumerate(chunks):
             C.memmove(C.byref(table[j]), C.byref(t._job), kd.job_bytes)

@@ -109,7 +109,8 @@ typedef struct {
     size_t workspace_bytes;
 } cs_plan;
 
-/* One job of a batched launch: a graph, a mode, its thresholds, sources and outputs.  Many jobs of
+/* One job of a batched launch: a graph, a mode (0 shortest, 1 segment, 3 both from one search per
+ * source), its thresholds, sources and outputs.  Many jobs of
  * uneven size run in one persistent launch (cs_batch_run), each source an item of a device queue. */
 typedef struct {
     cs_primal_graph g;
@@ -130,6 +131,8 @@ typedef struct {
     double *out_dev;          /* [7 (shortest) or 4 (segment)][k][n_bound], zeroed by the caller */
     double *bucket_dev;       /* [3][k][n_bound] scratch for shortest closeness: zero before the first run;
                                  every successful run leaves it zero again */
+    double *out2_dev;         /* mode 3 (shortest + segment from one search per source): the segment rows
+                                 [4][k][n_bound]; out_dev holds the shortest rows */
     int64_t item_begin;       /* first queue item of this job (set by cs_batch_prepare) */
 } cs_batch_job;
 

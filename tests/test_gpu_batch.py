@@ -67,6 +67,29 @@ def test_batch_matches_plain_calls():
         _check(res, spec, f"job {j} ({spec['mode']})")
 
 
+def test_batch_fused_shortest_segment():
+    """A shortest-path job and a segment job on the same graph and thresholds run as one fused job
+    (one search per source feeds both) and still equal their plain calls."""
+    gs = _graphs()
+    jobs = [dict(ns=gs[0], mode="shortest", distances=[500, 1000]),
+            dict(ns=gs[0], mode="segment", distances=[500, 1000]),
+            dict(ns=gs[1], mode="segment", distances=[300, 800, 1600]),
+            dict(ns=gs[1], mode="shortest", distances=[300, 800, 1600]),
+            dict(ns=gs[2], mode="segment", distances=[700])]
+    b = Batch(jobs, fuse=True)
+    assert b.n_fused == 2
+    assert b.n_items == sum(len(j["ns"].node_indices()) for j in jobs) - len(gs[0].node_indices()) - \
+        len(gs[1].node_indices())
+    b.run()
+    for j, (res, spec) in enumerate(zip(b.results(), jobs)):
+        _check(res, spec, f"job {j} ({spec['mode']}, fused)")
+    b.zero_outputs()
+    b.capture()
+    b.replay()
+    for j, (res, spec) in enumerate(zip(b.results(), jobs)):
+        _check(res, spec, f"job {j} ({spec['mode']}, fused, graph replay)")
+
+
 def test_batch_overflow_retry():
     # capacity 48 < reach: most sources overflow and are redone in-call at full capacity
     jobs = _jobs(_graphs())[:3]
