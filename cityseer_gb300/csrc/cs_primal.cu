@@ -566,12 +566,17 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     }
     if constexpr (SYNC) __syncthreads();
     phase_mark(ph, 3, tph);
-    if (!p.betweenness) return;  // uniform over the block
+    if constexpr (!SYNC) {
+        if (!p.betweenness) return;
+    }
+    // in the block-synchronous form the flag can differ between a block's warps (batched jobs):
+    // a warp without betweenness runs the remaining phases empty, so every warp meets the barriers
+    const int Rb = (SYNC && !p.betweenness) ? 0 : R;
     // --- sigma (f32 path counts) in settle order, chunked: ready once in-chunk preds are done
     float *sig = (float *)s.sig;
-    for (int base = 0; base < R; base += 32) {
+    for (int base = 0; base < Rb; base += 32) {
         const int i = base + lane;
-        const bool act = i < R;
+        const bool act = i < Rb;
         int pl[PM];
         const int np = act ? load_preds<PM>(s, i, P, pl) : 0;
         unsigned pm = 0;
@@ -608,16 +613,16 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     // they are half-integers and exact; otherwise they carry f32 rounding (well inside 1e-5).
     const int L = p.L;  // 2K floats per node: [0,K) plain, [K,2K) beta-weighted
     float *dl = (float *)s.dl;
-    for (int i = lane; i < R; i += 32)
+    for (int i = lane; i < Rb; i += 32)
         for (int q = 0; q < 2 * K; q++) dl[(size_t)i * L + q] = 0.0f;
     __syncwarp();
     const bool unit_wt = (wt == 1.0f);
     const double wtd = (double)wt;
-    const int nchunks = failed ? 0 : (R + 31) / 32;
+    const int nchunks = failed ? 0 : (Rb + 31) / 32;
     for (int ch = nchunks - 1; ch >= 0; ch--) {
         const int base = ch * 32;
         const int i = base + lane;
-        const bool act = i < R;
+        const bool act = i < Rb;
         int pl[PM];
         const int np = act ? load_preds<PM>(s, i, P, pl) : 0;
         unsigned pm = 0;
@@ -1238,6 +1243,105 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
     flush_counters(base, ph, relaxed, settled, done_src);
 }
 
+// Batched shortest-path items with block-synchronous phases (as primal_sync_kernel): a block
+// claims one item per warp; each warp looks its item's job up.  Every warp reaches every barrier.
+template <int PM, int MINB>
+__global__ void __launch_bounds__(256, MINB) batch_sync_kernel(const PrimalParams base, const cs_batch_job *jobs,
+                                                               int n_jobs, long long item_lo, long long item_hi) {
+    __shared__ uint32_t hist_all[8][256];
+    __shared__ int cnt_all[8][2 * MAXK];
+    __shared__ long long ph_all[8][8];
+    __shared__ int bw_pl_all[8][PM * 32];
+    __shared__ float bw_fr_all[8][PM * 32];
+    __shared__ long long blk_base;
+    __shared__ unsigned blk_err;
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    const int slot0 = blockIdx.x * (blockDim.x >> 5);
+    const int nw = min((int)(blockDim.x >> 5), base.n_slots - slot0);
+    const bool has_slot = wib < nw;
+    const SlotPtrs s = slot_ptrs(base.dense, base.dense_stride, base.compact, (size_t)base.cap, base.P, base.L,
+                                 has_slot ? slot0 + wib : 0, base.g.n_bound);
+    long long relaxed = 0, settled = 0, done_src = 0;
+    long long *ph = ph_all[wib];
+    if (lane < 8) ph[lane] = 0;
+    __syncwarp();
+    const long long n = item_hi - item_lo;
+    PrimalParams p;
+    int cur_job = -1;
+    while (true) {
+        if (threadIdx.x == 0) {
+            blk_base = (long long)atomicAdd(&base.hdr->work_next, (unsigned long long)max(nw, 0));
+            blk_err = __ldcg(&base.hdr->err);
+        }
+        __syncthreads();
+        const long long b0 = blk_base;
+        const unsigned berr = blk_err;
+        __syncthreads();
+        if (nw <= 0 || b0 >= n || berr != 0u) break;
+        const long long idx = b0 + wib;
+        const bool mine = has_slot && idx < n;
+        int src = 0, li = 0;
+        const long long item = item_lo + idx;
+        if (mine) {
+            const int jb = job_of(jobs, n_jobs, item);
+            if (jb != cur_job) {
+                job_params(base, jobs[jb], p);
+                cur_job = jb;
+            }
+            li = (int)(item - jobs[jb].item_begin);
+            src = p.src_list[li];
+        } else if (cur_job < 0) {
+            job_params(base, jobs[0], p);  // an idle warp still runs the phases (R = 0)
+            cur_job = 0;
+        }
+        long long t0 = clock64();
+        int R = 0;
+        if (mine) R = warp_search(p, s, src, relaxed);
+        phase_mark(ph, 0, t0);
+        __syncthreads();
+        const bool ok = mine && R >= 0;
+        if (mine && R < 0) {
+            for (int j = lane; j < p.g.n_bound; j += 32) {
+                s.dist[j] = __int_as_float(INF_BITS);
+                s.aux[j] = 0u;
+            }
+            if (lane == 0) {
+                const unsigned f = atomicAdd(&base.hdr->n_failed, 1u);
+                if (f < (unsigned)base.fail_cap) base.failed[f] = (int)item;
+                else raise_err(base.hdr, CS_ERR_CAPACITY, 8);
+            }
+        }
+        if (ok) {
+            warp_sort(s, R, hist_all[wib]);
+            __syncwarp();
+            for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+        }
+        __syncwarp();
+        phase_mark(ph, 1, t0);
+        __syncthreads();
+        // every warp of the block runs the phases with the same closeness / betweenness flags
+        // only when its jobs agree on them; the barrier count must not depend on the job
+        shortest_accumulate<PM, true>(p, s, ok ? src : 0, ok ? R : 0, ph, cnt_all[wib], bw_pl_all[wib],
+                                      bw_fr_all[wib]);
+        __syncwarp();
+        t0 = clock64();
+        if (ok) {
+            for (int i = lane; i < R; i += 32) {
+                const int v = s.ord[i];
+                s.dist[v] = __int_as_float(INF_BITS);
+                s.aux[v] = 0u;
+            }
+            settled += R;
+            done_src++;
+        }
+        __syncwarp();
+        phase_mark(ph, 6, t0);
+        __syncthreads();
+    }
+    flush_counters(base, ph, relaxed, settled, done_src);
+}
+
 // Source-indexed plan on the device (prepare_source_sampling with source_indices): src_wt = node
 // weight and eligible = 1 at each listed source, 0 elsewhere.  Pass 0 clears, pass 1 scatters.
 __global__ void source_weights_kernel(const int32_t *sources, long long n, const float *node_w, int n_bound,
@@ -1471,7 +1575,10 @@ cs_status launch_batch(cs::PrimalParams &p, const cs_plan *plan, const cs_batch_
     const int blocks = (n_slots + 7) / 8;
     p.n_slots = n_slots;
     const int minb = resolve_variant(plan);
-    if (mode == cs::MODE_SHORTEST)
+    if (mode == cs::MODE_SHORTEST && p.P <= 8 && !p.rerun && phase_sync()) {
+        if (minb == 3) cs::batch_sync_kernel<8, 3><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, item_lo, item_hi);
+        else cs::batch_sync_kernel<8, 2><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, item_lo, item_hi);
+    } else if (mode == cs::MODE_SHORTEST)
         launch_batch_mode<cs::MODE_SHORTEST>(p, minb, blocks, jobs_dev, n_jobs, item_lo, item_hi, stream);
     else if (mode == cs::MODE_SEGMENT)
         launch_batch_mode<cs::MODE_SEGMENT>(p, minb, blocks, jobs_dev, n_jobs, item_lo, item_hi, stream);
