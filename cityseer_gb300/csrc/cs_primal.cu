@@ -790,10 +790,12 @@ CS_PHASE_INLINE __device__ void segment_accumulate(const PrimalParams &p, const 
         }
     }
     // closeness integrals over visited edges (rust/src/centrality.rs:2201-2317), into the source
-    if (p.closeness) {
-        double acc[3 * MAXK];
+    // thresholds in groups of 4: per lane 12 f64 accumulators in registers and 4 unrolled copies of
+    // the integral code (not 16 of each), one pass over the visited edges per group
+    if (p.closeness) for (int kb = 0; kb < K; kb += 4) {
+        double acc[12];
 #pragma unroll
-        for (int q = 0; q < 3 * MAXK; q++) acc[q] = 0.0;
+        for (int q = 0; q < 12; q++) acc[q] = 0.0;
         for (int i = lane; i < R; i += 32) {
             const int u = s.ord[i];
             const float au = route_cost(s.sd[i], p.speed);
@@ -818,41 +820,43 @@ CS_PHASE_INLINE __device__ void segment_accumulate(const PrimalParams &p, const 
                 const float C = __fdiv_rn(fadd(fadd(elen, A), B), 2.0f), D = C;
                 const float Ci = fadd(Ai, fmul(__fadd_rn(C, -A), imp)), Di = Ci;
 #pragma unroll
-                for (int k = MAXK - 1; k >= 0; k--) {
-                    if (k >= K) continue;
+                for (int q = 0; q < 4; q++) {
+                    const int k = kb + q;
+                    if (k >= K) break;
                     const float df = p.dk[k];
                     const float beta = p.beta[k], nbeta = -beta;
                     const float inb = (beta != 0.0f) ? __fdiv_rn(1.0f, nbeta) : 0.0f;
                     if (A < df) {
                         float cc = C, cci = Ci;
                         if (cc > df) { cc = df; cci = fadd(Ai, fmul(__fadd_rn(df, -A), imp)); }
-                        acc[k] += (double)__fadd_rn(cc, -A);
+                        acc[q] += (double)__fadd_rn(cc, -A);
                         const float sh = (Ai < 1.0f) ? logf(cci) : logf(fmaxf(__fdiv_rn(cci, Ai), 1.1920929e-07f));
-                        acc[MAXK + k] += (double)sh;
+                        acc[4 + q] += (double)sh;
                         const float bet = (beta == 0.0f) ? __fadd_rn(cci, -Ai)
                                                          : fmul(__fadd_rn(expf(fmul(nbeta, cci)), -expf(fmul(nbeta, Ai))), inb);
-                        acc[2 * MAXK + k] += (double)bet;
+                        acc[8 + q] += (double)bet;
                     }
                     if (B == D) continue;
                     if (B <= df) {
                         float cd = D, cdi = Di;
                         if (cd > df) { cd = df; cdi = fadd(Bi, fmul(__fadd_rn(df, -B), imp)); }
-                        acc[k] += (double)__fadd_rn(cd, -B);
+                        acc[q] += (double)__fadd_rn(cd, -B);
                         const float sh = (Bi < 1.0f) ? logf(cdi) : logf(fmaxf(__fdiv_rn(cdi, Bi), 1.1920929e-07f));
-                        acc[MAXK + k] += (double)sh;
+                        acc[4 + q] += (double)sh;
                         const float bet = (beta == 0.0f) ? __fadd_rn(cdi, -Bi)
                                                          : fmul(__fadd_rn(expf(fmul(nbeta, cdi)), -expf(fmul(nbeta, Bi))), inb);
-                        acc[2 * MAXK + k] += (double)bet;
+                        acc[8 + q] += (double)bet;
                     }
                 }
             }
         }
 #pragma unroll
-        for (int k = 0; k < MAXK; k++) {
+        for (int q = 0; q < 4; q++) {
+            const int k = kb + q;
             if (k >= K) break;
-            const double a0 = warp_sum_d(acc[k]);
-            const double a1 = warp_sum_d(acc[MAXK + k]);
-            const double a2 = warp_sum_d(acc[2 * MAXK + k]);
+            const double a0 = warp_sum_d(acc[q]);
+            const double a1 = warp_sum_d(acc[4 + q]);
+            const double a2 = warp_sum_d(acc[8 + q]);
             if (lane == 0) {
                 atomicAdd(out + ((size_t)0 * K + k) * N + src, a0);
                 atomicAdd(out + ((size_t)1 * K + k) * N + src, a1);
