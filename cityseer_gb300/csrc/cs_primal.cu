@@ -474,10 +474,21 @@ __device__ __forceinline__ int load_preds(const SlotPtrs &s, int i, int P, int *
     return np;
 }
 
+// Phase barrier of the block-synchronous forms: GW warps (a whole 8-warp block: __syncthreads;
+// 4: a named barrier per half block) meet at the end of each phase.  GW = 0: no barrier.
+template <int GW>
+__device__ __forceinline__ void phase_barrier() {
+    if constexpr (GW == 8) {
+        __syncthreads();
+    } else if constexpr (GW > 0) {
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + (int)(threadIdx.x >> 5) / GW), "r"(GW * 32) : "memory");
+    }
+}
+
 // With SYNC, every warp of the block runs each phase together (a block barrier ends each phase,
 // and a warp without a source runs the phases with R = 0), so at any time a block's warps fetch one
 // phase's code; there is no early return in that form.
-template <int PM, bool SYNC>
+template <int PM, int SYNC>
 CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R, long long *ph,
                                     int *cnt, int *bw_pl, float *bw_fr) {
     const int lane = lane_id();
@@ -525,7 +536,7 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
         if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 1);
     }
     __syncwarp();
-    if constexpr (SYNC) __syncthreads();
+    phase_barrier<SYNC>();
     phase_mark(ph, 2, tph);
     // --- closeness (rust/src/centrality.rs:1733-1780).  Density, farness and harmonic terms do not
     // depend on the threshold: they go once into the bucket of the first qualifying threshold and a
@@ -564,14 +575,14 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
             }
         }
     }
-    if constexpr (SYNC) __syncthreads();
+    phase_barrier<SYNC>();
     phase_mark(ph, 3, tph);
-    if constexpr (!SYNC) {
+    if constexpr (SYNC == 0) {
         if (!p.betweenness) return;
     }
     // in the block-synchronous form the flag can differ between a block's warps (batched jobs):
     // a warp without betweenness runs the remaining phases empty, so every warp meets the barriers
-    const int Rb = (SYNC && !p.betweenness) ? 0 : R;
+    const int Rb = (SYNC != 0 && !p.betweenness) ? 0 : R;
     // --- sigma (f32 path counts) in settle order, chunked: ready once in-chunk preds are done
     float *sig = (float *)s.sig;
     for (int base = 0; base < Rb; base += 32) {
@@ -606,7 +617,7 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
             break;
         }
     }
-    if constexpr (SYNC) __syncthreads();
+    phase_barrier<SYNC>();
     phase_mark(ph, 4, tph);
     // --- backward Brandes sweep, all K thresholds in one pass (rust/src/centrality.rs:823-873,
     // 1782-1835).  Dependencies accumulate in f32: for sources whose paths are unique (sigma == 1)
@@ -686,7 +697,7 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
             break;
         }
     }
-    if constexpr (SYNC) __syncthreads();
+    phase_barrier<SYNC>();
     phase_mark(ph, 5, tph);
 }
 
@@ -997,18 +1008,18 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
     __syncwarp();
     phase_mark(ph, 1, t0);
     if constexpr (MODE == MODE_SHORTEST) {
-        shortest_accumulate<PM, false>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
+        shortest_accumulate<PM, 0>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
     } else if constexpr (MODE == MODE_SEGMENT) {
         segment_accumulate<PM>(p, s, src, R);
     } else if constexpr (MODE == MODE_TREE) {
         tree_rows<PM>(p, s, li, R);
     } else {
-        if (p.mode == MODE_SHORTEST) shortest_accumulate<PM, false>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
+        if (p.mode == MODE_SHORTEST) shortest_accumulate<PM, 0>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
         else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
         else if (p.mode == MODE_BOTH) {
             // one search and settle order serve both: shortest rows, then segment rows (its own
             // single-predecessor replay over the same positions)
-            shortest_accumulate<PM, false>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
+            shortest_accumulate<PM, 0>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
             __syncwarp();
             segment_accumulate<PM>(p, s, src, R);
         } else tree_rows<PM>(p, s, li, R);
@@ -1079,39 +1090,40 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
 // hold the code of at most one phase per resident block.  Every warp reaches every barrier: a warp
 // without a source (or whose source overflowed) runs the phases with R = 0.
 // ------------------------------------------------------------------------------------------
-template <int PM, int MINB, int WPB>
+template <int PM, int MINB, int WPB, int GW>
 __global__ void __launch_bounds__(WPB * 32, MINB) primal_sync_kernel(const PrimalParams p) {
     __shared__ uint32_t hist_all[WPB][256];
     __shared__ int cnt_all[WPB][2 * MAXK];
     __shared__ long long ph_all[WPB][8];
     __shared__ int bw_pl_all[WPB][PM * 32];
     __shared__ float bw_fr_all[WPB][PM * 32];
-    __shared__ long long blk_base;
-    __shared__ unsigned blk_err;
+    __shared__ long long blk_base[WPB / GW];
+    __shared__ unsigned blk_err[WPB / GW];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
-    const int slot0 = blockIdx.x * (blockDim.x >> 5);
-    const int nw = min((int)(blockDim.x >> 5), p.n_slots - slot0);  // warps of this block with a slot
-    const bool has_slot = wib < nw;
+    const int grp = wib / GW, gw = wib % GW;  // phase group of GW warps
+    const int slot0 = blockIdx.x * (blockDim.x >> 5) + grp * GW;
+    const int nw = min(GW, p.n_slots - slot0);  // warps of this group with a slot
+    const bool has_slot = gw < nw;
     const SlotPtrs s = slot_ptrs(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.P, p.L,
-                                 has_slot ? slot0 + wib : 0, p.g.n_bound);
+                                 has_slot ? slot0 + gw : 0, p.g.n_bound);
     long long relaxed = 0, settled = 0, done_src = 0;
     long long *ph = ph_all[wib];
     if (lane < 8) ph[lane] = 0;
     __syncwarp();
     const long long n = p.n_src;
     while (true) {
-        if (threadIdx.x == 0) {
-            blk_base = (long long)atomicAdd(p.rerun ? &p.hdr->work_next2 : &p.hdr->work_next,
-                                            (unsigned long long)max(nw, 0));
-            blk_err = __ldcg(&p.hdr->err);
+        if (gw == 0 && lane == 0) {
+            blk_base[grp] = (long long)atomicAdd(p.rerun ? &p.hdr->work_next2 : &p.hdr->work_next,
+                                                 (unsigned long long)max(nw, 0));
+            blk_err[grp] = __ldcg(&p.hdr->err);
         }
-        __syncthreads();
-        const long long base = blk_base;
-        const unsigned berr = blk_err;
-        __syncthreads();
+        phase_barrier<GW>();
+        const long long base = blk_base[grp];
+        const unsigned berr = blk_err[grp];
+        phase_barrier<GW>();
         if (nw <= 0 || base >= n || berr != 0u) break;
-        const long long idx = base + wib;
+        const long long idx = base + gw;
         const bool mine = has_slot && idx < n;
         const int li = mine ? (p.remap ? p.remap[idx] : (int)idx) : 0;
         const int src = mine ? p.src_list[li] : 0;
@@ -1119,7 +1131,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB) primal_sync_kernel(const Prima
         int R = 0;
         if (mine) R = warp_search(p, s, src, relaxed);
         phase_mark(ph, 0, t0);
-        __syncthreads();
+        phase_barrier<GW>();
         const bool ok = mine && R >= 0;
         if (mine && R < 0) {
             for (int j = lane; j < p.g.n_bound; j += 32) {
@@ -1139,8 +1151,8 @@ __global__ void __launch_bounds__(WPB * 32, MINB) primal_sync_kernel(const Prima
         }
         __syncwarp();
         phase_mark(ph, 1, t0);
-        __syncthreads();
-        shortest_accumulate<PM, true>(p, s, src, ok ? R : 0, ph, cnt_all[wib], bw_pl_all[wib], bw_fr_all[wib]);
+        phase_barrier<GW>();
+        shortest_accumulate<PM, GW>(p, s, src, ok ? R : 0, ph, cnt_all[wib], bw_pl_all[wib], bw_fr_all[wib]);
         __syncwarp();
         t0 = clock64();
         if (ok) {
@@ -1154,7 +1166,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB) primal_sync_kernel(const Prima
         }
         __syncwarp();
         phase_mark(ph, 6, t0);
-        __syncthreads();
+        phase_barrier<GW>();
     }
     flush_counters(p, ph, relaxed, settled, done_src);
 }
@@ -1326,8 +1338,8 @@ __global__ void __launch_bounds__(256, MINB) batch_sync_kernel(const PrimalParam
         __syncthreads();
         // every warp of the block runs the phases with the same closeness / betweenness flags
         // only when its jobs agree on them; the barrier count must not depend on the job
-        shortest_accumulate<PM, true>(p, s, ok ? src : 0, ok ? R : 0, ph, cnt_all[wib], bw_pl_all[wib],
-                                      bw_fr_all[wib]);
+        shortest_accumulate<PM, 8>(p, s, ok ? src : 0, ok ? R : 0, ph, cnt_all[wib], bw_pl_all[wib],
+                                   bw_fr_all[wib]);
         __syncwarp();
         t0 = clock64();
         if (ok) {
@@ -1534,9 +1546,10 @@ bool phase_sync() {
 template <int MODE>
 void launch_primal_mode(const cs::PrimalParams &p, int P, int minb, int blocks, cudaStream_t stream) {
     if (MODE == cs::MODE_SHORTEST && P <= 8 && phase_sync()) {
-        // (12- and 24-warp blocks measured no faster than 8 on the 202,500-node lattice)
-        if (minb == 3) cs::primal_sync_kernel<8, 3, 8><<<blocks, 256, 0, stream>>>(p);
-        else cs::primal_sync_kernel<8, 2, 8><<<blocks, 256, 0, stream>>>(p);
+        // whole 8-warp blocks in lockstep: on the 202,500-node lattice 12- and 24-warp blocks ran no
+        // faster and 4-warp groups (named barriers) 3% slower
+        if (minb == 3) cs::primal_sync_kernel<8, 3, 8, 8><<<blocks, 256, 0, stream>>>(p);
+        else cs::primal_sync_kernel<8, 2, 8, 8><<<blocks, 256, 0, stream>>>(p);
         return;
     }
     if (P <= 8) {
