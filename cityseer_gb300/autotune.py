@@ -20,7 +20,7 @@ from . import _native, centrality, device
 from .common import pair_distances_betas_time
 
 DELTA_MULTS = (1.0, 2.0, 4.0)
-VARIANTS = (3, 2)
+VARIANTS = (4, 3, 2)
 
 
 def cache_path() -> Path:
@@ -65,7 +65,7 @@ def key_of(csr, mode: str, secs, k: int) -> str:
 
 
 def default(csr, speed: float) -> dict:
-    return {"delta": 2.0 * csr.median_edge_seconds(speed), "variant": 3, "tuned": False}
+    return {"delta": 2.0 * csr.median_edge_seconds(speed), "variant": 4, "tuned": False}
 
 
 def lookup(ns, csr, mode: str, d, s, speed: float) -> dict:

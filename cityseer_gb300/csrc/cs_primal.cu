@@ -1521,18 +1521,20 @@ cs_status validate_primal(const cs_primal_graph *g) {
     return CS_OK;
 }
 
-// Register budget of the P <= 8 kernels: 3 resident 256-thread blocks per SM (80 registers) or 2
-// (128 registers).  A plan's variant field selects it; 0 means the default (3), which the
-// environment variable CS_MIN_BLOCKS_PER_SM=2 overrides.
+// Register budget of the P <= 8 kernels: 4 resident 256-thread blocks per SM (64 registers), 3
+// (80 registers) or 2 (128 registers).  A plan's variant field selects it; 0 means the default
+// (4: the block-synchronous shortest-path kernel is memory-latency bound and gains from the extra
+// warps), which the environment variable CS_MIN_BLOCKS_PER_SM (2, 3 or 4) overrides.
 int resolve_variant(const cs_plan *plan) {
-    if (plan && (plan->variant == 2 || plan->variant == 3)) return plan->variant;
+    if (plan && plan->variant >= 2 && plan->variant <= 4) return plan->variant;
     const char *e = getenv("CS_MIN_BLOCKS_PER_SM");
-    return (e && e[0] == '2') ? 2 : 3;
+    return (e && e[0] >= '2' && e[0] <= '4') ? e[0] - '0' : 4;
 }
 
 cudaError_t occupancy_blocks(int P, int variant, int *bpsm) {
     if (P > 8)
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<CS_MAX_DEGREE, 2, 0>, 256, 0);
+    if (variant == 4) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 4, 0>, 256, 0);
     if (variant == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 3, 0>, 256, 0);
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpsm, cs::primal_kernel<8, 2, 0>, 256, 0);
 }
@@ -1548,12 +1550,14 @@ void launch_primal_mode(const cs::PrimalParams &p, int P, int minb, int blocks, 
     if (MODE == cs::MODE_SHORTEST && P <= 8 && phase_sync()) {
         // whole 8-warp blocks in lockstep: on the 202,500-node lattice 12- and 24-warp blocks ran no
         // faster and 4-warp groups (named barriers) 3% slower
-        if (minb == 3) cs::primal_sync_kernel<8, 3, 8, 8><<<blocks, 256, 0, stream>>>(p);
+        if (minb == 4) cs::primal_sync_kernel<8, 4, 8, 8><<<blocks, 256, 0, stream>>>(p);
+        else if (minb == 3) cs::primal_sync_kernel<8, 3, 8, 8><<<blocks, 256, 0, stream>>>(p);
         else cs::primal_sync_kernel<8, 2, 8, 8><<<blocks, 256, 0, stream>>>(p);
         return;
     }
     if (P <= 8) {
-        if (minb == 3) cs::primal_kernel<8, 3, MODE><<<blocks, 256, 0, stream>>>(p);
+        if (minb == 4) cs::primal_kernel<8, 4, MODE><<<blocks, 256, 0, stream>>>(p);
+        else if (minb == 3) cs::primal_kernel<8, 3, MODE><<<blocks, 256, 0, stream>>>(p);
         else cs::primal_kernel<8, 2, MODE><<<blocks, 256, 0, stream>>>(p);
     } else {
         cs::primal_kernel<CS_MAX_DEGREE, 2, MODE><<<blocks, 256, 0, stream>>>(p);
@@ -1579,7 +1583,8 @@ template <int MODE>
 void launch_batch_mode(const cs::PrimalParams &p, int minb, int blocks, const cs_batch_job *jobs_dev, int n_jobs,
                        long long lo, long long hi, cudaStream_t stream) {
     if (p.P <= 8) {
-        if (minb == 3) cs::batch_kernel<8, 3, MODE><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, lo, hi);
+        if (minb == 4) cs::batch_kernel<8, 4, MODE><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, lo, hi);
+        else if (minb == 3) cs::batch_kernel<8, 3, MODE><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, lo, hi);
         else cs::batch_kernel<8, 2, MODE><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, lo, hi);
     } else {
         cs::batch_kernel<CS_MAX_DEGREE, 2, MODE><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, lo, hi);
@@ -1593,7 +1598,8 @@ cs_status launch_batch(cs::PrimalParams &p, const cs_plan *plan, const cs_batch_
     p.n_slots = n_slots;
     const int minb = resolve_variant(plan);
     if (mode == cs::MODE_SHORTEST && p.P <= 8 && !p.rerun && phase_sync()) {
-        if (minb == 3) cs::batch_sync_kernel<8, 3><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, item_lo, item_hi);
+        if (minb == 4) cs::batch_sync_kernel<8, 4><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, item_lo, item_hi);
+        else if (minb == 3) cs::batch_sync_kernel<8, 3><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, item_lo, item_hi);
         else cs::batch_sync_kernel<8, 2><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, item_lo, item_hi);
     } else if (mode == cs::MODE_SHORTEST)
         launch_batch_mode<cs::MODE_SHORTEST>(p, minb, blocks, jobs_dev, n_jobs, item_lo, item_hi, stream);
