@@ -280,13 +280,10 @@ def run_gpu(args):
         torch.distributed.barrier()
     clk = clocks.stop()
     step_s = float(np.mean(times))
-    t_max = step_s
-    if ws > 1:
-        tt = torch.tensor([step_s], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
     n_src = len(sp.process)
-    value = ws * n_src / t_max
+    from cityseer_gb300.replicas import job_throughput
+
+    value, t_max = job_throughput(n_src, step_s, dev)
     # ---- parity guard: the timed outputs equal the public API's first result
     res_rows = out.cpu().numpy()
     idx = np.asarray(ns.node_indices())
@@ -327,7 +324,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         if i > 0:
             e2e_times.append(time.perf_counter() - t0)
-    e2e_v = ws * n_src / float(np.mean(e2e_times)) if e2e_times else None
+    e2e_v = job_throughput(n_src, float(np.mean(e2e_times)), dev)[0] if e2e_times else None
     line = {
         "metric": METRIC,
         "value": value,
