@@ -174,6 +174,11 @@ SIGNATURES = {
         C.c_int32,
         [C.POINTER(DualGraph), C.POINTER(Query), C.POINTER(Plan), _ptr, C.c_size_t, Outputs, _ptr],
     ),
+    "cs_betweenness_od_shortest": (
+        C.c_int32,
+        [C.POINTER(PrimalGraph), C.POINTER(Query), _ptr, _ptr, _ptr, C.POINTER(Plan), _ptr, C.c_size_t, Outputs,
+         _ptr],
+    ),
     "cs_segment_centrality": (
         C.c_int32,
         [C.POINTER(PrimalGraph), C.POINTER(Query), C.POINTER(Plan), _ptr, C.c_size_t, Outputs, _ptr],

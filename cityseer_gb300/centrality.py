@@ -70,6 +70,49 @@ class CentralitySegmentResult(_Result):
     _rows = ("segment_density", "segment_harmonic", "segment_beta", "segment_betweenness")
 
 
+class BetweennessShortestResult(_Result):
+    """Result of betweenness_od_shortest (rust/src/centrality.rs:94-150)."""
+    _rows = ("node_betweenness", "node_betweenness_beta")
+
+
+class OdMatrix:
+    """Sparse origin-destination trip weights (rust/src/centrality.rs:56-91), from parallel arrays of
+    origin node indices, destination node indices and weights (COO).  A repeated (origin,
+    destination) pair keeps the weight given last, as the reference's map insert does.  Stored as
+    pairs sorted by (origin, destination); weights are f32."""
+
+    def __init__(self, origins, destinations, weights):
+        if not (len(origins) == len(destinations) == len(weights)):
+            raise ValueError(f"origins ({len(origins)}), destinations ({len(destinations)}), and weights "
+                             f"({len(weights)}) must have equal length")
+        o = np.asarray(origins, dtype=np.int64).reshape(-1)
+        d = np.asarray(destinations, dtype=np.int64).reshape(-1)
+        w = np.asarray(weights, dtype=np.float64).reshape(-1).astype(np.float32)
+        if (len(o) and o.min() < 0) or (len(d) and d.min() < 0):
+            raise OverflowError("can't convert negative int to unsigned")
+        order = np.lexsort((np.arange(len(o)), d, o))
+        o, d, w = o[order], d[order], w[order]
+        last = np.ones(len(o), bool)
+        if len(o) > 1:
+            last[:-1] = (o[1:] != o[:-1]) | (d[1:] != d[:-1])
+        self.origins, self.destinations, self.weights = o[last], d[last], w[last]
+
+    def len(self) -> int:
+        return int(len(self.origins))
+
+    def n_origins(self) -> int:
+        return int(len(np.unique(self.origins)))
+
+    def rows(self, n_bound: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(ptr [n_bound + 1], destinations, weights): each origin node's row, destinations
+        ascending.  Origins at or beyond n_bound have no row (the reference never looks them up)."""
+        keep = self.origins < n_bound
+        o = self.origins[keep]
+        ptr = np.zeros(n_bound + 1, np.int64)
+        np.cumsum(np.bincount(o, minlength=n_bound), out=ptr[1:])
+        return ptr, self.destinations[keep], self.weights[keep]
+
+
 # ---------------------------------------------------------------------------------------------
 # Source sampling plan
 # ---------------------------------------------------------------------------------------------
@@ -345,6 +388,64 @@ def centrality_shortest(ns, distances=None, betas=None, minutes=None, compute_cl
     if track:
         res.sampled_source_count = sp.sampled_count
         res.reachability_totals = [int(x) for x in reach_tot]
+    return res
+
+
+# ---------------------------------------------------------------------------------------------
+# betweenness_od_shortest (rust/src/centrality.rs:2419-2540)
+# ---------------------------------------------------------------------------------------------
+def betweenness_od_shortest(ns, od_matrix: OdMatrix, distances=None, betas=None, minutes=None,
+                            min_threshold_wt=None, speed_m_s=None, tolerance=None,
+                            pbar_disabled=None) -> BetweennessShortestResult:
+    """Shortest-path betweenness weighted by origin-destination trips: a search from every live
+    origin with a row; each reached destination within a threshold seeds the backward sweep with
+    its trip weight (and the weight times exp(-beta d) for the beta row)."""
+    speed = WALKING_SPEED if speed_m_s is None else float(speed_m_s)
+    dists, bets, secs = pair_distances_betas_time(speed, distances, betas, minutes, min_threshold_wt)
+    tol = validate_tolerance(tolerance)
+    nb = ns.node_bound()
+    node_indices = ns.node_indices()
+    K = len(dists)
+    ptr, dst, w = od_matrix.rows(nb)
+    idx = np.asarray(node_indices, np.int64)
+    live = ns.arrays()["live"][:nb]
+    has_row = ptr[1:] > ptr[:-1]
+    proc = idx[(live[idx] == 1) & has_row[idx]].astype(np.int32)
+    if len(proc):
+        # a destination beyond the node bound in a processed row is an index error in the reference
+        processed = np.zeros(nb, bool)
+        processed[proc] = True
+        used = dst[np.repeat(processed, np.diff(ptr))]
+        if len(used) and used.max() >= nb:
+            raise ValueError(f"OD destination {int(used.max())} is not a node index (node_bound {nb})")
+    data = np.zeros((2, K, nb), np.float64)
+    ns._progress = len(node_indices)
+    res = BetweennessShortestResult(dists, ns.node_keys_py(), node_indices, data)
+    if not len(proc):
+        return res
+    csr = _primal_csr(ns)
+    dev = csr.device
+    ptr_t = torch.from_numpy(ptr.astype(np.int32)).to(dev)
+    dst_t = torch.from_numpy(np.clip(dst, 0, nb).astype(np.int32)).to(dev)
+    w_t = torch.from_numpy(w).to(dev)
+    proc_t = torch.from_numpy(proc).to(dev)
+    dummy_w = torch.zeros(1, dtype=torch.float32, device=dev)
+    dummy_e = torch.zeros(1, dtype=torch.uint8, device=dev)
+    g = csr.struct(speed)
+    lib = _native.load()
+    for lo, hi in _groups(K):
+        k = hi - lo
+        ws = _workspace(ns, csr, 0, k, speed, max(secs[lo:hi]))
+        out = torch.zeros((2, k, nb), dtype=torch.float64, device=dev)
+        q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, tol, False, True, False, proc_t, dummy_w,
+                        dummy_e)
+        o = _native.Outputs(out.data_ptr(), 0)
+        rc = lib.cs_betweenness_od_shortest(C.byref(g), C.byref(q), ptr_t.data_ptr(), dst_t.data_ptr(),
+                                            w_t.data_ptr(), C.byref(ws.plan), ws.ptr, ws.nbytes, o, _stream_ptr())
+        if rc != _native.CS_OK:
+            ws.init(_stream_ptr())
+        _native.check(rc, "cs_betweenness_od_shortest")
+        data[:, lo:hi] = out.cpu().numpy()
     return res
 
 

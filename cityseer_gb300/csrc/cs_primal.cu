@@ -96,7 +96,8 @@ __host__ __device__ inline SlotPtrs slot_ptrs(char *dense, size_t dense_stride, 
     return s;
 }
 
-enum Mode { MODE_SHORTEST = 0, MODE_SEGMENT = 1, MODE_TREE = 2, MODE_BOTH = 3 };  // BOTH: batched jobs only
+// BOTH: batched jobs only.  OD: betweenness seeded by an origin-destination matrix.
+enum Mode { MODE_SHORTEST = 0, MODE_SEGMENT = 1, MODE_TREE = 2, MODE_BOTH = 3, MODE_OD = 4 };
 
 struct PrimalParams {
     cs_primal_graph g;
@@ -130,6 +131,9 @@ struct PrimalParams {
     int32_t row_cap;
     int32_t *t_count, *t_node, *t_pred;
     float *t_agg;
+    // MODE_OD: per origin node, its row [od_ptr[o], od_ptr[o+1]) of destinations (ascending) and weights
+    const int32_t *od_ptr, *od_dst;
+    const float *od_w;
 };
 
 // ------------------------------------------------------------------------------------------
@@ -488,7 +492,22 @@ __device__ __forceinline__ void phase_barrier() {
 // With SYNC, every warp of the block runs each phase together (a block barrier ends each phase,
 // and a warp without a source runs the phases with R = 0), so at any time a block's warps fetch one
 // phase's code; there is no early return in that form.
-template <int PM, int SYNC>
+// Trip weight of the pair (src, v) in the origin-destination rows, 0 when the pair has none.
+__device__ __forceinline__ float od_weight(const PrimalParams &p, int src, int v) {
+    int lo = __ldg(&p.od_ptr[src]);
+    const int end = __ldg(&p.od_ptr[src + 1]);
+    int hi = end;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&p.od_dst[mid]) < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < end && __ldg(&p.od_dst[lo]) == v) ? __ldg(&p.od_w[lo]) : 0.0f;
+}
+
+// OD: betweenness only, seeded per pair by the origin-destination weights instead of the 0.5 / 1.0
+// pair counts (rust/src/centrality.rs:2495-2507), source weight 1, written to rows 0 and 1.
+template <int PM, int SYNC, bool OD = false>
 CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R, long long *ph,
                                     int *cnt, int *bw_pl, float *bw_fr) {
     const int lane = lane_id();
@@ -497,8 +516,9 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     const int K = p.k;
     const int P = p.P;
     const int N = p.g.n_bound;
-    const float wt = __ldg(&p.src_wt[src]);
-    const float cycles_wt = wt / __ldg(&p.g.node_w_dev[src]);
+    const float wt = OD ? 1.0f : __ldg(&p.src_wt[src]);
+    const float cycles_wt = OD ? 0.0f : wt / __ldg(&p.g.node_w_dev[src]);
+    const bool closeness = !OD && p.closeness;
     // cnt[0..K): nodes whose first qualifying threshold is k; cnt[MAXK..MAXK+K): same for edges
     for (int q = lane; q < 2 * MAXK; q += 32) cnt[q] = 0;
     __syncwarp();
@@ -512,7 +532,7 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
         if (k0v < K) atomicAdd(&cnt[k0v], 1);
         Nb<PM> nb;
         load_nb<PM>(p, s, v, R, nb, bad);
-        if (p.closeness) {
+        if (closeness) {
 #pragma unroll
             for (int j = 0; j < PM; j++) {
                 if (nb.pos[j] < 0 || !__ldg(&p.g.out_cnt_dev[nb.beg + j])) continue;
@@ -541,7 +561,7 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     // --- closeness (rust/src/centrality.rs:1733-1780).  Density, farness and harmonic terms do not
     // depend on the threshold: they go once into the bucket of the first qualifying threshold and a
     // prefix over thresholds after the launch completes them.  Cycles and beta terms are per k.
-    if (p.closeness) {
+    if (closeness) {
         // per-threshold circuit-rank weights, computed by lane 0 into the (now free) edge-count half
         // of the warp's shared counters
         float *rankw = (float *)(cnt + MAXK);
@@ -650,7 +670,9 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
                 const int v = s.ord[i];
                 const float cost = route_cost(s.sd[i], p.speed);
                 const float sw = sig[i];
-                const float pair = __ldg(&p.eligible[v]) ? 0.5f : 1.0f;
+                float pair;
+                if constexpr (OD) pair = od_weight(p, src, v);
+                else pair = __ldg(&p.eligible[v]) ? 0.5f : 1.0f;
                 // predecessor rows and sigma fractions go to this lane's shared-memory column, so
                 // that the push loop below is a plain (not unrolled) loop over the np predecessors
 #pragma unroll
@@ -681,10 +703,11 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
                     if (v == src) continue;
                     const float credit = __fadd_rn(dep, -seed);
                     const float creditb = __fadd_rn(depb, -seedb);
+                    constexpr size_t row_b = OD ? 0 : 5;
                     if (credit > 0.0f)
-                        atomicAdd(p.out + ((size_t)5 * K + k) * N + v, unit_wt ? f2d(credit) : f2d(credit) * wtd);
+                        atomicAdd(p.out + (row_b * K + k) * N + v, unit_wt ? f2d(credit) : f2d(credit) * wtd);
                     if (creditb > 0.0f)
-                        atomicAdd(p.out + ((size_t)6 * K + k) * N + v, unit_wt ? f2d(creditb) : f2d(creditb) * wtd);
+                        atomicAdd(p.out + ((row_b + 1) * K + k) * N + v, unit_wt ? f2d(creditb) : f2d(creditb) * wtd);
                 }
                 mine = true;
             }
@@ -1013,6 +1036,8 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
         segment_accumulate<PM>(p, s, src, R);
     } else if constexpr (MODE == MODE_TREE) {
         tree_rows<PM>(p, s, li, R);
+    } else if constexpr (MODE == MODE_OD) {
+        shortest_accumulate<PM, 0, true>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
     } else {
         if (p.mode == MODE_SHORTEST) shortest_accumulate<PM, 0>(p, s, src, R, ph, cnt, bw_pl, bw_fr);
         else if (p.mode == MODE_SEGMENT) segment_accumulate<PM>(p, s, src, R);
@@ -1510,7 +1535,8 @@ cs_status retry_chain(const cs::PrimalParams &p, const cs_plan *plan, const Layo
 }
 
 int lanes_for(int mode, int k) {
-    return (mode == cs::MODE_SHORTEST || mode == cs::MODE_BOTH) ? 2 * k : (mode == cs::MODE_SEGMENT ? k : 1);
+    return (mode == cs::MODE_SHORTEST || mode == cs::MODE_BOTH || mode == cs::MODE_OD) ? 2 * k
+                                                                                      : (mode == cs::MODE_SEGMENT ? k : 1);
 }
 
 cs_status validate_primal(const cs_primal_graph *g) {
@@ -1572,6 +1598,7 @@ cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, c
     const int minb = resolve_variant(plan);
     if (p.mode == cs::MODE_SHORTEST) launch_primal_mode<cs::MODE_SHORTEST>(p, p.P, minb, blocks, stream);
     else if (p.mode == cs::MODE_SEGMENT) launch_primal_mode<cs::MODE_SEGMENT>(p, p.P, minb, blocks, stream);
+    else if (p.mode == cs::MODE_OD) launch_primal_mode<cs::MODE_OD>(p, p.P, minb, blocks, stream);
     else launch_primal_mode<cs::MODE_TREE>(p, p.P, minb, blocks, stream);
     g_counters[3]++;
     cudaError_t e = cudaGetLastError();
@@ -1627,7 +1654,8 @@ cs_status reset_dense(char *dense, size_t stride, int n_bound, int n_slots, cuda
 cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan, void *ws, size_t ws_bytes,
                      cs_outputs out, void *stream_v, int mode, int32_t row_cap, int32_t *t_count, int32_t *t_node,
                      float *t_agg, int32_t *t_pred, const int32_t *tree_src, int32_t n_tree, uint32_t tree_maxsec,
-                     float tree_speed, bool poll = false) {
+                     float tree_speed, bool poll = false, const int32_t *od_ptr = nullptr,
+                     const int32_t *od_dst = nullptr, const float *od_w = nullptr) {
     cs_status st = validate_primal(g);
     if (st != CS_OK) return st;
     if (!plan || !ws) return fail(CS_ERR_ARG, "plan/workspace is NULL");
@@ -1669,6 +1697,16 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
         p.n_src = q->n_sources;
         p.src_wt = q->src_wt_dev;
         p.eligible = q->eligible_dev;
+        if (mode == cs::MODE_OD) {
+            if (p.n_src > 0 && (!od_ptr || !od_dst || !od_w))
+                return fail(CS_ERR_ARG, "origin-destination rows are NULL");
+            p.closeness = 0;
+            p.betweenness = 1;
+            p.track_reach = 0;
+            p.od_ptr = od_ptr;
+            p.od_dst = od_dst;
+            p.od_w = od_w;
+        }
         if (p.track_reach && !out.reach_dev) return fail(CS_ERR_ARG, "reach_dev required when track_reach");
         if (!out.out_dev) return fail(CS_ERR_ARG, "out_dev is NULL");
     }
@@ -1828,6 +1866,13 @@ cs_status cs_centrality_shortest(const cs_primal_graph *g, const cs_query *q, co
                                  void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream) {
     return run_primal(g, q, plan, workspace_dev, workspace_bytes, out, stream, cs::MODE_SHORTEST, 0, nullptr, nullptr,
                       nullptr, nullptr, nullptr, 0, 0, 0.0f, true);
+}
+
+cs_status cs_betweenness_od_shortest(const cs_primal_graph *g, const cs_query *q, const int32_t *od_ptr_dev,
+                                     const int32_t *od_dst_dev, const float *od_w_dev, const cs_plan *plan,
+                                     void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream) {
+    return run_primal(g, q, plan, workspace_dev, workspace_bytes, out, stream, cs::MODE_OD, 0, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, 0, 0, 0.0f, true, od_ptr_dev, od_dst_dev, od_w_dev);
 }
 
 cs_status cs_segment_centrality(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan,

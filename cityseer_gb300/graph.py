@@ -614,6 +614,14 @@ class NetworkStructure:
             compute_betweenness=compute_betweenness, min_threshold_wt=min_threshold_wt, speed_m_s=speed_m_s,
             pbar_disabled=pbar_disabled)
 
+    def betweenness_od_shortest(self, od_matrix, distances=None, betas=None, minutes=None, min_threshold_wt=None,
+                                speed_m_s=None, tolerance=None, pbar_disabled=None):
+        from . import centrality
+
+        return centrality.betweenness_od_shortest(
+            self, od_matrix, distances=distances, betas=betas, minutes=minutes, min_threshold_wt=min_threshold_wt,
+            speed_m_s=speed_m_s, tolerance=tolerance, pbar_disabled=pbar_disabled)
+
     # aliases under the names of earlier cityseer releases
     def local_node_centrality_shortest(self, *args, **kwargs):
         return self.centrality_shortest(*args, **kwargs)

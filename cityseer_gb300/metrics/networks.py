@@ -171,3 +171,66 @@ def closeness_simplest(network_structure, nodes_gdf, **kw):
 def betweenness_simplest(network_structure, nodes_gdf, **kw):
     return node_centrality_simplest(network_structure, nodes_gdf, compute_closeness=False, compute_betweenness=True,
                                     **kw)
+
+
+def build_od_matrix(od_df, zones_gdf, network_structure, origin_col, destination_col, weight_col,
+                    zone_id_col=None, max_snap_dist=500.0):
+    """OdMatrix from OD flows and zones (pysrc/cityseer/metrics/networks.py:278-380): each zone's
+    centroid snaps to the nearest network node (scipy KDTree); zones farther than max_snap_dist are
+    left out, as are rows with a missing or non-positive weight or an unknown zone.  `zones_gdf` is a
+    GeoDataFrame (polygon or point geometry, projected CRS) or, without geopandas, a dict with
+    "x"/"y" centroid columns and the zone ids in `zone_id_col` (else "index").  `od_df` is anything
+    indexable by column name (DataFrame or dict of columns).  Reprojection from EPSG:4326 is not
+    restated: pass zones in the network's projected CRS."""
+    from scipy.spatial import KDTree
+
+    from ..centrality import OdMatrix
+
+    if hasattr(zones_gdf, "geometry"):
+        crs = getattr(zones_gdf, "crs", None)
+        if crs is not None and crs.to_epsg() == 4326:
+            raise ValueError("reproject the zones to the network's projected CRS first")
+        geom_types = set(zones_gdf.geometry.geom_type)
+        cents = zones_gdf.geometry.centroid if geom_types & {"Polygon", "MultiPolygon"} else zones_gdf.geometry
+        coords = np.array([(g.x, g.y) for g in cents], np.float64)
+        zone_ids = zones_gdf[zone_id_col].values if zone_id_col is not None else zones_gdf.index.values
+    else:
+        coords = np.column_stack([np.asarray(zones_gdf["x"], np.float64), np.asarray(zones_gdf["y"], np.float64)])
+        zone_ids = list(zones_gdf[zone_id_col if zone_id_col is not None else "index"])
+    tree = KDTree(np.asarray(network_structure.node_xys, np.float64))
+    snap_d, snap_i = tree.query(coords)
+    zone_to_node = {}
+    n_excluded = 0
+    for i, zid in enumerate(zone_ids):
+        if snap_d[i] > max_snap_dist:
+            n_excluded += 1
+            continue
+        zone_to_node[zid] = int(snap_i[i])
+    if n_excluded:
+        logger.warning(f"{n_excluded} zone centroids exceeded max_snap_dist={max_snap_dist}m and were excluded")
+    origins, dests, weights = [], [], []
+    for o_zone, d_zone, w in zip(list(od_df[origin_col]), list(od_df[destination_col]), list(od_df[weight_col])):
+        if w is None or not np.isfinite(float(w)) or float(w) <= 0:
+            continue
+        if o_zone not in zone_to_node or d_zone not in zone_to_node:
+            continue
+        origins.append(zone_to_node[o_zone])
+        dests.append(zone_to_node[d_zone])
+        weights.append(float(w))
+    logger.info(f"Built OD matrix: {len(origins)} pairs, {sum(weights):.0f} total trips")
+    return OdMatrix(origins, dests, weights)
+
+
+def betweenness_od(network_structure, nodes_gdf, od_matrix, distances=None, betas=None, minutes=None,
+                   min_threshold_wt=MIN_THRESH_WT, speed_m_s=SPEED_M_S, tolerance=None):
+    """OD-weighted shortest-path betweenness (pysrc/cityseer/metrics/networks.py:383-461): columns
+    cc_betweenness_{d} and cc_betweenness_beta_{d}; no closeness."""
+    res = network_structure.betweenness_od_shortest(
+        od_matrix=od_matrix, distances=distances, betas=betas, minutes=minutes, min_threshold_wt=min_threshold_wt,
+        speed_m_s=speed_m_s, tolerance=tolerance)
+    temp = {}
+    for measure, attr in (("betweenness", "node_betweenness"), ("betweenness_beta", "node_betweenness_beta")):
+        rows = getattr(res, attr)
+        for d in res.distances:
+            temp[config.prep_gdf_key(measure, d)] = rows[d]
+    return _write(nodes_gdf, res.node_keys_py, temp)

@@ -17,6 +17,8 @@ centrality = SimpleNamespace(
     CentralityShortestResult=_c.CentralityShortestResult,
     CentralitySimplestResult=_c.CentralitySimplestResult,
     CentralitySegmentResult=_c.CentralitySegmentResult,
+    BetweennessShortestResult=_c.BetweennessShortestResult,
+    OdMatrix=_c.OdMatrix,
 )
 
 __all__ = ["graph", "centrality", "pair_distances_betas_time", "betas_from_distances", "distances_from_betas",

@@ -221,6 +221,17 @@ cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, const cs_quer
 cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, const cs_plan *plan,
                                  void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream);
 
+/* Replaces NetworkStructure.betweenness_od_shortest (rust/src/centrality.rs:2419-2540): shortest-path
+ * betweenness weighted by a sparse origin-destination matrix (OdMatrix, :56-91).  od_ptr_dev
+ * [n_bound + 1] delimits each origin node's row of od_dst_dev (destination nodes, ascending, no
+ * repeats) and od_w_dev (trip weights).  q->sources_dev lists the live origins that have a row; the
+ * query's closeness, sampling and reach fields are ignored (source weight 1, no post-scale).  Plans
+ * from cs_plan_primal (mode 0, same k) serve this call.  out rows: 0 node_betweenness,
+ * 1 node_betweenness_beta ([2][k][n_bound], zeroed by the caller). */
+cs_status cs_betweenness_od_shortest(const cs_primal_graph *g, const cs_query *q, const int32_t *od_ptr_dev,
+                                     const int32_t *od_dst_dev, const float *od_w_dev, const cs_plan *plan,
+                                     void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream);
+
 /* Replaces NetworkStructure.segment_centrality (rust/src/centrality.rs:2134-2407).
  * out rows: 0 segment_density, 1 segment_harmonic, 2 segment_beta, 3 segment_betweenness.
  * q->sources_dev lists the live sources (segment centrality has no sampling). */

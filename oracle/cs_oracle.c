@@ -695,6 +695,11 @@ typedef struct {
     const uint8_t *src_take;   /* per-node: 1 if sample_source_weight returned Some */
     int32_t track_reach;       /* sampling or source-indexed */
     int32_t nthreads;
+    /* betweenness_od_shortest: per origin node o, destinations od_dst[od_ptr[o] .. od_ptr[o+1]) with
+       trip weights od_w (OdMatrix, centrality.rs:56-91, one entry per pair) */
+    const int64_t *od_ptr;
+    const int64_t *od_dst;
+    const float *od_w;
 } og_args;
 
 typedef struct {
@@ -774,6 +779,43 @@ static void run_shortest_source(job_t *J, int64_t src) {
         free(seed); free(seed_b); free(sorted);
     }
 #undef ROW
+    btrav_free(&t);
+}
+
+/* betweenness_od_shortest, one source (centrality.rs:2471-2533): live origins with a row only;
+   out: [2][K][n_bound] (betweenness, betweenness_beta), source weight 1. */
+static void run_od_source(job_t *J, int64_t src) {
+    const og_graph *g = J->g;
+    const og_args *a = J->a;
+    int64_t n = g->d.n_bound;
+    int k = a->k;
+    if (!g->d.live[src]) return;
+    int64_t r0 = a->od_ptr[src], r1 = a->od_ptr[src + 1];
+    if (r1 <= r0) return;
+    uint32_t maxs = 0;
+    for (int i = 0; i < k; i++) if (a->seconds[i] > maxs) maxs = a->seconds[i];
+    btrav t;
+    dijkstra_brandes_shortest(g, src, maxs, a->speed, a->tolerance, &t);
+    int64_t *sorted;
+    int64_t ns = sorted_state_indices(&t, &sorted);
+    double *seed = (double *)calloc(t.n_state > 0 ? t.n_state : 1, sizeof(double));
+    double *seed_b = (double *)calloc(t.n_state > 0 ? t.n_state : 1, sizeof(double));
+    for (int i = 0; i < k; i++) {
+        float thr = (float)a->distances[i];
+        double beta = (double)a->betas[i];
+        memset(seed, 0, sizeof(double) * t.n_state);
+        memset(seed_b, 0, sizeof(double) * t.n_state);
+        for (int64_t r = r0; r < r1; r++) {
+            int64_t dest = a->od_dst[r];
+            if (t.best_route_cost[dest] > thr) continue;
+            double w = (double)a->od_w[r];
+            seed[dest] += w;
+            seed_b[dest] += w * exp(-beta * (double)t.best_route_cost[dest]);
+        }
+        brandes_backprop(&t, sorted, ns, src, seed, seed_b, 0, thr, J->out + (int64_t)i * n,
+                         J->out + ((int64_t)k + i) * n, 1.0, J->atomic);
+    }
+    free(seed); free(seed_b); free(sorted);
     btrav_free(&t);
 }
 
@@ -1117,6 +1159,7 @@ static void *worker(void *arg) {
         int64_t src = J->a->sources[i];
         if (J->mode == 0) run_shortest_source(J, src);
         else if (J->mode == 1) run_simplest_source(J, src);
+        else if (J->mode == 3) run_od_source(J, src);
         else run_segment_source(J, src, visited, tree, vedges, emap);
     }
     free(visited); free(vedges); free(tree); free(emap);
@@ -1154,6 +1197,14 @@ int og_centrality_simplest(const og_graph *g, const og_args *a, double *out, uin
 int og_segment_centrality(const og_graph *g, const og_args *a, double *out) {
     if (a->k <= 0 || a->k > 64) return OG_ERR_ARG;
     job_t J = {g, a, out, NULL, 0, 2, 0};
+    return run_job(&J);
+}
+
+/* out: [2][K][n_bound] (betweenness, betweenness_beta); a->sources = node_indices; every destination
+   index is below n_bound (the caller checks). */
+int og_betweenness_od(const og_graph *g, const og_args *a, double *out) {
+    if (a->k <= 0 || a->k > 64 || !a->od_ptr || !a->od_dst || !a->od_w) return OG_ERR_ARG;
+    job_t J = {g, a, out, NULL, 0, 3, 0};
     return run_job(&J);
 }
 

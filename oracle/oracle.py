@@ -35,6 +35,7 @@ class _Args(C.Structure):
         ("angular_scaling_unit", C.c_float), ("farness_scaling_offset", C.c_float),
         ("n_sources", C.c_int64), ("sources", _P), ("eligible", _P), ("src_wt", _P), ("src_take", _P),
         ("track_reach", C.c_int32), ("nthreads", C.c_int32),
+        ("od_ptr", _P), ("od_dst", _P), ("od_w", _P),
     ]
 
 
@@ -75,6 +76,7 @@ def lib() -> C.CDLL:
             getattr(L, name).argtypes = [_P, C.POINTER(_Args), _P, _P]
         L.og_segment_centrality.restype = C.c_int
         L.og_segment_centrality.argtypes = [_P, C.POINTER(_Args), _P]
+        L.og_betweenness_od.argtypes = [_P, C.POINTER(_Args), _P]
         L.og_tree_shortest.restype = C.c_int64
         L.og_tree_shortest.argtypes = [_P, C.c_int64, C.c_uint32, C.c_float, _P, _P]
         L.og_tree_simplest.restype = C.c_int64
@@ -230,6 +232,30 @@ def centrality_shortest(og: OracleGraph, dists, betas, secs, speed=1.33333, tol=
         raise ValueError("oracle rejected the arguments")
     _post_scale(og, out, (5, 6), plan, betweenness)
     return out, reach
+
+
+def betweenness_od(og: OracleGraph, dists, betas, secs, od_rows, speed=1.33333, tol=1e-4, nthreads=1, ns=None):
+    """betweenness_od_shortest (rust/src/centrality.rs:2419-2540).  od_rows = (ptr [n_bound + 1],
+    dst, w): each origin node's destinations and trip weights, one entry per pair.  Returns
+    [2][K][n_bound] (node_betweenness, node_betweenness_beta)."""
+    plan = all_sources_plan(ns)
+    k = len(dists)
+    ptr = np.ascontiguousarray(od_rows[0], np.int64)
+    dst = np.ascontiguousarray(od_rows[1], np.int64)
+    w = np.ascontiguousarray(od_rows[2], np.float32)
+    if len(dst) and (dst.min() < 0 or dst.max() >= og.nb):
+        raise ValueError("OD destination is not a node index")
+    out = np.zeros((2, k, og.nb), np.float64)
+    a, keep = _args(og.nb, dists, betas, secs, speed, tol, False, True, plan, nthreads)
+    keep["od"] = (ptr, dst, w)
+    a.od_ptr = ptr.ctypes.data
+    a.od_dst = dst.ctypes.data if len(dst) else None
+    a.od_w = w.ctypes.data if len(w) else None
+    if not len(dst):
+        return out
+    if lib().og_betweenness_od(og.h, C.byref(a), out.ctypes.data) != 0:
+        raise ValueError("oracle rejected the arguments")
+    return out
 
 
 def _post_scale(og, out, rows, plan, betweenness):
