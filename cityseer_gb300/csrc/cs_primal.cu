@@ -134,6 +134,7 @@ struct PrimalParams {
     // MODE_OD: per origin node, its row [od_ptr[o], od_ptr[o+1]) of destinations (ascending) and weights
     const int32_t *od_ptr, *od_dst;
     const float *od_w;
+    int32_t radix_sort;  // settle-order sort: 0 distance buckets, 1 LSD radix
 };
 
 // ------------------------------------------------------------------------------------------
@@ -169,7 +170,9 @@ __device__ __forceinline__ void push_entries(bool first, int route, int v, float
 #define CS_PHASE_INLINE
 #endif
 
-CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs &s, int src, long long &relaxed) {
+// dmax: an upper bound of every reached distance (the last band's end, at most the cutoff).
+CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs &s, int src, long long &relaxed,
+                                           float &dmax) {
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
     const int cap = p.cap;
@@ -287,6 +290,7 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
         nfar = nf2;
     }
     __syncwarp();
+    dmax = fminf(T, p.maxsec);
     if (overflow) return -1;  // the slot's dense state is dirty: the caller resets it
     return R;
 }
@@ -294,10 +298,13 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
 // ------------------------------------------------------------------------------------------
 // 2. Warp LSD radix sort of the reached set by distance (cs_sort.cuh): the settle order.
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ void warp_sort(const SlotPtrs &s, int R, uint32_t *hist) {
+// The distance-bucket sort (3 passes) unless p.radix_sort selects the 4-pass LSD radix sort; both
+// give the same order (ascending distance, ties in reached-list order).
+__device__ __forceinline__ void warp_sort(const PrimalParams &p, const SlotPtrs &s, int R, float dmax, uint32_t *hist) {
     const float *dist = s.dist;
-    warp_radix_sort(R, s.rl, [dist](int v) { return (uint32_t)__float_as_int(__ldcg(&dist[v])); }, s.kb, s.vb,
-                    (uint32_t *)s.sd, s.ord, hist);
+    auto key_of = [dist](int v) { return (uint32_t)__float_as_int(__ldcg(&dist[v])); };
+    if (p.radix_sort) warp_radix_sort(R, s.rl, key_of, s.kb, s.vb, (uint32_t *)s.sd, s.ord, hist);
+    else warp_bucket_sort(R, dmax, s.rl, key_of, s.kb, s.vb, (uint32_t *)s.sd, s.ord, hist);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1007,7 +1014,8 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
                                            long long &settled) {
     const int lane = lane_id();
     long long t0 = clock64();
-    const int R = warp_search(p, s, src, relaxed);
+    float dmax = 0.0f;
+    const int R = warp_search(p, s, src, relaxed, dmax);
     phase_mark(ph, 0, t0);
     if (R < 0) {
         // Reach exceeded this slot's capacity: the reached list lost track of touched entries, so
@@ -1025,7 +1033,7 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
         __syncwarp();
         return false;
     }
-    warp_sort(s, R, hist);
+    warp_sort(p, s, R, dmax, hist);
     __syncwarp();
     for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
     __syncwarp();
@@ -1154,7 +1162,8 @@ __global__ void __launch_bounds__(WPB * 32, MINB) primal_sync_kernel(const Prima
         const int src = mine ? p.src_list[li] : 0;
         long long t0 = clock64();
         int R = 0;
-        if (mine) R = warp_search(p, s, src, relaxed);
+        float dmax = 0.0f;
+        if (mine) R = warp_search(p, s, src, relaxed, dmax);
         phase_mark(ph, 0, t0);
         phase_barrier<GW>();
         const bool ok = mine && R >= 0;
@@ -1170,7 +1179,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB) primal_sync_kernel(const Prima
             }
         }
         if (ok) {
-            warp_sort(s, R, hist_all[wib]);
+            warp_sort(p, s, R, dmax, hist_all[wib]);
             __syncwarp();
             for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
         }
@@ -1338,7 +1347,8 @@ __global__ void __launch_bounds__(256, MINB) batch_sync_kernel(const PrimalParam
         }
         long long t0 = clock64();
         int R = 0;
-        if (mine) R = warp_search(p, s, src, relaxed);
+        float dmax = 0.0f;
+        if (mine) R = warp_search(p, s, src, relaxed, dmax);
         phase_mark(ph, 0, t0);
         __syncthreads();
         const bool ok = mine && R >= 0;
@@ -1354,7 +1364,7 @@ __global__ void __launch_bounds__(256, MINB) batch_sync_kernel(const PrimalParam
             }
         }
         if (ok) {
-            warp_sort(s, R, hist_all[wib]);
+            warp_sort(p, s, R, dmax, hist_all[wib]);
             __syncwarp();
             for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
         }
@@ -1571,6 +1581,12 @@ bool phase_sync() {
     return !(e && e[0] == '0');
 }
 
+// Settle-order sort: distance buckets by default, CS_SORT=radix selects the LSD radix sort.
+int radix_sort_choice() {
+    const char *e = getenv("CS_SORT");
+    return (e && strcmp(e, "radix") == 0) ? 1 : 0;
+}
+
 template <int MODE>
 void launch_primal_mode(const cs::PrimalParams &p, int P, int minb, int blocks, cudaStream_t stream) {
     if (MODE == cs::MODE_SHORTEST && P <= 8 && phase_sync()) {
@@ -1672,6 +1688,7 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     char *base = (char *)ws;
     cs::PrimalParams p;
     memset(&p, 0, sizeof(p));
+    p.radix_sort = radix_sort_choice();
     p.g = *g;
     p.k = K;
     uint32_t maxs = 0;
@@ -2070,6 +2087,7 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
     char *base = (char *)ws;
     cs::PrimalParams p;
     memset(&p, 0, sizeof(p));
+    p.radix_sort = radix_sort_choice();
     p.g.n_bound = geo_n;  // slot geometry only; each job brings its own graph
     p.hdr = (cs::WsHeader *)(base + lay.hdr_off);
     p.failed = (int32_t *)(base + lay.failed_off);
