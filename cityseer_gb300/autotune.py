@@ -65,7 +65,7 @@ def key_of(csr, mode: str, secs, k: int) -> str:
 
 
 def default(csr, speed: float) -> dict:
-    return {"delta": 2.0 * csr.median_edge_seconds(speed), "variant": 4, "tuned": False}
+    return {"delta": 2.0 * csr.median_edge_seconds(speed), "variant": 3, "tuned": False}
 
 
 def lookup(ns, csr, mode: str, d, s, speed: float) -> dict:

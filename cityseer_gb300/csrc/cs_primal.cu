@@ -529,35 +529,77 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     // cnt[0..K): nodes whose first qualifying threshold is k; cnt[MAXK..MAXK+K): same for edges
     for (int q = lane; q < 2 * MAXK; q += 32) cnt[q] = 0;
     __syncwarp();
-    // --- one pass over out-edges: circuit-rank counts and predecessor replay
+    // --- one pass over out-edges in settle order, 32 nodes at a time: circuit-rank counts, the
+    // predecessor replay and, with betweenness, sigma (f32 path counts) of the chunk: a node is ready
+    // once its in-chunk predecessors are done.  The same pass zeroes each node's dependency lanes
+    // for the backward sweep.
     bool bad = false;
-    for (int i = lane; i < R; i += 32) {
-        const int v = s.ord[i];
-        const float dv = s.sd[i];
-        const float cv = route_cost(dv, p.speed);
-        const int k0v = first_k(p, cv);
-        if (k0v < K) atomicAdd(&cnt[k0v], 1);
+    float *sig = (float *)s.sig;
+    const int L = p.L;  // 2K floats per node: [0,K) plain, [K,2K) beta-weighted
+    float *dl = (float *)s.dl;
+    for (int base = 0; base < R; base += 32) {
+        const int i = base + lane;
+        const bool act = i < R;
+        unsigned pm = 0u;
         Nb<PM> nb;
-        load_nb<PM>(p, s, v, R, nb, bad);
-        if (closeness) {
+        if (act) {
+            const int v = s.ord[i];
+            const float dv = s.sd[i];
+            const float cv = route_cost(dv, p.speed);
+            const int k0v = first_k(p, cv);
+            if (k0v < K) atomicAdd(&cnt[k0v], 1);
+            load_nb<PM>(p, s, v, R, nb, bad);
+            if (closeness) {
 #pragma unroll
-            for (int j = 0; j < PM; j++) {
-                if (nb.pos[j] < 0 || !__ldg(&p.g.out_cnt_dev[nb.beg + j])) continue;
-                const float ec = fmaxf(cv, route_cost(nb.d[j], p.speed));
-                const int k0e = first_k(p, ec);
-                if (k0e < K) atomicAdd(&cnt[MAXK + k0e], 1);
+                for (int j = 0; j < PM; j++) {
+                    if (nb.pos[j] < 0 || !__ldg(&p.g.out_cnt_dev[nb.beg + j])) continue;
+                    const float ec = fmaxf(cv, route_cost(nb.d[j], p.speed));
+                    const int k0e = first_k(p, ec);
+                    if (k0e < K) atomicAdd(&cnt[MAXK + k0e], 1);
+                }
+            }
+            if (p.betweenness) {
+                if (i == 0) {
+                    s.np[0] = 0;
+                } else {
+                    bool ok = true;
+                    pm = replay_brandes<PM>(p, nb, i, dv, ok);
+                    if (!ok) { bad = true; pm = 0u; }
+                    int r = 0;
+#pragma unroll
+                    for (int j = 0; j < PM; j++)
+                        if ((pm >> j) & 1u) s.pr[(size_t)i * P + r++] = nb.pos[j];
+                    s.np[i] = (uint8_t)r;
+                }
             }
         }
-        if (!p.betweenness) continue;
-        if (i == 0) { s.np[0] = 0; continue; }
-        bool ok = true;
-        const unsigned pm = replay_brandes<PM>(p, nb, i, dv, ok);
-        if (!ok) { bad = true; s.np[i] = 0; continue; }
-        int r = 0;
+        if (!p.betweenness || failed) continue;  // uniform across the warp
+        unsigned blk = 0u;  // in-chunk predecessors, as lane bits
 #pragma unroll
         for (int j = 0; j < PM; j++)
-            if ((pm >> j) & 1u) s.pr[(size_t)i * P + r++] = nb.pos[j];
-        s.np[i] = (uint8_t)r;
+            if (((pm >> j) & 1u) && nb.pos[j] >= base) blk |= 1u << (nb.pos[j] - base);
+        unsigned done = __ballot_sync(FULL, !act);
+        bool mine = !act;
+        int guard = 0;
+        while (done != FULL) {
+            const bool ready = !mine && ((blk & ~done) == 0u);
+            if (ready) {
+                float sg = (i == 0) ? 1.0f : 0.0f;
+#pragma unroll
+                for (int j = 0; j < PM; j++)
+                    if ((pm >> j) & 1u) sg = fadd(sg, sig[nb.pos[j]]);
+                sig[i] = sg;
+                for (int q = 0; q < 2 * K; q++) dl[(size_t)i * L + q] = 0.0f;
+                mine = true;
+            }
+            __syncwarp();
+            done |= __ballot_sync(FULL, ready);
+            if (++guard > 64) break;
+        }
+        if (done != FULL) {
+            if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 2);
+            failed = true;
+        }
     }
     if (__any_sync(FULL, bad)) {
         if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 1);
@@ -610,49 +652,11 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     // in the block-synchronous form the flag can differ between a block's warps (batched jobs):
     // a warp without betweenness runs the remaining phases empty, so every warp meets the barriers
     const int Rb = (SYNC != 0 && !p.betweenness) ? 0 : R;
-    // --- sigma (f32 path counts) in settle order, chunked: ready once in-chunk preds are done
-    float *sig = (float *)s.sig;
-    for (int base = 0; base < Rb; base += 32) {
-        const int i = base + lane;
-        const bool act = i < Rb;
-        int pl[PM];
-        const int np = act ? load_preds<PM>(s, i, P, pl) : 0;
-        unsigned pm = 0;
-#pragma unroll
-        for (int r = 0; r < PM; r++)
-            if (r < np && pl[r] >= base) pm |= 1u << (pl[r] - base);
-        unsigned done = __ballot_sync(FULL, !act);
-        bool mine = !act;
-        int guard = 0;
-        while (done != FULL) {
-            const bool ready = !mine && ((pm & ~done) == 0u);
-            if (ready) {
-                float sg = (i == 0) ? 1.0f : 0.0f;
-#pragma unroll
-                for (int r = 0; r < PM; r++)
-                    if (r < np) sg = fadd(sg, sig[pl[r]]);
-                sig[i] = sg;
-                mine = true;
-            }
-            __syncwarp();
-            done |= __ballot_sync(FULL, ready);
-            if (++guard > 64) break;
-        }
-        if (done != FULL) {
-            if (lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 2);
-            failed = true;
-            break;
-        }
-    }
-    phase_barrier<SYNC>();
+    // (sigma was built in the replay pass)
     phase_mark(ph, 4, tph);
     // --- backward Brandes sweep, all K thresholds in one pass (rust/src/centrality.rs:823-873,
     // 1782-1835).  Dependencies accumulate in f32: for sources whose paths are unique (sigma == 1)
     // they are half-integers and exact; otherwise they carry f32 rounding (well inside 1e-5).
-    const int L = p.L;  // 2K floats per node: [0,K) plain, [K,2K) beta-weighted
-    float *dl = (float *)s.dl;
-    for (int i = lane; i < Rb; i += 32)
-        for (int q = 0; q < 2 * K; q++) dl[(size_t)i * L + q] = 0.0f;
     __syncwarp();
     const bool unit_wt = (wt == 1.0f);
     const double wtd = (double)wt;
@@ -1564,7 +1568,7 @@ cs_status validate_primal(const cs_primal_graph *g) {
 int resolve_variant(const cs_plan *plan) {
     if (plan && plan->variant >= 2 && plan->variant <= 4) return plan->variant;
     const char *e = getenv("CS_MIN_BLOCKS_PER_SM");
-    return (e && e[0] >= '2' && e[0] <= '4') ? e[0] - '0' : 4;
+    return (e && e[0] >= '2' && e[0] <= '4') ? e[0] - '0' : 3;
 }
 
 cudaError_t occupancy_blocks(int P, int variant, int *bpsm) {

@@ -103,7 +103,7 @@ typedef struct {
     int32_t blocks;
     float delta_seconds;  /* band width of the label-correcting search; <= 0 picks a default */
     int32_t lanes;        /* accumulator lanes per reached node */
-    int32_t variant;      /* register budget: 4 (default), 3 or 2 resident 256-thread blocks per SM */
+    int32_t variant;      /* register budget: 3 (default), 4 or 2 resident 256-thread blocks per SM */
     int32_t max_degree;   /* batches: largest out-degree over the jobs */
     int32_t n_bound;      /* node bound the slot geometry was sized for (set by the planners) */
     size_t workspace_bytes;
