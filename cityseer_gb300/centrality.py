@@ -2,7 +2,7 @@
 
 Host logic mirrored here, kernels in libcsgpu.so:
   validate_tolerance          rust/src/centrality.rs:34-48
-  prepare_source_sampling     rust/src/centrality.rs:1032-1104
+  prepare_source_sampling     rust/src/centrality.rs:1032-1104 (random stream: stdrng.StdRng)
   sample_source_weight        rust/src/centrality.rs:1107-1139
   scale_metric_results        rust/src/centrality.rs:875-893 (betweenness post-scale)
   result getters              rust/src/centrality.rs:152-355, MetricResult.load_compact common.rs:37-53
@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -18,6 +19,7 @@ import torch
 
 from . import _native, device
 from .common import WALKING_SPEED, pair_distances_betas_time
+from .stdrng import StdRng
 from .graph import NodeVisit
 
 TIE_EPSILON = np.float32(1e-4)
@@ -172,10 +174,10 @@ def prepare_source_sampling(ns, sample_probability, sampling_weights, random_see
         eligible[node_indices[live[node_indices]]] = 1
     randoms = None
     if prob is not None and not is_indexed:
-        # The reference draws from rand's StdRng (ChaCha12); this stream differs, so sampled runs
-        # agree with it in distribution, not source by source.
-        rng = np.random.default_rng(random_seed)
-        randoms = rng.random(nb, dtype=np.float32)
+        # one f32 per node index from rand's StdRng (rust/src/centrality.rs:1082-1091): a seeded
+        # run samples the same sources as the reference; unseeded, the seed comes from the OS
+        rng = StdRng.seed_from_u64(int(random_seed)) if random_seed is not None else StdRng(os.urandom(32))
+        randoms = rng.random_f32(nb)
     src_wt = np.zeros(nb, np.float32)
     take = np.zeros(len(sources), bool)
     count = 0
