@@ -127,6 +127,91 @@ class EdgeVisit:
         self.edge_idx = None
 
 
+class NodePayload:
+    """Node payload as rustalgos.graph.NodePayload exposes it (rust/src/graph.rs:24-88)."""
+
+    __slots__ = ("node_key", "x", "y", "z", "live", "weight", "is_transport")
+
+    def __init__(self, node_key, x, y, z, live, weight, is_transport):
+        self.node_key, self.x, self.y, self.z = node_key, x, y, z
+        self.live, self.weight, self.is_transport = live, weight, is_transport
+
+    @property
+    def coord(self) -> tuple[float, float]:
+        return (self.x, self.y)
+
+    @property
+    def coord_z(self) -> tuple[float, float, float | None]:
+        return (self.x, self.y, self.z)
+
+
+class EdgePayload:
+    """Edge payload as rustalgos.graph.EdgePayload exposes it (rust/src/graph.rs:90-115).  This
+    store keeps no geometry, so geom_wkt is None."""
+
+    __slots__ = ("start_nd_key_py", "end_nd_key_py", "edge_idx", "length", "angle_sum", "imp_factor",
+                 "in_bearing", "out_bearing", "seconds", "geom_wkt", "is_transport")
+
+    def __init__(self, **kw):
+        for k in self.__slots__:
+            setattr(self, k, kw.get(k))
+
+
+def _leaving_direction(coords, at_start: bool) -> tuple[float, float] | None:
+    """Direction in which a polyline leaves its start (or, reversed, its end): the first vertex
+    that differs from the end point, minus the end point."""
+    pts = coords if at_start else coords[::-1]
+    x0, y0 = pts[0][0], pts[0][1]
+    for q in pts[1:]:
+        if q[0] != x0 or q[1] != y0:
+            return (q[0] - x0, q[1] - y0)
+    return None
+
+
+def _recover_shared_keys(edges, coords_of_edge, node_xy) -> list[str]:
+    """Shared primal node of each dual edge, up to naming, from the edge geometries.
+
+    A dual edge runs from one dual node's midpoint through the primal node the two primal edges
+    share to the other's midpoint; at a dual node, edges towards the same primal endpoint leave
+    along the same half of its primal edge (same direction) and edges towards the other endpoint
+    leave the opposite way.  Each (dual node, side) is a port, each edge joins the ports of its two
+    ends, and the connected ports are one primal node.  Only equality of the keys matters to the
+    endpoint slots (rust/src/centrality.rs:533-566), so the component id serves as the key."""
+    n_e = len(edges)
+    ref_dir: dict[int, tuple[float, float]] = {}
+    port = [[0, 0] for _ in range(n_e)]
+    for j, (s, e, _k) in enumerate(edges):
+        c = coords_of_edge(j)
+        sx, sy = node_xy(s)
+        fwd = (c[0][0] - sx) ** 2 + (c[0][1] - sy) ** 2 <= (c[-1][0] - sx) ** 2 + (c[-1][1] - sy) ** 2
+        for end, node in enumerate((s, e)):
+            at_start = fwd if end == 0 else not fwd
+            d = _leaving_direction(c, at_start)
+            if d is None:
+                raise ValueError(f"dual edge {s} -> {e} has no length: its shared primal node is undefined")
+            r = ref_dir.setdefault(node, d)
+            port[j][end] = 0 if d[0] * r[0] + d[1] * r[1] > 0.0 else 1
+    parent: dict[tuple[int, int], tuple[int, int]] = {}
+
+    def find(a):
+        parent.setdefault(a, a)
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+
+    for j, (s, e, _k) in enumerate(edges):
+        ra, rb = find((s, port[j][0])), find((e, port[j][1]))
+        if ra != rb:
+            parent[rb] = ra
+    ids: dict[tuple[int, int], int] = {}
+    out = []
+    for j, (s, _e, _k) in enumerate(edges):
+        r = find((s, port[j][0]))
+        out.append(f"shared-{ids.setdefault(r, len(ids))}")
+    return out
+
+
 class NetworkStructure:
     """Graph store with the reference's builder API; centralities run on the GPU."""
 
@@ -247,6 +332,75 @@ class NetworkStructure:
     def set_is_dual(self, is_dual: bool) -> None:
         self._is_dual = bool(is_dual)
         self._touch()
+
+    @classmethod
+    def from_reference(cls, ref) -> "NetworkStructure":
+        """Imports a `cityseer.rustalgos.graph.NetworkStructure` (rust/src/graph.rs:381-1341) through
+        its public getters.  Nodes keep their indices (gaps after removals included); edges are added
+        in `edge_references()` order with their stored payloads (length, angle sum, impedance,
+        bearings, seconds), so nothing is recomputed.  A dual graph's shared primal node per edge is
+        not a public field: it is recovered from the edge geometries (`geom_wkt`), see
+        `_recover_shared_keys`.  Transport nodes and edges are not imported (transport linking is
+        outside this package).  Where edges were removed and others added later, the reference's
+        adjacency order can differ from edge-reference order, and so can heap ties."""
+        ns = cls()
+        dual = ref.is_dual() if callable(getattr(ref, "is_dual", None)) else bool(ref.is_dual)
+        ns.set_is_dual(bool(dual))
+        present = [int(i) for i in ref.node_indices()]
+        nb = (max(present) + 1) if present else 0
+        have = set(present)
+        gaps = []
+        xy: dict[int, tuple[float, float]] = {}
+        for i in range(nb):
+            if i not in have:
+                ns._add_node(None, 0.0, 0.0, None, False, np.float32(0.0), False)
+                gaps.append(i)
+                continue
+            p = ref.get_node_payload_py(i)
+            if p.is_transport:
+                raise NotImplementedError("transport nodes are not imported")
+            x, y, z = p.coord_z
+            xy[i] = (float(x), float(y))
+            ns._add_node(p.node_key, x, y, z, bool(p.live), np.float32(p.weight), False)
+        edges = [tuple(int(v) for v in er) for er in ref.edge_references()]
+        pls = [ref.get_edge_payload_py(s, e, k) for s, e, k in edges]
+        shared = [None] * len(edges)
+        if dual and edges:
+            if any(pl.geom_wkt is None for pl in pls):
+                raise ValueError("dual edges need geom_wkt to recover their shared primal nodes")
+            shared = _recover_shared_keys(edges, lambda j: parse_linestring_wkt(pls[j].geom_wkt), xy.__getitem__)
+        for (s, e, k), pl, sh in zip(edges, pls, shared):
+            if pl.is_transport:
+                raise NotImplementedError("transport edges are not imported")
+            ns._add_edge(s, e, k, np.float32(pl.length), np.float32(pl.angle_sum), np.float32(pl.imp_factor),
+                         np.float32(np.nan if pl.seconds is None else pl.seconds), np.float32(pl.in_bearing),
+                         np.float32(pl.out_bearing), sh, (pl.start_nd_key_py, pl.end_nd_key_py), False)
+        for i in gaps:
+            ns._exists.view()[i] = 0
+        ns._touch()
+        ns.validate()
+        return ns
+
+    def get_node_payload_py(self, node_idx: int) -> NodePayload:
+        self._node_checked(node_idx)
+        z = None if not self._has_z.view()[node_idx] else float(self._z.view()[node_idx])
+        return NodePayload(self._keys[node_idx] if self._keys is not None else node_idx,
+                           float(self._x.view()[node_idx]), float(self._y.view()[node_idx]), z,
+                           bool(self._live.view()[node_idx]), float(self._weight.view()[node_idx]),
+                           bool(self._transport.view()[node_idx]))
+
+    def get_edge_payload_py(self, start_nd_idx: int, end_nd_idx: int, edge_idx: int) -> EdgePayload:
+        self._require_node(start_nd_idx, "start_nd_idx")
+        self._require_node(end_nd_idx, "end_nd_idx")
+        e = self._find_edge(start_nd_idx, end_nd_idx, edge_idx)
+        if e < 0:
+            raise ValueError("Edge not found")
+        keys = self._e_keys[e] if self._e_keys is not None and self._e_keys[e] is not None else (None, None)
+        return EdgePayload(start_nd_key_py=keys[0], end_nd_key_py=keys[1], edge_idx=int(self._e_idx.view()[e]),
+                           length=float(self._e_len.view()[e]), angle_sum=float(self._e_ang.view()[e]),
+                           imp_factor=float(self._e_imp.view()[e]), in_bearing=float(self._e_inb.view()[e]),
+                           out_bearing=float(self._e_outb.view()[e]), seconds=float(self._e_sec.view()[e]),
+                           geom_wkt=None, is_transport=bool(self._e_transport.view()[e]))
 
     # ------------------------------------------------------------------ builders
     def add_street_node(self, node_key: Any, x: float, y: float, live: bool, weight: float, z: float | None = None) -> int:
