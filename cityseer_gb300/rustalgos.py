@@ -12,7 +12,8 @@ from .common import (
     seconds_from_distances,
 )
 
-graph = SimpleNamespace(NetworkStructure=_g.NetworkStructure, NodeVisit=_g.NodeVisit, EdgeVisit=_g.EdgeVisit)
+graph = SimpleNamespace(NetworkStructure=_g.NetworkStructure, NodeVisit=_g.NodeVisit, EdgeVisit=_g.EdgeVisit,
+                        NodePayload=_g.NodePayload, EdgePayload=_g.EdgePayload)
 centrality = SimpleNamespace(
     CentralityShortestResult=_c.CentralityShortestResult,
     CentralitySimplestResult=_c.CentralitySimplestResult,
