@@ -140,10 +140,14 @@ def cpu_baseline(ns, dists, n_total: int, target_seconds: float, nthreads: int |
         oracle.centrality_shortest(og, d, b, s, plan=pl, nthreads=nthreads)
         return time.perf_counter() - t0
 
-    probe = max(nthreads * 2, 32)
+    probe = max(nthreads * 8, 128)
+    run(probe)  # first call pays one-time costs (library load, first touch of the output rows)
     tp = run(probe)
     count = int(min(n_total, max(probe, probe * target_seconds / max(tp, 1e-6))))
     t = run(count)
+    if t < 0.5 * target_seconds and count < n_total:  # the probe overestimated the per-source cost
+        count = int(min(n_total, count * target_seconds / max(t, 1e-6)))
+        t = run(count)
     return {
         "value": count / t,
         "unit": UNIT,
