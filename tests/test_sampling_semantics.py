@@ -106,3 +106,36 @@ def test_betweenness_sampling_converges(primal):
     full = _rows(primal, closeness=False, betweenness=True)[5]
     avg = np.mean([_rows(primal, 0.5, seed, closeness=False, betweenness=True)[5] for seed in range(20)], axis=0)
     assert _rel_err(avg, full) < 0.25
+
+
+def test_hoeffding_model():
+    """The reach -> p model (pysrc/cityseer/sampling.py:32-104; tests/test_sampling.py:414-490)."""
+    import math
+
+    from cityseer_gb300 import sampling
+
+    assert (sampling.HOEFFDING_EPSILON, sampling.HOEFFDING_DELTA) == (0.06, 0.1)
+    k = math.log(2 * 1000.0 / 0.1) / (2 * 0.1 ** 2)
+    assert sampling.compute_hoeffding_p(1000.0, epsilon=0.1, delta=0.1) == pytest.approx(min(1.0, k / 1000.0))
+    ps = [sampling.compute_hoeffding_p(r) for r in (200.0, 500.0, 1000.0, 5000.0, 10000.0)]
+    assert all(a >= b for a, b in zip(ps, ps[1:]))
+    for bad in (sampling.compute_hoeffding_p(50.0), sampling.compute_hoeffding_p(0), sampling.compute_hoeffding_p(-100),
+                sampling.compute_hoeffding_p(1000.0, delta=0.0), sampling.compute_hoeffding_p(1000.0, delta=1.0)):
+        assert bad == 1.0
+    pd = [sampling.compute_distance_p(d) for d in (500, 1000, 2000, 5000, 10000, 20000)]
+    assert all(a >= b for a, b in zip(pd, pd[1:])) and 0.0 < sampling.compute_distance_p(2000) <= 1.0
+    assert sampling.compute_distance_p(100) == 1.0 and sampling.compute_distance_p(0) == 1.0
+    assert sampling.compute_distance_p(5000, epsilon=0.05) >= sampling.compute_distance_p(5000, epsilon=0.1)
+
+
+def test_tolerance_zero_is_the_default_and_tolerance_moves_betweenness(primal):
+    """tests/test_sampling.py:574-618: tolerance 0 equals the default; a wide tolerance spreads
+    betweenness over near-equal paths."""
+    ns, og = primal
+    d, b, s = pair_distances_betas_time(1.33333, distances=[D])
+    plan = oracle.all_sources_plan(ns)
+    default, _ = oracle.centrality_shortest(og, d, b, s, tol=validate_tolerance(None), plan=plan)
+    zero, _ = oracle.centrality_shortest(og, d, b, s, tol=validate_tolerance(0.0), plan=plan)
+    wide, _ = oracle.centrality_shortest(og, d, b, s, tol=validate_tolerance(10.0), plan=plan)
+    np.testing.assert_array_equal(default, zero)
+    assert not np.allclose(default[5], wide[5])
