@@ -41,6 +41,23 @@ def _interpolate(coords, dist):
     return tuple(coords[-1][:2])
 
 
+def _interpolate_z(coords, dist):
+    """z at `dist` (2D length) along a 3D polyline, linear within the segment, as GEOS interpolates
+    a 3D LineString; None for a 2D polyline."""
+    if not coords or len(coords[0]) < 3 or any(len(c) < 3 for c in coords):
+        return None
+    if dist <= 0:
+        return float(coords[0][2])
+    acc = 0.0
+    for i in range(len(coords) - 1):
+        s = _seg_len(coords[i], coords[i + 1])
+        if acc + s >= dist and s > 0:
+            f = (dist - acc) / s
+            return float(coords[i][2] + (coords[i + 1][2] - coords[i][2]) * f)
+        acc += s
+    return float(coords[-1][2])
+
+
 def substring(coords, start_dist, end_dist):
     """Part of the polyline between two distances from its start (start < end)."""
     sp = _interpolate(coords, start_dist)
@@ -127,6 +144,9 @@ def nx_to_dual(g: nx.MultiGraph) -> nx.MultiGraph:
         key = _dual_key(s, e, k)
         d.add_node(key, x=mid[0], y=mid[1], primal_edge=line, primal_edge_node_a=s, primal_edge_node_b=e,
                    primal_edge_idx=k)
+        mz = _interpolate_z(line, 0.5 * _length(line))
+        if mz is not None:  # the midpoint of a 3D primal edge keeps its z (graphs.py:2099-2100)
+            d.nodes[key]["z"] = mz
         if "live" in g.nodes[s] and "live" in g.nodes[e]:
             d.nodes[key]["live"] = bool(g.nodes[s]["live"]) or bool(g.nodes[e]["live"])
     for s, e, k in g.edges(keys=True):
