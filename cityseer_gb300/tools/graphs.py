@@ -3,6 +3,7 @@
 Edge geometries are sequences of coordinate tuples (anything with a ``.coords`` attribute, such as
 a shapely LineString, is accepted as well).
   nx_simple_geoms  pysrc/cityseer/tools/graphs.py:58-107
+  nx_decompose     pysrc/cityseer/tools/graphs.py:1829-1962
   nx_to_dual       pysrc/cityseer/tools/graphs.py:1965-2149 (half geometries split at the
                    normalised midpoint, welded at the shared primal node; util.py:264-312 for the
                    coordinate alignment)
@@ -110,6 +111,48 @@ def nx_simple_geoms(g: nx.MultiGraph) -> nx.MultiGraph:
     for s, e, k in remove:
         g.remove_edge(s, e, key=k)
     return g
+
+
+def _sub_name(parts) -> str:
+    """util.add_node's name for a node made from others (pysrc/cityseer/tools/util.py:529-541)."""
+    names = []
+    for n in parts:
+        n = str(n)
+        names.append(f"{n[:5]}|{n[-5:]}" if len(n) > 10 else n)
+    return "±".join(names)
+
+
+def nx_decompose(g: nx.MultiGraph, decompose_max: float) -> nx.MultiGraph:
+    """Splits every edge into ceil(length / decompose_max) pieces of equal length
+    (pysrc/cityseer/tools/graphs.py:1829-1962).  New nodes are named from the edge's end nodes and
+    a counter; a new node is live unless both parent nodes are non-live (when both carry `live`)."""
+    if decompose_max <= 0:
+        raise ValueError("decompose_max must be positive")
+    out = g.copy()
+    for s, e, data in g.edges(data=True):
+        sxy = (g.nodes[s]["x"], g.nodes[s]["y"])
+        line = align_linestring_coords(coords_of(data["geom"]), sxy)
+        L = _length(line)
+        cuts = max(1, int(math.ceil(L / decompose_max)))
+        step_size = L / cuts
+        out.remove_edge(s, e)
+        rest = {k: v for k, v in data.items() if k != "geom"}
+        prior, step = s, 0.0
+        for i in range(cuts - 1):
+            seg = substring(line, step, step + step_size)
+            x, y = seg[-1][0], seg[-1][1]
+            name = _sub_name([s, i, e])
+            if name in out:
+                raise ValueError(f"Attempted to add a duplicate node at x: {x}, y:{y}. "
+                                 f"Check for existence of duplicate edges in the vicinity of {s}-{e}.")
+            out.add_node(name, x=x, y=y)
+            if "live" in g.nodes[s] and "live" in g.nodes[e]:
+                out.nodes[name]["live"] = bool(g.nodes[s]["live"]) or bool(g.nodes[e]["live"])
+            out.add_edge(prior, name, geom=seg, **rest)
+            prior = name
+            step += step_size
+        out.add_edge(prior, e, geom=substring(line, step, L), **rest)
+    return out
 
 
 def _dual_key(a, b, k) -> str:

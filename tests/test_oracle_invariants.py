@@ -89,3 +89,22 @@ def test_betweenness_with_a_non_live_node_invariant_to_node_order():
     for e in [("A", "B"), ("B", "C"), ("C", "D")]:
         vals = [r[e] for r in simp_runs]
         assert max(vals) - min(vals) < 0.01, (e, vals)
+
+
+def test_segment_closeness_invariant_under_decomposition():
+    """tests/rustalgos/test_centrality.py:622-649: segment closeness measures to the cut endpoints of
+    each threshold, so decomposing every edge into 20 m pieces leaves the sums over the original
+    nodes unchanged."""
+    g = mock_graph()
+    gd = graphs.nx_decompose(g, 20)
+    assert gd.number_of_nodes() > g.number_of_nodes()
+    assert all(graphs._length(graphs.coords_of(dd["geom"])) <= 20.0 + 1e-6 for _, _, dd in gd.edges(data=True))
+    _, _, ns = io.network_structure_from_nx(g)
+    _, _, nsd = io.network_structure_from_nx(gd)
+    d, b, s = _thr([200, 400, 800, 5000])
+    seg = oracle.segment_centrality(oracle.OracleGraph(ns), d, b, s, ns=ns)
+    segd = oracle.segment_centrality(oracle.OracleGraph(nsd), d, b, s, ns=nsd)
+    n = ns.node_count()
+    k = list(d).index(400)
+    for m in (0, 1, 2):  # density, harmonic, beta
+        assert np.isclose(seg[m, k].sum(), segd[m, k][:n].sum()), m
