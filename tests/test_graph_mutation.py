@@ -1,0 +1,56 @@
+"""Graph store robustness after removals (the reference's tests/test_graph_mutation.py): removed nodes
+and edges are rejected with the reference's ValueError messages, before any GPU work."""
+import pytest
+
+from cityseer_gb300.tools import io
+from helpers import mock_graph
+
+
+@pytest.fixture
+def ns():
+    return io.network_structure_from_nx(mock_graph())[2]
+
+
+def test_removed_node_is_rejected_by_setters_and_getters(ns):
+    v = ns.street_node_indices()[0]
+    ns.remove_street_node(v)
+    with pytest.raises(ValueError, match="does not exist"):
+        ns.set_node_live(v, True)
+    for get in (ns.get_node_payload_py, ns.get_node_weight, ns.is_node_live):
+        with pytest.raises(ValueError, match="node_idx .* does not exist"):
+            get(v)
+
+
+@pytest.mark.parametrize("closeness,betweenness", [(True, False), (False, True)])
+def test_removed_source_index_is_rejected(ns, closeness, betweenness):
+    v = ns.street_node_indices()[0]
+    ns.remove_street_node(v)
+    with pytest.raises(ValueError, match="does not exist"):
+        ns.centrality_shortest(compute_closeness=closeness, compute_betweenness=betweenness, distances=[500],
+                               source_indices=[v], sample_probability=1.0, pbar_disabled=True)
+
+
+def test_add_edge_to_a_removed_endpoint_is_rejected(ns):
+    a, b = ns.street_node_indices()[:2]
+    pa, pb = ns.get_node_payload_py(a), ns.get_node_payload_py(b)
+    wkt = f"LINESTRING({pa.coord[0]} {pa.coord[1]}, {pb.coord[0]} {pb.coord[1]})"
+    ns.remove_street_node(b)
+    with pytest.raises(ValueError, match="end_nd_idx .* does not exist"):
+        ns.add_street_edge(a, b, 999999, pa.node_key, pb.node_key, wkt)
+
+
+def test_removed_edge_getters(ns):
+    s, e, k = ns.edge_references()[0]
+    pl = ns.get_edge_payload_py(s, e, k)
+    assert pl.edge_idx == k and pl.length > 0 and pl.imp_factor == 1.0 and not pl.is_transport
+    ns.remove_street_edge(s, e, k)
+    for get in (ns.get_edge_payload_py, ns.get_edge_length, ns.get_edge_impedance):
+        with pytest.raises(ValueError, match="Edge not found"):
+            get(s, e, k)
+
+
+def test_remove_edge_with_a_removed_endpoint(ns):
+    s, e, k = ns.edge_references()[0]
+    ns.remove_street_node(s)
+    with pytest.raises(ValueError, match="start_nd_idx .* does not exist"):
+        ns.remove_street_edge(s, e, k)
