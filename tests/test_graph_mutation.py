@@ -54,3 +54,12 @@ def test_remove_edge_with_a_removed_endpoint(ns):
     ns.remove_street_node(s)
     with pytest.raises(ValueError, match="start_nd_idx .* does not exist"):
         ns.remove_street_edge(s, e, k)
+
+
+def test_simplest_wrappers_require_a_dual_graph(ns):
+    """tests/metrics/test_networks.py:247-261 (raised before any GPU work)."""
+    from cityseer_gb300.metrics import networks
+
+    for fn in (networks.closeness_simplest, networks.betweenness_simplest, networks.node_centrality_simplest):
+        with pytest.raises(ValueError, match="dual graph"):
+            fn(ns, {}, distances=[200, 400])
