@@ -178,29 +178,23 @@ def prepare_source_sampling(ns, sample_probability, sampling_weights, random_see
         # run samples the same sources as the reference; unseeded, the seed comes from the OS
         rng = StdRng.seed_from_u64(int(random_seed)) if random_seed is not None else StdRng(os.urandom(32))
         randoms = rng.random_f32(nb)
+    # sample_source_weight (rust/src/centrality.rs:1107-1139) for every listed source at once, in f32
     src_wt = np.zeros(nb, np.float32)
-    take = np.zeros(len(sources), bool)
+    take = eligible[sources] == 1
+    wt = weight[sources].astype(np.float32)
     count = 0
-    for j, s in enumerate(sources):
-        if not eligible[s]:
-            continue
-        wt = weight[s]
-        if is_indexed:
-            if prob is not None:
-                wt = np.float32(wt / prob)
-            count += 1
-        elif prob is not None:
-            p = prob
-            if sw is not None:
-                p = np.float32(p * sw[s])
-            if p <= 0.0:
-                continue
-            if randoms[s] >= p:
-                continue
-            count += 1
-            wt = np.float32(wt / p)
-        take[j] = True
-        src_wt[s] = wt
+    if is_indexed:
+        if prob is not None:
+            wt = (wt / prob).astype(np.float32)
+        count = int(take.sum())
+    elif prob is not None:
+        p = np.full(len(sources), prob, np.float32)
+        if sw is not None:
+            p = (p * sw[sources]).astype(np.float32)
+        take &= (p > 0.0) & (randoms[sources] < p)
+        wt = np.where(take, wt / np.where(p > 0.0, p, np.float32(1.0)), wt).astype(np.float32)
+        count = int(take.sum())
+    src_wt[sources[take]] = wt[take]
     return SourcePlan(
         process=sources[take].astype(np.int32),
         src_wt=src_wt,
