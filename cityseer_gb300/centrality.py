@@ -387,6 +387,41 @@ def centrality_shortest(ns, distances=None, betas=None, minutes=None, compute_cl
     return res
 
 
+def shortest_rows(ns, sp: SourcePlan, process: np.ndarray, dists, bets, secs, speed: float, tol: float,
+                  closeness: bool, betweenness: bool, track: bool):
+    """The device rows of centrality_shortest for the sources `process` under the plan `sp` (its
+    eligibility and source weights): ([7][K][N] f64, [K] i64 reach counts) on the graph's device,
+    before any post-scale.  The sharded multi-GPU form runs one slice of a plan's sources per rank
+    through it."""
+    nb = ns.node_bound()
+    K = len(dists)
+    csr = _primal_csr(ns)
+    dev = csr.device
+    proc_t = torch.from_numpy(np.ascontiguousarray(process, np.int32)).to(dev)
+    wt_t = torch.from_numpy(sp.src_wt).to(dev)
+    el_t = torch.from_numpy(sp.eligible).to(dev)
+    g = csr.struct(speed)
+    lib = _native.load()
+    rows = torch.zeros((7, K, nb), dtype=torch.float64, device=dev)
+    reach_all = torch.zeros(K, dtype=torch.int64, device=dev)
+    for lo, hi in _groups(K):
+        k = hi - lo
+        ws = _workspace(ns, csr, 0, k, speed, max(secs[lo:hi]))
+        out = torch.zeros((7, k, nb), dtype=torch.float64, device=dev)
+        reach = torch.zeros(k, dtype=torch.int32, device=dev)
+        q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, tol, closeness, betweenness, track,
+                        proc_t, wt_t, el_t)
+        o = _native.Outputs(out.data_ptr(), reach.data_ptr())
+        rc = lib.cs_centrality_shortest(C.byref(g), C.byref(q), C.byref(ws.plan), ws.ptr, ws.nbytes, o,
+                                        _stream_ptr())
+        if rc != _native.CS_OK:
+            ws.init(_stream_ptr())
+        _native.check(rc, "cs_centrality_shortest")
+        rows[:, lo:hi] = out
+        reach_all[lo:hi] = reach.to(torch.int64)
+    return rows, reach_all
+
+
 # ---------------------------------------------------------------------------------------------
 # betweenness_od_shortest (rust/src/centrality.rs:2419-2540)
 # ---------------------------------------------------------------------------------------------

@@ -1,10 +1,17 @@
-"""Multi-GPU form: replicas.  Sources are independent, so N ranks (one process per GPU) each run the
-whole workload on their own GPU with no collective on the data path; the only exchange is the
-timing reduction below (the slowest rank's time), which turns per-rank work into the whole job's
-throughput.  A graph sharded by sources would add one f64 sum-reduce of the accumulator rows at
-the end; with replicas there is none."""
+"""Multi-GPU forms.  Sources are independent units:
+
+* replicas: N ranks (one process per GPU) each run a whole workload with no collective on the data
+  path; the only exchange is the timing reduction (`job_throughput`: the slowest rank's time), which
+  turns per-rank work into the whole job's throughput;
+* one graph sharded by sources (`sharded_centrality_shortest`): every rank holds the graph, runs a
+  strided slice of the sources, and one f64 sum all-reduce of the accumulator rows gives every rank
+  the whole result.
+"""
 from __future__ import annotations
 
+import os
+
+import numpy as np
 import torch
 
 
@@ -22,3 +29,59 @@ def job_throughput(units_per_rank: float, seconds: float, device: torch.device |
     dist.all_reduce(u, op=dist.ReduceOp.SUM)
     t_max = float(t.item())
     return float(u.item()) / t_max, t_max
+
+
+def sharded_centrality_shortest(ns, distances=None, betas=None, minutes=None, compute_closeness=None,
+                                compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, tolerance=None,
+                                sample_probability=None, sampling_weights=None, random_seed=None,
+                                source_indices=None, group=None, rows_fn=None):
+    """centrality_shortest (rust/src/centrality.rs:1624-1874) for one graph over the ranks of a process
+    group: the same source plan on every rank (a sampled plan without a seed takes rank 0's seed),
+    rank r runs the plan's sources r, r + N, ..., and the rows and reach counts are summed over the
+    ranks (NCCL on GPUs; any backend for `rows_fn` results on the CPU).  Every rank returns the whole
+    result.  Without a process group it is centrality_shortest.  rows_fn(ns, plan, sources, distances,
+    betas, seconds, speed, tolerance, closeness, betweenness, track) -> (rows, reach) computes one
+    rank's share; the default runs it on the GPU (centrality.shortest_rows)."""
+    import torch.distributed as dist
+
+    from . import centrality as c
+    from .common import WALKING_SPEED, pair_distances_betas_time
+
+    closeness = True if compute_closeness is None else bool(compute_closeness)
+    betweenness = True if compute_betweenness is None else bool(compute_betweenness)
+    if not closeness and not betweenness:
+        raise ValueError(
+            "Either or both closeness and betweenness flags is required, but both parameters are False.")
+    speed = WALKING_SPEED if speed_m_s is None else float(speed_m_s)
+    tol = c.validate_tolerance(tolerance)
+    dists, bets, secs = pair_distances_betas_time(speed, distances, betas, minutes, min_threshold_wt)
+    on = dist.is_available() and dist.is_initialized()
+    world = dist.get_world_size(group) if on else 1
+    rank = dist.get_rank(group) if on else 0
+    seed = random_seed
+    if world > 1 and sample_probability is not None and seed is None:
+        box = [int.from_bytes(os.urandom(8), "little") if rank == 0 else None]
+        dist.broadcast_object_list(box, src=dist.get_global_rank(group, 0) if group is not None else 0, group=group)
+        seed = box[0]
+    sp = c.prepare_source_sampling(ns, sample_probability, sampling_weights, seed, source_indices)
+    track = sp.sample_probability is not None or sp.is_source_indexed
+    fn = rows_fn if rows_fn is not None else c.shortest_rows
+    rows, reach = fn(ns, sp, np.ascontiguousarray(sp.process[rank::world]), dists, bets, secs, speed, tol,
+                     closeness, betweenness, track)
+    if world > 1:
+        dist.all_reduce(rows, op=dist.ReduceOp.SUM, group=group)
+        dist.all_reduce(reach, op=dist.ReduceOp.SUM, group=group)
+    data = rows.cpu().numpy()
+    node_indices = ns.node_indices()
+    if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
+        scale = sp.n_live / sp.n_sources
+        if scale != 1.0:
+            idx = np.asarray(node_indices, np.int64)
+            data[5][:, idx] *= scale
+            data[6][:, idx] *= scale
+    ns._progress = sp.n_sources
+    res = c.CentralityShortestResult(dists, ns.node_keys_py(), node_indices, data)
+    if track:
+        res.sampled_source_count = sp.sampled_count
+        res.reachability_totals = [int(x) for x in reach.cpu().numpy()]
+    return res

@@ -47,3 +47,93 @@ def test_two_gloo_ranks():
     for rank, value, t_max in got:
         assert t_max == 3.0
         assert value == pytest.approx((1000.0 + 1001.0) / 3.0)
+
+
+def _oracle_rows(ns, sp, process, dists, bets, secs, speed, tol, closeness, betweenness, track):
+    """One rank's share on the CPU: the oracle over `process` under the plan's weights."""
+    import numpy as np
+
+    import oracle
+
+    plan = oracle.plan_from(sp, ns.node_bound())
+    plan["sources"] = np.asarray(process, np.int64)
+    plan["betweenness_scale"] = 1.0  # the sharded form scales after the reduction
+    out, reach = oracle.centrality_shortest(oracle.OracleGraph(ns), dists, bets, secs, speed=speed, tol=tol,
+                                            closeness=closeness, betweenness=betweenness, plan=plan)
+    return torch.from_numpy(out), torch.from_numpy(reach.astype(np.int64))
+
+
+_SHARD_CASES = [
+    dict(distances=[200, 800, 5000]),
+    dict(distances=[400, 1600], sample_probability=0.5, random_seed=9),
+    dict(distances=[600], source_indices=[0, 3, 5, 8, 13, 21, 34, 40], compute_closeness=False),
+]
+
+
+def _shard_rank(rank, world, port, q):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from cityseer_gb300.replicas import sharded_centrality_shortest
+        from cityseer_gb300.tools import io
+        from helpers import mock_graph
+
+        ns = io.network_structure_from_nx(mock_graph())[2]
+        for j, kw in enumerate(_SHARD_CASES):
+            r = sharded_centrality_shortest(ns, rows_fn=_oracle_rows, **kw)
+            q.put((rank, j, r._data, r.reachability_totals, r.sampled_source_count))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.timeout(180)
+def test_sharded_single_graph_equals_one_process():
+    """Two gloo ranks, each running half of the sources through the oracle, then one sum all-reduce,
+    equal the whole job run in one process (plain, sampled, source-indexed)."""
+    import numpy as np
+
+    from cityseer_gb300.replicas import sharded_centrality_shortest
+    from cityseer_gb300.tools import io
+    from helpers import mock_graph
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_shard_rank, args=(r, 2, port, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    got = [q.get(timeout=150) for _ in range(2 * len(_SHARD_CASES))]
+    for pr in procs:
+        pr.join(60)
+        assert pr.exitcode == 0
+    ns = io.network_structure_from_nx(mock_graph())[2]
+    for j, kw in enumerate(_SHARD_CASES):
+        want = sharded_centrality_shortest(ns, rows_fn=_oracle_rows, **kw)  # no process group: one rank
+        for rank, jj, data, reach, sampled in got:
+            if jj != j:
+                continue
+            np.testing.assert_allclose(data, want._data, rtol=1e-12, atol=1e-12)
+            assert reach == want.reachability_totals and sampled == want.sampled_source_count
+
+
+def test_sharded_form_without_a_group_equals_the_oracle_call():
+    import numpy as np
+
+    import oracle
+    from cityseer_gb300.centrality import prepare_source_sampling, validate_tolerance
+    from cityseer_gb300.common import pair_distances_betas_time
+    from cityseer_gb300.replicas import sharded_centrality_shortest
+    from cityseer_gb300.tools import io
+    from helpers import mock_graph
+
+    ns = io.network_structure_from_nx(mock_graph())[2]
+    for kw in _SHARD_CASES:
+        got = sharded_centrality_shortest(ns, rows_fn=_oracle_rows, **kw)
+        sp = prepare_source_sampling(ns, kw.get("sample_probability"), None, kw.get("random_seed"),
+                                     kw.get("source_indices"))
+        d, b, s = pair_distances_betas_time(1.33333, distances=kw["distances"])
+        want, _ = oracle.centrality_shortest(oracle.OracleGraph(ns), d, b, s, tol=validate_tolerance(None),
+                                             closeness=kw.get("compute_closeness", True),
+                                             plan=oracle.plan_from(sp, ns.node_bound()))
+        np.testing.assert_array_equal(got._data, want)
