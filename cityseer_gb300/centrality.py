@@ -345,34 +345,11 @@ def centrality_shortest(ns, distances=None, betas=None, minutes=None, compute_cl
     tol = validate_tolerance(tolerance)
     dists, bets, secs = pair_distances_betas_time(speed, distances, betas, minutes, min_threshold_wt)
     sp = prepare_source_sampling(ns, sample_probability, sampling_weights, random_seed, source_indices)
-    nb = ns.node_bound()
     node_indices = ns.node_indices()
-    K = len(dists)
-    data = np.zeros((7, K, nb), np.float64)
-    reach_tot = np.zeros(K, np.int64)
     track = sp.sample_probability is not None or sp.is_source_indexed
-    csr = _primal_csr(ns)
-    dev = csr.device
-    proc_t = torch.from_numpy(sp.process).to(dev)
-    wt_t = torch.from_numpy(sp.src_wt).to(dev)
-    el_t = torch.from_numpy(sp.eligible).to(dev)
-    g = csr.struct(speed)
-    lib = _native.load()
-    for lo, hi in _groups(K):
-        k = hi - lo
-        ws = _workspace(ns, csr, 0, k, speed, max(secs[lo:hi]))
-        out = torch.zeros((7, k, nb), dtype=torch.float64, device=dev)
-        reach = torch.zeros(k, dtype=torch.int32, device=dev)
-        q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, tol, closeness, betweenness, track,
-                        proc_t, wt_t, el_t)
-        o = _native.Outputs(out.data_ptr(), reach.data_ptr())
-        rc = lib.cs_centrality_shortest(C.byref(g), C.byref(q), C.byref(ws.plan), ws.ptr, ws.nbytes, o,
-                                        _stream_ptr())
-        if rc != _native.CS_OK:
-            ws.init(_stream_ptr())
-        _native.check(rc, "cs_centrality_shortest")
-        data[:, lo:hi] = out.cpu().numpy()
-        reach_tot[lo:hi] = reach.cpu().numpy().astype(np.int64)
+    rows, reach = shortest_rows(ns, sp, sp.process, dists, bets, secs, speed, tol, closeness, betweenness, track)
+    data = rows.cpu().numpy()
+    reach_tot = reach.cpu().numpy()
     if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
         scale = sp.n_live / sp.n_sources
         if scale != 1.0:
@@ -402,9 +379,10 @@ def shortest_rows(ns, sp: SourcePlan, process: np.ndarray, dists, bets, secs, sp
     el_t = torch.from_numpy(sp.eligible).to(dev)
     g = csr.struct(speed)
     lib = _native.load()
-    rows = torch.zeros((7, K, nb), dtype=torch.float64, device=dev)
+    groups = _groups(K)
+    rows = torch.zeros((7, K, nb), dtype=torch.float64, device=dev) if len(groups) > 1 else None
     reach_all = torch.zeros(K, dtype=torch.int64, device=dev)
-    for lo, hi in _groups(K):
+    for lo, hi in groups:
         k = hi - lo
         ws = _workspace(ns, csr, 0, k, speed, max(secs[lo:hi]))
         out = torch.zeros((7, k, nb), dtype=torch.float64, device=dev)
@@ -417,7 +395,10 @@ def shortest_rows(ns, sp: SourcePlan, process: np.ndarray, dists, bets, secs, sp
         if rc != _native.CS_OK:
             ws.init(_stream_ptr())
         _native.check(rc, "cs_centrality_shortest")
-        rows[:, lo:hi] = out
+        if rows is None:
+            rows = out
+        else:
+            rows[:, lo:hi] = out
         reach_all[lo:hi] = reach.to(torch.int64)
     return rows, reach_all
 
