@@ -302,6 +302,23 @@ def _groups(k: int):
     return [(i, min(k, i + step)) for i in range(0, k, step)]
 
 
+def _cutoff_groups(k: int):
+    """Launch groups for the modes whose results at a threshold depend on the search cutoff, which
+    the reference sets to the largest threshold for all of them: simplest paths (the cutoff prunes
+    by metric seconds while routes are ordered by angle) and segment betweenness (a target beyond a
+    threshold still credits it when its first and last segments are long).  Each group is
+    (lo, hi, sel): thresholds lo..hi-1 are returned, sel lists the thresholds launched, and a group
+    that does not end at the largest threshold carries it as a hidden last lane."""
+    if k <= _native.MAX_K:
+        return [(0, k, list(range(k)))]
+    step = _native.MAX_K - 1
+    out = []
+    for lo in range(0, k, step):
+        hi = min(k, lo + step)
+        out.append((lo, hi, list(range(lo, hi)) + ([k - 1] if hi < k else [])))
+    return out
+
+
 def _make_query(dists, betas, secs, speed, tol, closeness, betweenness, track_reach, proc_t, wt_t, el_t,
                 asu=180.0, fso=1.0) -> _native.Query:
     q = _native.Query()
@@ -515,19 +532,19 @@ def segment_centrality(ns, distances=None, betas=None, minutes=None, compute_clo
     el_t = torch.zeros(max(nb, 1), dtype=torch.uint8, device=dev)
     g = csr.struct(speed)
     lib = _native.load()
-    for lo, hi in _groups(K):
-        k = hi - lo
-        ws = _workspace(ns, csr, 1, k, speed, max(secs[lo:hi]))
+    for lo, hi, sel in _cutoff_groups(K):
+        k = len(sel)
+        gd, gb, gs = [dists[i] for i in sel], [bets[i] for i in sel], [secs[i] for i in sel]
+        ws = _workspace(ns, csr, 1, k, speed, max(gs))
         out = torch.zeros((4, k, nb), dtype=torch.float64, device=dev)
-        q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, float(TIE_EPSILON), closeness, betweenness,
-                        False, proc_t, wt_t, el_t)
+        q = _make_query(gd, gb, gs, speed, float(TIE_EPSILON), closeness, betweenness, False, proc_t, wt_t, el_t)
         o = _native.Outputs(out.data_ptr(), None)
         rc = lib.cs_segment_centrality(C.byref(g), C.byref(q), C.byref(ws.plan), ws.ptr, ws.nbytes, o,
                                        _stream_ptr())
         if rc != _native.CS_OK:
             ws.init(_stream_ptr())
         _native.check(rc, "cs_segment_centrality")
-        data[:, lo:hi] = out.cpu().numpy()
+        data[:, lo:hi] = out[:, : hi - lo].cpu().numpy()
     ns._progress = len(node_indices)
     return CentralitySegmentResult(dists, ns.node_keys_py(), node_indices, data)
 

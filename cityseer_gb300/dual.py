@@ -182,7 +182,7 @@ def estimate_states(ns, speed: float, max_seconds: int) -> int:
 
 
 def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, betweenness, sp):
-    from .centrality import CentralitySimplestResult, _groups, _make_query, _stream_ptr
+    from .centrality import CentralitySimplestResult, _cutoff_groups, _make_query, _stream_ptr
 
     nb = ns.node_bound()
     node_indices = ns.node_indices()
@@ -197,20 +197,21 @@ def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, between
     el_t = torch.from_numpy(sp.eligible).to(dev)
     g = csr.struct(speed)
     lib = _native.load()
-    for lo, hi in _groups(K):
-        k = hi - lo
-        ws = dual_workspace(ns, csr, k, speed, cap=estimate_states(ns, speed, max(secs[lo:hi])))
+    # every launch searches to the largest threshold, as the reference's single search does
+    for lo, hi, sel in _cutoff_groups(K):
+        k = len(sel)
+        gd, gb, gs = [dists[i] for i in sel], [bets[i] for i in sel], [secs[i] for i in sel]
+        ws = dual_workspace(ns, csr, k, speed, cap=estimate_states(ns, speed, max(gs)))
         out = torch.zeros((4, k, nb), dtype=torch.float64, device=dev)
         reach = torch.zeros(k, dtype=torch.int32, device=dev)
-        q = _make_query(dists[lo:hi], bets[lo:hi], secs[lo:hi], speed, tol, closeness, betweenness, track, proc_t,
-                        wt_t, el_t, asu, fso)
+        q = _make_query(gd, gb, gs, speed, tol, closeness, betweenness, track, proc_t, wt_t, el_t, asu, fso)
         o = _native.Outputs(out.data_ptr(), reach.data_ptr())
         rc = lib.cs_centrality_simplest(C.byref(g), C.byref(q), C.byref(ws.plan), ws.ptr, ws.nbytes, o, _stream_ptr())
         if rc != _native.CS_OK:
             ws.init(_stream_ptr())
         _native.check(rc, "cs_centrality_simplest")
-        data[:, lo:hi] = out.cpu().numpy()
-        reach_tot[lo:hi] = reach.cpu().numpy().astype(np.int64)
+        data[:, lo:hi] = out[:, : hi - lo].cpu().numpy()
+        reach_tot[lo:hi] = reach[: hi - lo].cpu().numpy().astype(np.int64)
     if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
         scale = sp.n_live / sp.n_sources
         if scale != 1.0:

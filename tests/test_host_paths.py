@@ -57,6 +57,30 @@ class _StandInLib:
             C.memmove(o.reach, r.ctypes.data, r.nbytes)
         return _native.CS_OK
 
+    def cs_centrality_simplest(self, g, q_ref, plan_ref, ws, ws_bytes, o, stream):
+        self.calls += 1
+        q = q_ref._obj
+        d, b, s, plan = self._query(q)
+        out, reach = oracle.centrality_simplest(self.og, d, b, s, speed=q.speed_m_s, tol=q.tolerance,
+                                                closeness=bool(q.compute_closeness),
+                                                betweenness=bool(q.compute_betweenness), plan=plan,
+                                                asu=q.angular_scaling_unit, fso=q.farness_scaling_offset)
+        C.memmove(o.out, out.ctypes.data, out.nbytes)
+        r = reach.astype(np.int32)
+        C.memmove(o.reach, r.ctypes.data, r.nbytes)
+        return _native.CS_OK
+
+    def cs_segment_centrality(self, g, q_ref, plan_ref, ws, ws_bytes, o, stream):
+        self.calls += 1
+        q = q_ref._obj
+        d, b, s, plan = self._query(q)
+        live = np.asarray(self.ns.node_indices())[self.ns.arrays()["live"][np.asarray(self.ns.node_indices())] == 1]
+        assert sorted(plan["sources"].tolist()) == sorted(live.tolist())  # every live node is a source
+        out = oracle.segment_centrality(self.og, d, b, s, speed=q.speed_m_s, closeness=bool(q.compute_closeness),
+                                        betweenness=bool(q.compute_betweenness), ns=self.ns)
+        C.memmove(o.out, out.ctypes.data, out.nbytes)
+        return _native.CS_OK
+
     def cs_betweenness_od_shortest(self, g, q_ref, od_ptr, od_dst, od_w, plan_ref, ws, ws_bytes, o, stream):
         self.calls += 1
         q = q_ref._obj
@@ -100,6 +124,11 @@ def stand_in(monkeypatch):
     monkeypatch.setattr(centrality, "_primal_csr", lambda ns: _StandInCSR(ns))
     monkeypatch.setattr(centrality, "_workspace", lambda *a, **k: _StandInWS())
     monkeypatch.setattr(centrality, "_stream_ptr", lambda: None)
+    from cityseer_gb300 import dual
+
+    monkeypatch.setattr(dual, "dual_csr", lambda ns: _StandInCSR(ns))
+    monkeypatch.setattr(dual, "dual_workspace", lambda *a, **k: _StandInWS())
+    monkeypatch.setattr(dual, "estimate_states", lambda *a, **k: 1024)
 
     def use(ns):
         box["lib"] = _StandInLib(ns, real)
@@ -164,3 +193,37 @@ def test_od_host_path(stand_in):
     d, b, s = pair_distances_betas_time(1.33333, distances=[300, 1200])
     want = oracle.betweenness_od(oracle.OracleGraph(ns), d, b, s, od.rows(ns.node_bound()), ns=ns)
     np.testing.assert_array_equal(res._data, want)
+
+
+def test_simplest_host_path(stand_in):
+    from cityseer_gb300.tools import graphs
+
+    ns = io.network_structure_from_nx(graphs.nx_to_dual(mock_graph()))[2]
+    lib = stand_in(ns)
+    cases = (dict(), dict(p=0.5, seed=8), dict(src=[0, 4, 9, 16, 25, 36]), dict(asu=90.0, fso=2.0, closeness=True),
+             dict(dists=list(range(100, 2000, 100))))
+    for kw in cases:
+        dists = kw.get("dists", [300, 1200])
+        sp = prepare_source_sampling(ns, kw.get("p"), None, kw.get("seed"), kw.get("src"))
+        d, b, s = pair_distances_betas_time(1.33333, distances=dists)
+        want, reach = oracle.centrality_simplest(oracle.OracleGraph(ns), d, b, s, tol=validate_tolerance(None),
+                                                 plan=oracle.plan_from(sp, ns.node_bound()),
+                                                 asu=kw.get("asu", 180.0), fso=kw.get("fso", 1.0))
+        res = ns.centrality_simplest(distances=dists, sample_probability=kw.get("p"), random_seed=kw.get("seed"),
+                                     source_indices=kw.get("src"), angular_scaling_unit=kw.get("asu"),
+                                     farness_scaling_offset=kw.get("fso"))
+        np.testing.assert_array_equal(res._data, want)
+        if kw.get("p") or kw.get("src"):
+            assert res.reachability_totals == [int(x) for x in reach]
+    assert lib.calls == 6  # 19 thresholds: two groups
+
+
+def test_segment_host_path(stand_in):
+    ns = io.network_structure_from_nx(mock_graph())[2]
+    ns.set_node_live(ns.node_indices()[3], False)
+    lib = stand_in(ns)
+    for dists in ([200, 600], list(range(50, 1000, 50))):
+        res = ns.segment_centrality(distances=dists)
+        d, b, s = pair_distances_betas_time(1.33333, distances=dists)
+        np.testing.assert_array_equal(res._data, oracle.segment_centrality(oracle.OracleGraph(ns), d, b, s, ns=ns))
+    assert lib.calls == 3
