@@ -111,3 +111,17 @@ def test_segment_host_path(stand_in):
         d, b, s = pair_distances_betas_time(1.33333, distances=dists)
         np.testing.assert_array_equal(res._data, oracle.segment_centrality(oracle.OracleGraph(ns), d, b, s, ns=ns))
     assert lib.calls == 3
+
+
+def test_od_host_path_more_than_sixteen_thresholds(stand_in):
+    ns = io.network_structure_from_nx(mock_graph())[2]
+    lib = stand_in(ns)
+    rng = np.random.default_rng(5)
+    idx = np.asarray(ns.node_indices())
+    od = OdMatrix(rng.choice(idx, 200).tolist(), rng.choice(idx, 200).tolist(), rng.uniform(0, 3, 200).tolist())
+    dists = list(range(100, 2000, 100))
+    res = ns.betweenness_od_shortest(od, distances=dists)
+    d, b, s = pair_distances_betas_time(1.33333, distances=dists)
+    want = oracle.betweenness_od(oracle.OracleGraph(ns), d, b, s, od.rows(ns.node_bound()), ns=ns)
+    np.testing.assert_array_equal(res._data, want)
+    assert lib.calls == 2
