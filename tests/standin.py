@@ -76,6 +76,25 @@ class _StandInLib:
         C.memmove(o.out, out.ctypes.data, out.nbytes)
         return _native.CS_OK
 
+    def cs_tree_shortest(self, g, nq, src_ptr, max_seconds, speed, plan_ref, ws, ws_bytes, row_cap, count_ptr,
+                         node_ptr, agg_ptr, pred_ptr, stream):
+        """Per query the oracle's tree (dijkstra_tree_shortest): settle order, agg_seconds, pred."""
+        self.calls += 1
+        srcs = _arr(src_ptr, C.c_int32, nq)
+        counts = np.zeros(nq, np.int32)
+        for qi, src in enumerate(srcs.tolist()):
+            vis, tree = oracle.tree_shortest(self.og, int(src), int(max_seconds), float(speed.value))
+            n = len(vis)
+            counts[qi] = n if n <= row_cap else -n
+            m = min(n, row_cap)
+            rows = (vis[:m].astype(np.int32), tree["agg_seconds"][vis[:m]].astype(np.float32),
+                    tree["pred"][vis[:m]].astype(np.int32))
+            for ptr, arr in zip((node_ptr, agg_ptr, pred_ptr), rows):
+                if m:
+                    C.memmove(ptr + qi * row_cap * 4, arr.ctypes.data, arr.nbytes)
+        C.memmove(count_ptr, counts.ctypes.data, counts.nbytes)
+        return _native.CS_OK
+
     def cs_betweenness_od_shortest(self, g, q_ref, od_ptr, od_dst, od_w, plan_ref, ws, ws_bytes, o, stream):
         self.calls += 1
         q = q_ref._obj

@@ -125,3 +125,41 @@ def test_od_host_path_more_than_sixteen_thresholds(stand_in):
     want = oracle.betweenness_od(oracle.OracleGraph(ns), d, b, s, od.rows(ns.node_bound()), ns=ns)
     np.testing.assert_array_equal(res._data, want)
     assert lib.calls == 2
+
+
+def test_tree_host_bookkeeping(stand_in):
+    """dijkstra_tree_shortest / dijkstra_tree_segment host decoding and edge bookkeeping (visited
+    edges, last and origin segments) from the kernel's rows, against the oracle for every source,
+    including equal-distance ties (the stand-in's rows follow the oracle's settle order)."""
+    import networkx as nx
+
+    from cityseer_gb300.tools import graphs
+
+    grid = nx.MultiGraph()  # a perfect 6 x 6 grid: equal edge lengths, many equal distances
+    for i in range(6):
+        for j in range(6):
+            grid.add_node(f"{i}-{j}", x=100.0 * i, y=100.0 * j)
+            if i:
+                grid.add_edge(f"{i - 1}-{j}", f"{i}-{j}")
+            if j:
+                grid.add_edge(f"{i}-{j - 1}", f"{i}-{j}")
+    for g in (mock_graph(), graphs.nx_simple_geoms(grid)):
+        ns = io.network_structure_from_nx(g)[2]
+        ns.remove_street_node(ns.node_indices()[7])
+        stand_in(ns)
+        og = oracle.OracleGraph(ns)
+        for src in ns.node_indices():
+            for max_seconds in (0, 200, 1500):
+                vis, tree = ns.dijkstra_tree_shortest(src, max_seconds, 1.33333)
+                vis_ref, t_ref = oracle.tree_shortest(og, src, max_seconds, 1.33333)
+                assert vis == vis_ref.tolist()
+                vis, vedges, tree, emap = ns.dijkstra_tree_segment(src, max_seconds, 1.33333)
+                vis_ref, ve_ref, t_ref = oracle.tree_segment(og, src, max_seconds, 1.33333)
+                assert vis == vis_ref.tolist() and vedges == ve_ref.tolist()
+                for v in vis_ref:
+                    assert np.float32(tree[v].agg_seconds) == t_ref["agg_seconds"][v]
+                    assert (tree[v].pred if tree[v].pred is not None else -1) == t_ref["pred"][v]
+                    assert (tree[v].last_seg if tree[v].last_seg is not None else -1) == t_ref["last_seg"][v]
+                    assert (tree[v].origin_seg if tree[v].origin_seg is not None else -1) == t_ref["origin_seg"][v]
+                for e in ve_ref:
+                    assert emap[e].visited
