@@ -190,6 +190,8 @@ class Batch:
         return a.value, b.value
 
     def results(self):
+        """Each job's result object, as its plain call returns it, except that the batched launch does
+        not count reachability_totals (left empty) for jobs with source subsets."""
         out = []
         for jb in self.jobs:
             ns = jb["ns"]
