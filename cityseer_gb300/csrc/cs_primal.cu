@@ -1,30 +1,33 @@
-// cs_primal.cu -- GB300 kernels for shortest-path node centrality, segment centrality and
-// shortest-path trees (isochrones) on the primal graph.
+// cs_primal.cu -- GB300 kernels for shortest-path node centrality, OD-weighted betweenness, segment
+// centrality and shortest-path trees (isochrones) on the primal graph.
 //
 // Reference behaviour (cityseer-api v4.24.0):
 //   centrality_shortest        rust/src/centrality.rs:1624-1874
 //   dijkstra_brandes_shortest  rust/src/centrality.rs:1344-1494
 //   circuit_ranks_from_traversal rust/src/centrality.rs:470-526
 //   brandes_backprop_with_beta rust/src/centrality.rs:823-873
+//   betweenness_od_shortest    rust/src/centrality.rs:2419-2540
 //   segment_centrality         rust/src/centrality.rs:2134-2407
 //   dijkstra_tree_segment      rust/src/centrality.rs:1524-1611
 //   dijkstra_tree_shortest_inner rust/src/centrality.rs:1141-1200
 //
-// Design (one warp per source, persistent warps pulling sources from a work counter):
+// Design (one warp per source; persistent warps pull sources from a work counter, and in the
+// block-synchronous form the warps of a block run each phase together):
 //  1. Bounded label-correcting search ("near-far" banded Bellman-Ford) from the source over
 //     reversed edges.  Every relaxation is fl(d[u] + w) with w >= 0, so the least fixpoint is
 //     unique and bit-identical to the reference's heap Dijkstra whatever the relaxation order.
-//  2. Warp LSD radix sort of the reached set by distance: the reference's settle order.
+//  2. Warp sort of the reached set by distance (cs_sort.cuh: distance buckets, or LSD radix): the
+//     reference's settle order.
 //  3. Replay, per reached node and in parallel, of the exact sequence of candidate offers the
 //     heap Dijkstra would make to it (offering neighbours in settle order), through the
 //     reference's Phase-1 tie rules (and Phase 2 when tolerance > 1e-4).  This reproduces its
-//     multi-predecessor lists; sigma follows in settle order.
+//     multi-predecessor lists; sigma follows chunk by chunk in settle order in the same pass.
 //  4. Closeness into target rows and circuit ranks; one backward Brandes sweep carrying all K
 //     thresholds (a state beyond threshold k contributes nothing to lane k, so one sweep equals
 //     the reference's K sweeps).
 // Per-slot scratch: dense dist/aux arrays over node_bound (reset touched entries only) plus
-// compact per-reached-node arrays of capacity `cap`; sources that overflow `cap` are retried
-// with cap = node_bound inside the same API call.
+// compact per-reached-node arrays of capacity `cap`; sources that overflow `cap` are redone inside
+// the same API call at 4x the capacity, then 4x again, up to cap = node_bound.
 #include <cstdio>
 #include <cstring>
 #include <string>
