@@ -711,6 +711,66 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c3(args):
+    """The curved-lattice configuration (250x250 jittered lattice, 30% of streets curved): simplest-path
+    centrality on its dual (124,500 dual nodes) and segment centrality on the primal, thresholds
+    [500, 1000, 2000] m, through the public API; wall clock around each call with the device
+    synchronised, inputs resident after the warm-up calls.  Parity of both paths is in the tests."""
+    import torch
+
+    from cityseer_gb300 import _native, synth
+
+    p, dists = synth.lattice_config("c3", side=args.side)
+    t0 = time.perf_counter()
+    nsd = synth.dual_structure(p)
+    ns = synth.primal_structure(p)
+    t_build = time.perf_counter() - t0
+    n_seg = sum(1 for v in ns.node_indices() if ns.is_node_live(v))
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t)
+        return float(np.mean(ts))
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    t_simp = timed(lambda: nsd.centrality_simplest(distances=dists))
+    over, inexact = C.c_int64(), C.c_int64()
+    _native.load().cs_last_retries(C.byref(over), C.byref(inexact))
+    t_seg = timed(lambda: ns.segment_centrality(distances=dists))
+    clk = clocks.stop()
+    line = {
+        "metric": "sources/s, 250x250 curved lattice, d<=2 km: simplest-path centrality on the dual "
+                  "(segment centrality on the primal beside it)",
+        "value": nsd.node_count() / t_simp,
+        "unit": "sources/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_simp * 1000.0,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded curved jittered lattice and its dual, see cityseer_gb300/synth.py)",
+        "config": {"workload": "c3_curved250", "dual_nodes": nsd.node_count(), "primal_nodes": ns.node_count(),
+                   "distances": dists, "timing": "wall clock per public-API call, device synchronised"},
+        "segment": {"value": n_seg / t_seg, "unit": "sources/s", "ms_per_step": t_seg * 1000.0},
+        "simplest_sources_redone_exactly": int(inexact.value),
+        "setup_s": round(t_build, 1),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -721,8 +781,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "batch", "serve"],
-                    help="c2: the 202,500-node lattice (default); batch: the 96-graph batched form; "
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "batch", "serve"],
+                    help="c2: the 202,500-node lattice (default); c3: the curved lattice, simplest paths "
+                         "on its dual and segments on the primal; batch: the 96-graph batched form; "
                          "serve: the served form")
     ap.add_argument("--serve-sizes", default="50000,100000,200000,400000,800000,1200000")
     ap.add_argument("--serve-rates", default="20,100,500,2000")
@@ -735,6 +796,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve" and args.impl != "reference":
         run_serve(args)
+    elif args.workload == "c3" and args.impl != "reference":
+        run_c3(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
