@@ -239,6 +239,8 @@ class NetworkStructure:
         self._e_shared: list[str | None] = []
         self._e_keys: list[tuple[Any, Any] | None] | None = []
         self._is_dual = False
+        self._barriers: list[str] | None = None
+        self._edge_rtree_built = False
         self._progress = 0
         self._version = 0
         self._cache: dict[str, Any] = {}
@@ -600,6 +602,34 @@ class NetworkStructure:
     @property
     def node_lives(self) -> list[bool]:
         return [bool(v) for v in self._live.view()[self._exists.view() == 1]]
+
+    @property
+    def street_node_lives(self) -> list[bool]:
+        m = (self._exists.view() == 1) & (self._transport.view() == 0)
+        return [bool(v) for v in self._live.view()[m]]
+
+    @property
+    def node_zs(self) -> list[float | None]:
+        m = self._exists.view() == 1
+        return [float(z) if h else None for z, h in zip(self._z.view()[m], self._has_z.view()[m])]
+
+    @property
+    def node_xyzs(self) -> list[tuple[float, float, float | None]]:
+        m = self._exists.view() == 1
+        return list(zip(self._x.view()[m].tolist(), self._y.view()[m].tolist(), self.node_zs))
+
+    # Spatial indexes and barriers serve data assignment (rust/src/graph.rs:1064-1231), which this
+    # package does not restate; centrality never reads them, in the reference as here.
+    def build_edge_rtree(self) -> None:
+        """Accepted for compatibility: no edge R-tree is kept (centrality does not use one)."""
+        self._edge_rtree_built = True
+
+    def set_barriers(self, barriers_wkt: list[str]) -> None:
+        """Stores the barrier geometries (WKT); centrality does not use them."""
+        self._barriers = list(barriers_wkt)
+
+    def unset_barriers(self) -> None:
+        self._barriers = None
 
     def _node_checked(self, node_idx: int) -> None:
         self._require_node(node_idx, "node_idx")

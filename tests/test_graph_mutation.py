@@ -63,3 +63,28 @@ def test_simplest_wrappers_require_a_dual_graph(ns):
     for fn in (networks.closeness_simplest, networks.betweenness_simplest, networks.node_centrality_simplest):
         with pytest.raises(ValueError, match="dual graph"):
             fn(ns, {}, distances=[200, 400])
+
+
+def test_remaining_getters_and_compatibility_methods():
+    """street_node_lives, node_zs, node_xyzs (rust/src/graph.rs:660-696); barriers and the edge
+    R-tree are accepted and do not change centrality inputs."""
+    import networkx as nx
+
+    from cityseer_gb300.tools import graphs
+
+    g = nx.MultiGraph()
+    g.add_node("a", x=0.0, y=0.0, z=3.0)
+    g.add_node("b", x=100.0, y=0.0)
+    g.add_edge("a", "b")
+    ns = io.network_structure_from_nx(graphs.nx_simple_geoms(g))[2]
+    assert ns.node_zs == [3.0, None]
+    assert ns.node_xyzs == [(0.0, 0.0, 3.0), (100.0, 0.0, None)]
+    assert ns.street_node_lives == [True, True]
+    import numpy as np
+
+    before = {k: np.copy(v) for k, v in ns.arrays().items()}
+    ns.build_edge_rtree()
+    ns.set_barriers(["LINESTRING (50 -10, 50 10)"])
+    ns.unset_barriers()
+    for k, v in ns.arrays().items():
+        np.testing.assert_array_equal(v, before[k], err_msg=k)  # NaN z compares equal here
