@@ -6,8 +6,13 @@ from types import SimpleNamespace
 from . import centrality as _c
 from . import graph as _g
 from .common import (
+    avg_distances_for_betas,
     betas_from_distances,
+    check_numerical_data,
+    clip_wts_curve,
+    clipped_beta_wt,
     distances_from_betas,
+    distances_from_seconds,
     pair_distances_betas_time,
     seconds_from_distances,
 )
@@ -23,4 +28,5 @@ centrality = SimpleNamespace(
 )
 
 __all__ = ["graph", "centrality", "pair_distances_betas_time", "betas_from_distances", "distances_from_betas",
-           "seconds_from_distances"]
+           "seconds_from_distances", "distances_from_seconds", "avg_distances_for_betas", "clip_wts_curve",
+           "clipped_beta_wt", "check_numerical_data"]
