@@ -362,11 +362,16 @@ def centrality_shortest(ns, distances=None, betas=None, minutes=None, compute_cl
     tol = validate_tolerance(tolerance)
     dists, bets, secs = pair_distances_betas_time(speed, distances, betas, minutes, min_threshold_wt)
     sp = prepare_source_sampling(ns, sample_probability, sampling_weights, random_seed, source_indices)
-    node_indices = ns.node_indices()
     track = sp.sample_probability is not None or sp.is_source_indexed
     rows, reach = shortest_rows(ns, sp, sp.process, dists, bets, secs, speed, tol, closeness, betweenness, track)
-    data = rows.cpu().numpy()
-    reach_tot = reach.cpu().numpy()
+    return finish_shortest(ns, dists, sp, rows.cpu().numpy(), reach.cpu().numpy(), betweenness, track)
+
+
+def finish_shortest(ns, dists, sp: SourcePlan, data: np.ndarray, reach_tot: np.ndarray, betweenness: bool,
+                    track: bool) -> CentralityShortestResult:
+    """Post-scale of betweenness for source subsets (rust/src/centrality.rs:1852-1868) and the
+    result object of centrality_shortest."""
+    node_indices = ns.node_indices()
     if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
         scale = sp.n_live / sp.n_sources
         if scale != 1.0:

@@ -181,24 +181,25 @@ def estimate_states(ns, speed: float, max_seconds: int) -> int:
     return hit
 
 
-def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, betweenness, sp):
-    from .centrality import CentralitySimplestResult, _cutoff_groups, _make_query, _stream_ptr
+def simplest_rows(ns, sp, process, dists, bets, secs, speed, tol, asu, fso, closeness, betweenness, track):
+    """The device rows of centrality_simplest for the sources `process` under the plan `sp`:
+    ([4][K][N] f64, [K] i64 reach counts) on the graph's device, before any post-scale.  Every
+    launch searches to the largest threshold, as the reference's single search does."""
+    from .centrality import _cutoff_groups, _make_query, _stream_ptr
 
     nb = ns.node_bound()
-    node_indices = ns.node_indices()
     K = len(dists)
-    data = np.zeros((4, K, nb), np.float64)
-    reach_tot = np.zeros(K, np.int64)
-    track = sp.sample_probability is not None or sp.is_source_indexed
     csr = dual_csr(ns)
     dev = csr.device
-    proc_t = torch.from_numpy(sp.process).to(dev)
+    proc_t = torch.from_numpy(np.ascontiguousarray(process, np.int32)).to(dev)
     wt_t = torch.from_numpy(sp.src_wt).to(dev)
     el_t = torch.from_numpy(sp.eligible).to(dev)
     g = csr.struct(speed)
     lib = _native.load()
-    # every launch searches to the largest threshold, as the reference's single search does
-    for lo, hi, sel in _cutoff_groups(K):
+    groups = _cutoff_groups(K)
+    rows = torch.zeros((4, K, nb), dtype=torch.float64, device=dev) if len(groups) > 1 else None
+    reach_all = torch.zeros(K, dtype=torch.int64, device=dev)
+    for lo, hi, sel in groups:
         k = len(sel)
         gd, gb, gs = [dists[i] for i in sel], [bets[i] for i in sel], [secs[i] for i in sel]
         ws = dual_workspace(ns, csr, k, speed, cap=estimate_states(ns, speed, max(gs)))
@@ -210,8 +211,19 @@ def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, between
         if rc != _native.CS_OK:
             ws.init(_stream_ptr())
         _native.check(rc, "cs_centrality_simplest")
-        data[:, lo:hi] = out[:, : hi - lo].cpu().numpy()
-        reach_tot[lo:hi] = reach[: hi - lo].cpu().numpy().astype(np.int64)
+        if rows is None:
+            rows = out
+        else:
+            rows[:, lo:hi] = out[:, : hi - lo]
+        reach_all[lo:hi] = reach[: hi - lo].to(torch.int64)
+    return rows, reach_all
+
+
+def finish_simplest(ns, dists, sp, data: np.ndarray, reach_tot: np.ndarray, betweenness: bool, track: bool):
+    """Post-scale (source subsets) and the result object of centrality_simplest."""
+    from .centrality import CentralitySimplestResult
+
+    node_indices = ns.node_indices()
     if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
         scale = sp.n_live / sp.n_sources
         if scale != 1.0:
@@ -223,6 +235,13 @@ def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, between
         res.sampled_source_count = sp.sampled_count
         res.reachability_totals = [int(x) for x in reach_tot]
     return res
+
+
+def run_simplest(ns, dists, bets, secs, speed, tol, asu, fso, closeness, betweenness, sp):
+    track = sp.sample_probability is not None or sp.is_source_indexed
+    rows, reach = simplest_rows(ns, sp, sp.process, dists, bets, secs, speed, tol, asu, fso, closeness, betweenness,
+                                track)
+    return finish_simplest(ns, dists, sp, rows.cpu().numpy(), reach.cpu().numpy(), betweenness, track)
 
 
 class DualTreeWorkspace(device.Workspace):

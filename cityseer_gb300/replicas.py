@@ -31,17 +31,9 @@ def job_throughput(units_per_rank: float, seconds: float, device: torch.device |
     return float(u.item()) / t_max, t_max
 
 
-def sharded_centrality_shortest(ns, distances=None, betas=None, minutes=None, compute_closeness=None,
-                                compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, tolerance=None,
-                                sample_probability=None, sampling_weights=None, random_seed=None,
-                                source_indices=None, group=None, rows_fn=None):
-    """centrality_shortest (rust/src/centrality.rs:1624-1874) for one graph over the ranks of a process
-    group: the same source plan on every rank (a sampled plan without a seed takes rank 0's seed),
-    rank r runs the plan's sources r, r + N, ..., and the rows and reach counts are summed over the
-    ranks (NCCL on GPUs; any backend for `rows_fn` results on the CPU).  Every rank returns the whole
-    result.  Without a process group it is centrality_shortest.  rows_fn(ns, plan, sources, distances,
-    betas, seconds, speed, tolerance, closeness, betweenness, track) -> (rows, reach) computes one
-    rank's share; the default runs it on the GPU (centrality.shortest_rows)."""
+def _sharded(ns, kind, distances, betas, minutes, compute_closeness, compute_betweenness, min_threshold_wt,
+             speed_m_s, tolerance, sample_probability, sampling_weights, random_seed, source_indices, group,
+             rows_fn, extra):
     import torch.distributed as dist
 
     from . import centrality as c
@@ -65,23 +57,54 @@ def sharded_centrality_shortest(ns, distances=None, betas=None, minutes=None, co
         seed = box[0]
     sp = c.prepare_source_sampling(ns, sample_probability, sampling_weights, seed, source_indices)
     track = sp.sample_probability is not None or sp.is_source_indexed
-    fn = rows_fn if rows_fn is not None else c.shortest_rows
-    rows, reach = fn(ns, sp, np.ascontiguousarray(sp.process[rank::world]), dists, bets, secs, speed, tol,
-                     closeness, betweenness, track)
+    mine = np.ascontiguousarray(sp.process[rank::world])
+    if kind == "shortest":
+        fn = rows_fn if rows_fn is not None else c.shortest_rows
+        rows, reach = fn(ns, sp, mine, dists, bets, secs, speed, tol, closeness, betweenness, track)
+    else:
+        from . import dual
+
+        fn = rows_fn if rows_fn is not None else dual.simplest_rows
+        rows, reach = fn(ns, sp, mine, dists, bets, secs, speed, tol, extra[0], extra[1], closeness, betweenness,
+                         track)
     if world > 1:
         dist.all_reduce(rows, op=dist.ReduceOp.SUM, group=group)
         dist.all_reduce(reach, op=dist.ReduceOp.SUM, group=group)
-    data = rows.cpu().numpy()
-    node_indices = ns.node_indices()
-    if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
-        scale = sp.n_live / sp.n_sources
-        if scale != 1.0:
-            idx = np.asarray(node_indices, np.int64)
-            data[5][:, idx] *= scale
-            data[6][:, idx] *= scale
-    ns._progress = sp.n_sources
-    res = c.CentralityShortestResult(dists, ns.node_keys_py(), node_indices, data)
-    if track:
-        res.sampled_source_count = sp.sampled_count
-        res.reachability_totals = [int(x) for x in reach.cpu().numpy()]
-    return res
+    data, reach_tot = rows.cpu().numpy(), reach.cpu().numpy()
+    if kind == "shortest":
+        return c.finish_shortest(ns, dists, sp, data, reach_tot, betweenness, track)
+    from . import dual
+
+    return dual.finish_simplest(ns, dists, sp, data, reach_tot, betweenness, track)
+
+
+def sharded_centrality_shortest(ns, distances=None, betas=None, minutes=None, compute_closeness=None,
+                                compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, tolerance=None,
+                                sample_probability=None, sampling_weights=None, random_seed=None,
+                                source_indices=None, group=None, rows_fn=None):
+    """centrality_shortest (rust/src/centrality.rs:1624-1874) for one graph over the ranks of a process
+    group: the same source plan on every rank (a sampled plan without a seed takes rank 0's seed),
+    rank r runs the plan's sources r, r + N, ..., and the rows and reach counts are summed over the
+    ranks (NCCL on GPUs; any backend for `rows_fn` results on the CPU).  Every rank returns the whole
+    result.  Without a process group it is centrality_shortest.  rows_fn(ns, plan, sources, distances,
+    betas, seconds, speed, tolerance, closeness, betweenness, track) -> (rows, reach) computes one
+    rank's share; the default runs it on the GPU (centrality.shortest_rows)."""
+    return _sharded(ns, "shortest", distances, betas, minutes, compute_closeness, compute_betweenness,
+                    min_threshold_wt, speed_m_s, tolerance, sample_probability, sampling_weights, random_seed,
+                    source_indices, group, rows_fn, None)
+
+
+def sharded_centrality_simplest(ns, distances=None, betas=None, minutes=None, compute_closeness=None,
+                                compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, tolerance=None,
+                                angular_scaling_unit=None, farness_scaling_offset=None, sample_probability=None,
+                                sampling_weights=None, random_seed=None, source_indices=None, group=None,
+                                rows_fn=None):
+    """centrality_simplest (rust/src/centrality.rs:1880-2132) sharded like sharded_centrality_shortest;
+    rows_fn(ns, plan, sources, distances, betas, seconds, speed, tolerance, angular_scaling_unit,
+    farness_scaling_offset, closeness, betweenness, track) defaults to dual.simplest_rows."""
+    ns.validate_dual_for_angular("centrality_simplest")
+    asu = 180.0 if angular_scaling_unit is None else float(angular_scaling_unit)
+    fso = 1.0 if farness_scaling_offset is None else float(farness_scaling_offset)
+    return _sharded(ns, "simplest", distances, betas, minutes, compute_closeness, compute_betweenness,
+                    min_threshold_wt, speed_m_s, tolerance, sample_probability, sampling_weights, random_seed,
+                    source_indices, group, rows_fn, (asu, fso))

@@ -67,6 +67,19 @@ def test_sharded_default_share_equals_the_plain_call(stand_in):
     assert shard.reachability_totals == plain.reachability_totals
 
 
+def test_sharded_simplest_default_share_equals_the_plain_call(stand_in):
+    from cityseer_gb300.replicas import sharded_centrality_simplest
+    from cityseer_gb300.tools import graphs
+
+    ns = io.network_structure_from_nx(graphs.nx_to_dual(mock_graph()))[2]
+    stand_in(ns)
+    subset = ns.node_indices()[::4]
+    plain = ns.centrality_simplest(distances=list(range(100, 2000, 100)), source_indices=subset)
+    shard = sharded_centrality_simplest(ns, distances=list(range(100, 2000, 100)), source_indices=subset)
+    np.testing.assert_array_equal(shard._data, plain._data)
+    assert shard.reachability_totals == plain.reachability_totals
+
+
 def test_od_host_path(stand_in):
     ns = io.network_structure_from_nx(mock_graph())[2]
     stand_in(ns)

@@ -63,6 +63,20 @@ def _oracle_rows(ns, sp, process, dists, bets, secs, speed, tol, closeness, betw
     return torch.from_numpy(out), torch.from_numpy(reach.astype(np.int64))
 
 
+def _oracle_rows_simplest(ns, sp, process, dists, bets, secs, speed, tol, asu, fso, closeness, betweenness, track):
+    import numpy as np
+
+    import oracle
+
+    plan = oracle.plan_from(sp, ns.node_bound())
+    plan["sources"] = np.asarray(process, np.int64)
+    plan["betweenness_scale"] = 1.0
+    out, reach = oracle.centrality_simplest(oracle.OracleGraph(ns), dists, bets, secs, speed=speed, tol=tol,
+                                            closeness=closeness, betweenness=betweenness, plan=plan, asu=asu,
+                                            fso=fso)
+    return torch.from_numpy(out), torch.from_numpy(reach.astype(np.int64))
+
+
 _SHARD_CASES = [
     dict(distances=[200, 800, 5000]),
     dict(distances=[400, 1600], sample_probability=0.5, random_seed=9),
@@ -83,6 +97,13 @@ def _shard_rank(rank, world, port, q):
         for j, kw in enumerate(_SHARD_CASES):
             r = sharded_centrality_shortest(ns, rows_fn=_oracle_rows, **kw)
             q.put((rank, j, r._data, r.reachability_totals, r.sampled_source_count))
+        from cityseer_gb300.replicas import sharded_centrality_simplest
+        from cityseer_gb300.tools import graphs
+
+        nsd = io.network_structure_from_nx(graphs.nx_to_dual(mock_graph()))[2]
+        r = sharded_centrality_simplest(nsd, distances=[300, 1200], sample_probability=0.6, random_seed=2,
+                                        rows_fn=_oracle_rows_simplest)
+        q.put((rank, "simplest", r._data, r.reachability_totals, r.sampled_source_count))
     finally:
         dist.destroy_process_group()
 
@@ -103,10 +124,20 @@ def test_sharded_single_graph_equals_one_process():
     procs = [ctx.Process(target=_shard_rank, args=(r, 2, port, q)) for r in range(2)]
     for pr in procs:
         pr.start()
-    got = [q.get(timeout=150) for _ in range(2 * len(_SHARD_CASES))]
+    got = [q.get(timeout=150) for _ in range(2 * (len(_SHARD_CASES) + 1))]
     for pr in procs:
         pr.join(60)
         assert pr.exitcode == 0
+    from cityseer_gb300.replicas import sharded_centrality_simplest
+    from cityseer_gb300.tools import graphs
+
+    nsd = io.network_structure_from_nx(graphs.nx_to_dual(mock_graph()))[2]
+    want_s = sharded_centrality_simplest(nsd, distances=[300, 1200], sample_probability=0.6, random_seed=2,
+                                         rows_fn=_oracle_rows_simplest)
+    for rank, jj, data, reach, sampled in got:
+        if jj == "simplest":
+            np.testing.assert_allclose(data, want_s._data, rtol=1e-12, atol=1e-12)
+            assert reach == want_s.reachability_totals and sampled == want_s.sampled_source_count
     ns = io.network_structure_from_nx(mock_graph())[2]
     for j, kw in enumerate(_SHARD_CASES):
         want = sharded_centrality_shortest(ns, rows_fn=_oracle_rows, **kw)  # no process group: one rank
