@@ -521,23 +521,33 @@ def segment_centrality(ns, distances=None, betas=None, minutes=None, compute_clo
     if not closeness and not betweenness:
         raise ValueError(
             "Either or both closeness and betweenness flags is required, but both parameters are False.")
+    rows = segment_rows(ns, segment_sources(ns), dists, bets, secs, speed, closeness, betweenness)
+    return finish_segment(ns, dists, rows.cpu().numpy())
+
+
+def segment_sources(ns) -> np.ndarray:
+    """The live nodes, in node-index order: segment centrality's sources (rust/src/centrality.rs:2190)."""
+    idx = np.asarray(ns.node_indices(), np.int64)
+    return idx[ns.arrays()["live"][idx] == 1].astype(np.int32)
+
+
+def segment_rows(ns, process, dists, bets, secs, speed: float, closeness: bool, betweenness: bool):
+    """The device rows of segment_centrality ([4][K][N] f64) for the sources `process`.  Every launch
+    searches to the largest threshold (segment betweenness depends on the cutoff)."""
     nb = ns.node_bound()
-    node_indices = ns.node_indices()
-    a = ns.arrays()
-    idx = np.asarray(node_indices, np.int64)
-    process = idx[a["live"][idx] == 1].astype(np.int32)
     K = len(dists)
-    data = np.zeros((4, K, nb), np.float64)
     csr = _primal_csr(ns)
     if csr.has_missing_reverse:
         raise ValueError("Edge not found")
     dev = csr.device
-    proc_t = torch.from_numpy(process).to(dev)
+    proc_t = torch.from_numpy(np.ascontiguousarray(process, np.int32)).to(dev)
     wt_t = torch.zeros(max(nb, 1), dtype=torch.float32, device=dev)
     el_t = torch.zeros(max(nb, 1), dtype=torch.uint8, device=dev)
     g = csr.struct(speed)
     lib = _native.load()
-    for lo, hi, sel in _cutoff_groups(K):
+    groups = _cutoff_groups(K)
+    rows = torch.zeros((4, K, nb), dtype=torch.float64, device=dev) if len(groups) > 1 else None
+    for lo, hi, sel in groups:
         k = len(sel)
         gd, gb, gs = [dists[i] for i in sel], [bets[i] for i in sel], [secs[i] for i in sel]
         ws = _workspace(ns, csr, 1, k, speed, max(gs))
@@ -549,7 +559,15 @@ def segment_centrality(ns, distances=None, betas=None, minutes=None, compute_clo
         if rc != _native.CS_OK:
             ws.init(_stream_ptr())
         _native.check(rc, "cs_segment_centrality")
-        data[:, lo:hi] = out[:, : hi - lo].cpu().numpy()
+        if rows is None:
+            rows = out
+        else:
+            rows[:, lo:hi] = out[:, : hi - lo]
+    return rows
+
+
+def finish_segment(ns, dists, data: np.ndarray) -> CentralitySegmentResult:
+    node_indices = ns.node_indices()
     ns._progress = len(node_indices)
     return CentralitySegmentResult(dists, ns.node_keys_py(), node_indices, data)
 

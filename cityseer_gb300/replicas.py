@@ -108,3 +108,33 @@ def sharded_centrality_simplest(ns, distances=None, betas=None, minutes=None, co
     return _sharded(ns, "simplest", distances, betas, minutes, compute_closeness, compute_betweenness,
                     min_threshold_wt, speed_m_s, tolerance, sample_probability, sampling_weights, random_seed,
                     source_indices, group, rows_fn, (asu, fso))
+
+
+def sharded_segment_centrality(ns, distances=None, betas=None, minutes=None, compute_closeness=None,
+                               compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, group=None,
+                               rows_fn=None):
+    """segment_centrality (rust/src/centrality.rs:2134-2407) sharded like sharded_centrality_shortest:
+    rank r runs the live sources r, r + N, ... and the rows are summed over the ranks.
+    rows_fn(ns, sources, distances, betas, seconds, speed, closeness, betweenness) -> rows defaults to
+    centrality.segment_rows."""
+    import torch.distributed as dist
+
+    from . import centrality as c
+    from .common import WALKING_SPEED, pair_distances_betas_time
+
+    speed = WALKING_SPEED if speed_m_s is None else float(speed_m_s)
+    dists, bets, secs = pair_distances_betas_time(speed, distances, betas, minutes, min_threshold_wt)
+    closeness = True if compute_closeness is None else bool(compute_closeness)
+    betweenness = True if compute_betweenness is None else bool(compute_betweenness)
+    if not closeness and not betweenness:
+        raise ValueError(
+            "Either or both closeness and betweenness flags is required, but both parameters are False.")
+    on = dist.is_available() and dist.is_initialized()
+    world = dist.get_world_size(group) if on else 1
+    rank = dist.get_rank(group) if on else 0
+    mine = np.ascontiguousarray(c.segment_sources(ns)[rank::world])
+    fn = rows_fn if rows_fn is not None else c.segment_rows
+    rows = fn(ns, mine, dists, bets, secs, speed, closeness, betweenness)
+    if world > 1:
+        dist.all_reduce(rows, op=dist.ReduceOp.SUM, group=group)
+    return c.finish_segment(ns, dists, rows.cpu().numpy())

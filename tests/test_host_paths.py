@@ -80,6 +80,16 @@ def test_sharded_simplest_default_share_equals_the_plain_call(stand_in):
     assert shard.reachability_totals == plain.reachability_totals
 
 
+def test_sharded_segment_default_share_equals_the_plain_call(stand_in):
+    from cityseer_gb300.replicas import sharded_segment_centrality
+
+    ns = io.network_structure_from_nx(mock_graph())[2]
+    stand_in(ns)
+    dists = list(range(50, 1000, 50))
+    np.testing.assert_array_equal(sharded_segment_centrality(ns, distances=dists)._data,
+                                  ns.segment_centrality(distances=dists)._data)
+
+
 def test_od_host_path(stand_in):
     ns = io.network_structure_from_nx(mock_graph())[2]
     stand_in(ns)

@@ -77,6 +77,27 @@ def _oracle_rows_simplest(ns, sp, process, dists, bets, secs, speed, tol, asu, f
     return torch.from_numpy(out), torch.from_numpy(reach.astype(np.int64))
 
 
+def _oracle_rows_segment(ns, sources, dists, bets, secs, speed, closeness, betweenness):
+    """One rank's share of segment centrality: the oracle over the live nodes, restricted to
+    `sources` through the node liveness the oracle reads (a stand-in for the GPU's source list)."""
+    import numpy as np
+
+    import oracle
+
+    saved = ns._live.view().copy()
+    try:
+        keep = np.zeros_like(saved)
+        keep[np.asarray(sources, np.int64)] = saved[np.asarray(sources, np.int64)]
+        ns._live.view()[:] = keep
+        ns._touch()
+        out = oracle.segment_centrality(oracle.OracleGraph(ns), dists, bets, secs, speed=speed, closeness=closeness,
+                                        betweenness=betweenness, ns=ns)
+    finally:
+        ns._live.view()[:] = saved
+        ns._touch()
+    return torch.from_numpy(out)
+
+
 _SHARD_CASES = [
     dict(distances=[200, 800, 5000]),
     dict(distances=[400, 1600], sample_probability=0.5, random_seed=9),
@@ -104,6 +125,10 @@ def _shard_rank(rank, world, port, q):
         r = sharded_centrality_simplest(nsd, distances=[300, 1200], sample_probability=0.6, random_seed=2,
                                         rows_fn=_oracle_rows_simplest)
         q.put((rank, "simplest", r._data, r.reachability_totals, r.sampled_source_count))
+        from cityseer_gb300.replicas import sharded_segment_centrality
+
+        r = sharded_segment_centrality(ns, distances=[200, 600], rows_fn=_oracle_rows_segment)
+        q.put((rank, "segment", r._data, [], 0))
     finally:
         dist.destroy_process_group()
 
@@ -124,7 +149,7 @@ def test_sharded_single_graph_equals_one_process():
     procs = [ctx.Process(target=_shard_rank, args=(r, 2, port, q)) for r in range(2)]
     for pr in procs:
         pr.start()
-    got = [q.get(timeout=150) for _ in range(2 * (len(_SHARD_CASES) + 1))]
+    got = [q.get(timeout=150) for _ in range(2 * (len(_SHARD_CASES) + 2))]
     for pr in procs:
         pr.join(60)
         assert pr.exitcode == 0
@@ -134,7 +159,15 @@ def test_sharded_single_graph_equals_one_process():
     nsd = io.network_structure_from_nx(graphs.nx_to_dual(mock_graph()))[2]
     want_s = sharded_centrality_simplest(nsd, distances=[300, 1200], sample_probability=0.6, random_seed=2,
                                          rows_fn=_oracle_rows_simplest)
+    import oracle
+    from cityseer_gb300.common import pair_distances_betas_time
+
+    ns_p = io.network_structure_from_nx(mock_graph())[2]
+    d, b, s = pair_distances_betas_time(1.33333, distances=[200, 600])
+    want_seg = oracle.segment_centrality(oracle.OracleGraph(ns_p), d, b, s, ns=ns_p)
     for rank, jj, data, reach, sampled in got:
+        if jj == "segment":
+            np.testing.assert_allclose(data, want_seg, rtol=1e-9, atol=1e-9)
         if jj == "simplest":
             np.testing.assert_allclose(data, want_s._data, rtol=1e-12, atol=1e-12)
             assert reach == want_s.reachability_totals and sampled == want_s.sampled_source_count
