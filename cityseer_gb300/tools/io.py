@@ -32,10 +32,12 @@ def network_structure_from_nx(g: nx.MultiGraph):
                 if geom is None:
                     raise ValueError(f"Edge has no geometry: start_node={s}, end_node={e}, edge_idx={k}")
                 coords = align_linestring_coords(coords_of(geom), (sx, sy))
-                ei = ns.add_street_edge_coords(s_idx, e_idx, int(k), s, e, coords,
-                                               float(data.get("imp_factor", 1.0)),
-                                               shared_primal_node_key=data.get("primal_node_id"))
-                edge_rows[f"{s}-{e}"] = (ei, s_idx, e_idx, k, s, e)
+                imp = float(data.get("imp_factor", 1.0))
+                shared = data.get("primal_node_id")
+                ei = ns.add_street_edge_coords(s_idx, e_idx, int(k), s, e, coords, imp,
+                                               shared_primal_node_key=shared)
+                # keyed like the reference's frame (io.py:1149): parallel edges share a row, the last wins
+                edge_rows[f"{s}-{e}"] = (ei, s_idx, e_idx, k, s, e, imp, coords, shared)
     ns.validate()
     nodes = {"index": list(node_rows), "ns_node_idx": [r[0] for r in node_rows.values()],
              "x": [r[1] for r in node_rows.values()], "y": [r[2] for r in node_rows.values()],
@@ -43,7 +45,67 @@ def network_structure_from_nx(g: nx.MultiGraph):
     if g.graph.get("is_dual"):
         for col in ("primal_edge_node_a", "primal_edge_node_b", "primal_edge_idx"):
             nodes[col] = [g.nodes[k].get(col) for k in node_rows]
-    edges = {"index": list(edge_rows), "ns_edge_idx": [r[0] for r in edge_rows.values()],
-             "start_ns_node_idx": [r[1] for r in edge_rows.values()],
-             "end_ns_node_idx": [r[2] for r in edge_rows.values()]}
+    rows = list(edge_rows.values())
+    edges = {"index": list(edge_rows), "ns_edge_idx": [r[0] for r in rows],
+             "start_ns_node_idx": [r[1] for r in rows], "end_ns_node_idx": [r[2] for r in rows],
+             "edge_idx": [int(r[3]) for r in rows], "nx_start_node_key": [r[4] for r in rows],
+             "nx_end_node_key": [r[5] for r in rows], "imp_factor": [r[6] for r in rows],
+             "geom": [r[7] for r in rows], "primal_node_id": [r[8] for r in rows]}
+    nodes["z"] = [r[3] for r in node_rows.values()]
     return nodes, edges, ns
+
+
+def _records(frame):
+    """Rows of a (Geo)DataFrame or of a dict of equal-length columns, as dicts (index under "index")."""
+    if hasattr(frame, "iterrows"):
+        for key, row in frame.iterrows():
+            rec = dict(row)
+            rec["index"] = key
+            if hasattr(frame, "geometry"):
+                rec["geom"] = row[frame.geometry.name]
+            yield rec
+        return
+    cols = list(frame)
+    n = len(frame[cols[0]]) if cols else 0
+    for i in range(n):
+        yield {c: frame[c][i] for c in cols}
+
+
+def network_structure_from_gpd(nodes_gdf, edges_gdf) -> NetworkStructure:
+    """Rebuilds a NetworkStructure from the node and edge frames network_structure_from_nx returns
+    (pysrc/cityseer/tools/io.py:1213-1321): GeoDataFrames, or the plain dicts of columns this package
+    returns where geopandas is absent.  Edges whose end nodes are missing are skipped."""
+    node_cols = ("x", "y", "live", "weight")
+    edge_cols = ("start_ns_node_idx", "end_ns_node_idx", "edge_idx", "nx_start_node_key", "nx_end_node_key",
+                 "imp_factor")
+    have_n = set(nodes_gdf.columns) if hasattr(nodes_gdf, "columns") else set(nodes_gdf)
+    have_e = set(edges_gdf.columns) if hasattr(edges_gdf, "columns") else set(edges_gdf)
+    for c in node_cols:
+        if c not in have_n:
+            raise ValueError(f"Missing expected column in nodes GDF: {c}")
+    for c in edge_cols:
+        if c not in have_e:
+            raise ValueError(f"Missing expected column in edges GDF: {c}")
+    ns = NetworkStructure()
+    mapping, xy = {}, {}
+    for rec in _records(nodes_gdf):
+        z = rec.get("z")
+        if z is not None and isinstance(z, float) and z != z:
+            z = None
+        key = rec["index"]
+        mapping[key] = ns.add_street_node(str(key), float(rec["x"]), float(rec["y"]), bool(rec["live"]),
+                                          float(rec["weight"]), z=None if z is None else float(z))
+        xy[key] = (float(rec["x"]), float(rec["y"]))
+    for rec in _records(edges_gdf):
+        a, b = rec["nx_start_node_key"], rec["nx_end_node_key"]
+        if a not in mapping or b not in mapping:
+            continue
+        coords = align_linestring_coords(coords_of(rec["geom"]), xy[a])
+        shared = rec.get("primal_node_id")
+        if shared is not None and isinstance(shared, float) and shared != shared:
+            shared = None
+        ns.add_street_edge_coords(mapping[a], mapping[b], int(rec["edge_idx"]), a, b, coords,
+                                  float(rec["imp_factor"]), shared_primal_node_key=None if shared is None else str(shared))
+    ns.validate()
+    ns.build_edge_rtree()
+    return ns
