@@ -1,7 +1,6 @@
 """The synthetic workloads stand in for the benchmark configurations' networks; their shapes are
 checked here against the configurations' stated sizes and recipes (node counts, streets, drop and
 diagonal fractions, curvature, dual sizes, thresholds)."""
-import numpy as np
 
 from cityseer_gb300 import synth
 
