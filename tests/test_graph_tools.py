@@ -1,0 +1,61 @@
+"""Graph tools against the reference's own checks (tests/tools/test_graphs.py:548-700): the dual of
+the diamond graph (5 dual nodes, 8 dual edges, degrees, 100 m welded geometries, bearings and shared
+primal nodes per pair) and nx_decompose (lengths preserved, pieces no longer than the maximum)."""
+import math
+
+import networkx as nx
+import numpy as np
+import pytest
+
+from cityseer_gb300.tools import graphs
+from helpers import diamond_graph, mock_graph
+
+# (dual edge from -> to): (in bearing, out bearing, shared primal node), tests/tools/test_graphs.py:660-700
+EXPECTED = {
+    ("0_1_k0", "0_2_k0"): (-60, 60, "0"),
+    ("0_1_k0", "1_2_k0"): (120, 0, "1"),
+    ("0_1_k0", "1_3_k0"): (120, 60, "1"),
+    ("0_2_k0", "1_2_k0"): (60, 180, "2"),
+    ("0_2_k0", "2_3_k0"): (60, 120, "2"),
+    ("1_2_k0", "1_3_k0"): (180, 60, "1"),
+    ("1_2_k0", "2_3_k0"): (0, 120, "2"),
+    ("1_3_k0", "2_3_k0"): (60, -60, "3"),
+}
+
+
+def test_diamond_dual():
+    g = diamond_graph()
+    gd = graphs.nx_to_dual(g)
+    assert gd.number_of_nodes() == 5 and gd.number_of_edges() == 8
+    for n, d in gd.nodes(data=True):
+        assert nx.degree(gd, n) == (4 if n == "1_2_k0" else 3)
+        pg = graphs.coords_of(g[d["primal_edge_node_a"]][d["primal_edge_node_b"]][d["primal_edge_idx"]]["geom"])
+        assert [tuple(c) for c in graphs.coords_of(d["primal_edge"])] == [tuple(c) for c in pg]
+    for (a, b), (inb, outb, shared) in EXPECTED.items():
+        (d,) = gd[a][b].values()
+        c = graphs.coords_of(d["geom"])
+        assert round(graphs._length(c)) == 100
+        if (gd.nodes[a]["x"], gd.nodes[a]["y"]) != tuple(c[0][:2]):
+            c = c[::-1]
+        (sx, sy), (mx, my), (ex, ey) = c[0][:2], c[1][:2], c[-1][:2]
+        got = (round(math.degrees(math.atan2(my - sy, mx - sx))), round(math.degrees(math.atan2(ey - my, ex - mx))))
+        assert got == (inb, outb), (a, b, got)
+        assert d["primal_node_id"] == shared
+        assert shared in (gd.nodes[b]["primal_edge_node_a"], gd.nodes[b]["primal_edge_node_b"])
+
+
+def test_dual_requires_geometries():
+    g = diamond_graph()
+    del g["0"]["1"][0]["geom"]
+    with pytest.raises(KeyError):
+        graphs.nx_to_dual(g)
+
+
+def test_decompose_preserves_length_and_caps_pieces():
+    g = mock_graph()
+    gd = graphs.nx_decompose(g, 50)
+    total = sum(graphs._length(graphs.coords_of(d["geom"])) for _, _, d in g.edges(data=True))
+    total_d = sum(graphs._length(graphs.coords_of(d["geom"])) for _, _, d in gd.edges(data=True))
+    assert np.isclose(total, total_d, atol=0.01, rtol=1e-4)
+    assert all(graphs._length(graphs.coords_of(d["geom"])) <= 50 + 1e-6 for _, _, d in gd.edges(data=True))
+    assert gd.number_of_nodes() > g.number_of_nodes()
