@@ -59,3 +59,49 @@ def test_decompose_preserves_length_and_caps_pieces():
     assert np.isclose(total, total_d, atol=0.01, rtol=1e-4)
     assert all(graphs._length(graphs.coords_of(d["geom"])) <= 50 + 1e-6 for _, _, d in gd.edges(data=True))
     assert gd.number_of_nodes() > g.number_of_nodes()
+
+
+# edge payloads on the diamond graph (tests/tools/test_io.py:300-520):
+# (start, end): (length, angle_sum, imp_factor, in_bearing, out_bearing)
+PRIMAL_PAYLOADS = {
+    ("0", "1"): (100.0, 0.0, 1.0, 120.0, 120.0), ("0", "2"): (100.0, 0.0, 1.0, 60.0, 60.0),
+    ("1", "0"): (100.0, 0.0, 1.0, -60.0, -60.0), ("1", "2"): (100.0, 0.0, 1.0, 0.0, 0.0),
+    ("1", "3"): (100.0, 0.0, 1.0, 60.0, 60.0), ("2", "0"): (100.0, 0.0, 1.0, -120.0, -120.0),
+    ("2", "1"): (100.0, 0.0, 1.0, 180.0, 180.0), ("2", "3"): (100.0, 0.0, 1.0, 120.0, 120.0),
+    ("3", "1"): (100.0, 0.0, 1.0, -120.0, -120.0), ("3", "2"): (100.0, 0.0, 1.0, -60.0, -60.0),
+}
+DUAL_PAYLOADS = {
+    ("0_1_k0", "0_2_k0"): (100.0, 120.0, 1.0, -60.0, 60.0), ("0_1_k0", "1_2_k0"): (100.0, 120.0, 1.0, 120.0, 0.0),
+    ("0_1_k0", "1_3_k0"): (100.0, 60.0, 1.0, 120.0, 60.0), ("0_2_k0", "0_1_k0"): (100.0, 120.0, 1.0, -120.0, 120.0),
+    ("0_2_k0", "1_2_k0"): (100.0, 120.0, 1.0, 60.0, 180.0), ("0_2_k0", "2_3_k0"): (100.0, 60.0, 1.0, 60.0, 120.0),
+    ("1_2_k0", "0_1_k0"): (100.0, 120.0, 1.0, 180.0, -60.0),
+}
+
+
+@pytest.mark.parametrize("dual", [False, True])
+def test_diamond_edge_payloads(dual):
+    from cityseer_gb300.tools import io
+
+    g = diamond_graph()
+    g.nodes["3"]["live"] = False
+    if dual:
+        g = graphs.nx_to_dual(g)
+    nodes, edges, ns = io.network_structure_from_nx(g)
+    assert ns.is_dual is dual and ns.edge_count == 2 * g.number_of_edges() and len(nodes["index"]) == ns.node_count()
+    for v in ns.street_node_indices():
+        p = ns.get_node_payload_py(v)
+        i = nodes["index"].index(p.node_key)
+        assert p.coord == (nodes["x"][i], nodes["y"][i]) and p.live == nodes["live"][i]
+    want = DUAL_PAYLOADS if dual else PRIMAL_PAYLOADS
+    seen = 0
+    for s, e, k in ns.edge_references():
+        pl = ns.get_edge_payload_py(s, e, k)
+        row = edges["index"].index(f"{pl.start_nd_key_py}-{pl.end_nd_key_py}")
+        assert (edges["start_ns_node_idx"][row], edges["end_ns_node_idx"][row], edges["edge_idx"][row]) == (s, e, k)
+        assert np.isnan(pl.seconds)
+        key = (pl.start_nd_key_py, pl.end_nd_key_py)
+        if key in want:
+            np.testing.assert_allclose((pl.length, pl.angle_sum, pl.imp_factor, pl.in_bearing, pl.out_bearing),
+                                       want[key], atol=0.01, rtol=1e-4, err_msg=str(key))
+            seen += 1
+    assert seen == len(want)
