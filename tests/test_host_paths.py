@@ -186,3 +186,36 @@ def test_tree_host_bookkeeping(stand_in):
                     assert (tree[v].origin_seg if tree[v].origin_seg is not None else -1) == t_ref["origin_seg"][v]
                 for e in ve_ref:
                     assert emap[e].visited
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_randomised_host_calls(stand_in, seed):
+    """Seeded random graphs, removals, liveness, thresholds (up to 20), flags, sampling and subsets:
+    the public calls equal the oracle on the same plan."""
+    rng = np.random.default_rng(100 + seed)
+    p, _ = synth.lattice_config("c1", side=int(rng.integers(6, 12)))
+    ns = synth.primal_structure(p)
+    nb = ns.node_bound()
+    for v in rng.choice(nb, 3, replace=False):
+        ns.remove_street_node(int(v))
+    idx = ns.node_indices()
+    for v in rng.choice(idx, 4, replace=False):
+        ns.set_node_live(int(v), False)
+    stand_in(ns)
+    k = int(rng.integers(1, 21))
+    dists = sorted(int(x) for x in rng.choice(np.arange(100, 3000, 50), k, replace=False))
+    closeness, betweenness = [(True, True), (True, False), (False, True)][seed % 3]
+    kw = {}
+    if seed % 2:
+        kw = dict(sample_probability=float(rng.uniform(0.2, 0.9)), random_seed=int(rng.integers(0, 1 << 31)))
+    elif seed % 3 == 0:
+        kw = dict(source_indices=sorted(int(x) for x in rng.choice(idx, 15, replace=False)))
+    res = ns.centrality_shortest(distances=dists, compute_closeness=closeness, compute_betweenness=betweenness, **kw)
+    want, reach, sp = _want(ns, dists, p=kw.get("sample_probability"), seed=kw.get("random_seed"),
+                            src=kw.get("source_indices"), closeness=closeness, betweenness=betweenness)
+    np.testing.assert_array_equal(res._data, want)
+    seg = ns.segment_centrality(distances=dists, compute_closeness=closeness, compute_betweenness=betweenness)
+    d, b, s = pair_distances_betas_time(1.33333, distances=dists)
+    np.testing.assert_array_equal(seg._data, oracle.segment_centrality(oracle.OracleGraph(ns), d, b, s,
+                                                                       closeness=closeness,
+                                                                       betweenness=betweenness, ns=ns))
