@@ -36,6 +36,31 @@ def check_quiet() -> bool:
 QUIET_MODE = check_quiet()
 
 
+def check_debug() -> bool:
+    """CITYSEER_DEBUG_MODE set to true or 1 (pysrc/cityseer/config.py:48-53)."""
+    return os.environ.get("CITYSEER_DEBUG_MODE", "").lower() in ("true", "1")
+
+
+DEBUG_MODE: bool = check_debug()
+SKIP_VALIDATION: bool = False
+
+
+def log_thresholds(distances=None, betas=None, minutes=None, min_threshold_wt: float = MIN_THRESH_WT,
+                   speed_m_s: float = SPEED_M_S) -> list[int]:
+    """Resolves and logs the thresholds, returning the distances (pysrc/cityseer/config.py:67-83)."""
+    import logging
+
+    from .common import pair_distances_betas_time
+
+    dists, betas_, secs = pair_distances_betas_time(speed_m_s, distances, betas, minutes,
+                                                    min_threshold_wt=min_threshold_wt)
+    log = logging.getLogger(__name__)
+    log.info("Metrics computed for:")
+    for d, b, t in zip(dists, betas_, secs):
+        log.info(f"Distance: {d}m, Beta: {round(b, 5)}, Walking Time: {t / 60} minutes.")
+    return dists
+
+
 def wrap_progress(total: int, rust_struct, partial_func: Callable, desc: str | None = None):
     """Runs partial_func on a worker thread and polls rust_struct.progress(), re-raising worker
     exceptions (pysrc/cityseer/config.py:96-130).  Progress is reported when the call returns."""

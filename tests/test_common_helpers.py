@@ -56,3 +56,14 @@ def test_avg_distances_and_clipped_curves():
                     assert np.isclose(got, 1.0 if dd <= tol else np.exp(-b * dd), atol=ATOL, rtol=RTOL)
     with pytest.raises(ValueError, match=r"\[0, 1\]"):
         rustalgos.clipped_beta_wt(0.01, 1.5, 10.0)
+
+
+def test_config_helpers():
+    """pysrc/cityseer/config.py:21-83: column keys, debug flag, threshold logging."""
+    from cityseer_gb300 import config
+
+    assert config.prep_gdf_key("density", 400) == "cc_density_400"
+    assert config.prep_gdf_key("harmonic", 800, angular=True) == "cc_harmonic_800_ang"
+    assert config.prep_gdf_key("beta", 200, weighted=False) == "cc_beta_200_nw"
+    assert config.log_thresholds(betas=[0.01, 0.005]) == [400, 800]
+    assert isinstance(config.DEBUG_MODE, bool)
