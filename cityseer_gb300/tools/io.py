@@ -109,3 +109,28 @@ def network_structure_from_gpd(nodes_gdf, edges_gdf) -> NetworkStructure:
     ns.validate()
     ns.build_edge_rtree()
     return ns
+
+
+def nx_from_cityseer_geopandas(nodes_gdf, edges_gdf) -> nx.MultiGraph:
+    """The inverse of network_structure_from_nx's frames (pysrc/cityseer/tools/io.py:1431-1501): nodes
+    with x, y, live, weight (and z), edges keyed by (start, end, edge_idx) with their impedance and
+    geometry, and every cc_* metric column copied onto the nodes.  Accepts GeoDataFrames or the dicts
+    of columns this package returns."""
+    g = nx.MultiGraph()
+    recs = list(_records(nodes_gdf))
+    for rec in recs:
+        kw = {"x": rec["x"], "y": rec["y"], "live": rec.get("live", True), "weight": rec.get("weight", 1)}
+        z = rec.get("z")
+        if z is not None and not (isinstance(z, float) and z != z):
+            kw["z"] = z
+        g.add_node(str(rec["index"]), **kw)
+    for rec in _records(edges_gdf):
+        a, b, k = str(rec["nx_start_node_key"]), str(rec["nx_end_node_key"]), rec["edge_idx"]
+        if not g.has_edge(a, b, k):
+            extra = {"total_bearing": rec["total_bearing"]} if "total_bearing" in rec else {}
+            g.add_edge(a, b, k, imp_factor=rec["imp_factor"], geom=rec["geom"], **extra)
+    cols = [c for c in (nodes_gdf.columns if hasattr(nodes_gdf, "columns") else nodes_gdf) if str(c).startswith("cc_")]
+    for c in cols:
+        for rec in recs:
+            g.nodes[str(rec["index"])][c] = rec[c]
+    return g

@@ -40,3 +40,19 @@ def test_missing_columns_are_reported():
         io.network_structure_from_gpd({k: v for k, v in nodes.items() if k != "weight"}, edges)
     with pytest.raises(ValueError, match="edges GDF: imp_factor"):
         io.network_structure_from_gpd(nodes, {k: v for k, v in edges.items() if k != "imp_factor"})
+
+
+def test_frames_back_to_networkx_with_metrics():
+    """network_structure_from_nx -> frames (+ a cc_* column) -> nx_from_cityseer_geopandas -> the same
+    graph, and the ingest of that graph gives the same store."""
+    g = _grid()
+    nodes, edges, ns = io.network_structure_from_nx(g)
+    nodes["cc_density_400"] = np.arange(len(nodes["index"]), dtype=float)
+    g2 = io.nx_from_cityseer_geopandas(nodes, edges)
+    assert sorted(g2.nodes) == sorted(g.nodes) and g2.number_of_edges() == g.number_of_edges()
+    for i, key in enumerate(nodes["index"]):
+        assert g2.nodes[key]["cc_density_400"] == i
+        assert g2.nodes[key]["live"] == g.nodes[key]["live"]
+    ns2 = io.network_structure_from_nx(g2)[2]
+    for k, v in ns.arrays().items():
+        np.testing.assert_array_equal(np.asarray(v), np.asarray(ns2.arrays()[k]), err_msg=k)
