@@ -105,3 +105,18 @@ def test_diamond_edge_payloads(dual):
                                        want[key], atol=0.01, rtol=1e-4, err_msg=str(key))
             seen += 1
     assert seen == len(want)
+
+
+def test_bearing_and_angle_helpers():
+    """The geometry helpers behind edge bearings and angle sums, on the reference's known answers
+    (tests/tools/test_util.py:14-86)."""
+    from cityseer_gb300.graph import _bearing, _coords_angle, cumulative_angle
+
+    for b, want in (((1, 0), 0), ((1, 1), 45), ((0, 1), 90), ((-1, 0), 180), ((-1, -1), -135), ((0, -1), -90),
+                    ((1, -1), -45)):
+        assert _bearing((0, 0), b) == want
+    for coords, want in (([[0, 0], [1, 0], [2, 0]], 0), ([[0, 0], [1, 0], [2, 1]], 45),
+                         ([[0, 0], [1, 0], [1, 1]], 90), ([[0, 0], [1, 0], [0, 1]], 135)):
+        assert np.isclose(_coords_angle(*coords), want) and np.isclose(_coords_angle(*coords[::-1]), want)
+        assert np.isclose(cumulative_angle(coords), want)
+    assert np.isclose(cumulative_angle([[0, 0], [1, 0], [1, 1], [2, 1]]), 180)
