@@ -42,12 +42,26 @@ class _Result:
 
     def __init__(self, distances, node_keys_py, node_indices, data: np.ndarray):
         self.distances = list(distances)
-        self.node_keys_py = list(node_keys_py)
-        self.node_indices = list(node_indices)
+        self._keys = node_keys_py
+        self._idx = np.asarray(node_indices, dtype=np.int64)
         self._data = data  # [M][K][node_bound] f64
-        self._idx = np.asarray(self.node_indices, dtype=np.int64)
+        self._keys_list: list | None = None
+        self._idx_list: list[int] | None = None
         self.reachability_totals: list[int] = []
         self.sampled_source_count = 0
+
+    # the key and index lists are built on first access (large graphs: a few ms each)
+    @property
+    def node_keys_py(self) -> list:
+        if self._keys_list is None:
+            self._keys_list = list(self._keys)
+        return self._keys_list
+
+    @property
+    def node_indices(self) -> list[int]:
+        if self._idx_list is None:
+            self._idx_list = self._idx.tolist()
+        return self._idx_list
 
     def _load_compact(self, m: int) -> dict[int, np.ndarray]:
         return {d: self._data[m, i][self._idx].copy() for i, d in enumerate(self.distances)}
@@ -133,7 +147,7 @@ class SourcePlan:
 def prepare_source_sampling(ns, sample_probability, sampling_weights, random_seed, source_indices) -> SourcePlan:
     nb = ns.node_bound()
     nc = ns.node_count()
-    node_indices = np.asarray(ns.node_indices(), dtype=np.int64)
+    node_indices = ns._node_index_array()
     a = ns.arrays()
     live = a["live"][:nb].astype(bool)
     weight = a["weight"][:nb]
@@ -242,7 +256,7 @@ def estimate_reach(ns, csr, speed: float, max_seconds: int, n_samples: int = 48)
     hit = ns._cache.get(key)
     if hit is not None:
         return hit
-    idx = np.asarray(ns.node_indices(), np.int64)
+    idx = ns._node_index_array()
     if len(idx) == 0:
         return 1
     pick = idx[np.linspace(0, len(idx) - 1, min(n_samples, len(idx))).astype(np.int64)]
@@ -371,13 +385,12 @@ def finish_shortest(ns, dists, sp: SourcePlan, data: np.ndarray, reach_tot: np.n
                     track: bool) -> CentralityShortestResult:
     """Post-scale of betweenness for source subsets (rust/src/centrality.rs:1852-1868) and the
     result object of centrality_shortest."""
-    node_indices = ns.node_indices()
+    node_indices = ns._node_index_array()
     if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
         scale = sp.n_live / sp.n_sources
         if scale != 1.0:
-            idx = np.asarray(node_indices, np.int64)
-            data[5][:, idx] *= scale
-            data[6][:, idx] *= scale
+            data[5][:, node_indices] *= scale
+            data[6][:, node_indices] *= scale
     ns._progress = sp.n_sources
     res = CentralityShortestResult(dists, ns.node_keys_py(), node_indices, data)
     if track:
@@ -438,10 +451,10 @@ def betweenness_od_shortest(ns, od_matrix: OdMatrix, distances=None, betas=None,
     dists, bets, secs = pair_distances_betas_time(speed, distances, betas, minutes, min_threshold_wt)
     tol = validate_tolerance(tolerance)
     nb = ns.node_bound()
-    node_indices = ns.node_indices()
+    node_indices = ns._node_index_array()
     K = len(dists)
     ptr, dst, w = od_matrix.rows(nb)
-    idx = np.asarray(node_indices, np.int64)
+    idx = node_indices
     live = ns.arrays()["live"][:nb]
     has_row = ptr[1:] > ptr[:-1]
     proc = idx[(live[idx] == 1) & has_row[idx]].astype(np.int32)
@@ -527,7 +540,7 @@ def segment_centrality(ns, distances=None, betas=None, minutes=None, compute_clo
 
 def segment_sources(ns) -> np.ndarray:
     """The live nodes, in node-index order: segment centrality's sources (rust/src/centrality.rs:2190)."""
-    idx = np.asarray(ns.node_indices(), np.int64)
+    idx = ns._node_index_array()
     return idx[ns.arrays()["live"][idx] == 1].astype(np.int32)
 
 
@@ -567,7 +580,7 @@ def segment_rows(ns, process, dists, bets, secs, speed: float, closeness: bool, 
 
 
 def finish_segment(ns, dists, data: np.ndarray) -> CentralitySegmentResult:
-    node_indices = ns.node_indices()
+    node_indices = ns._node_index_array()
     ns._progress = len(node_indices)
     return CentralitySegmentResult(dists, ns.node_keys_py(), node_indices, data)
 

@@ -223,12 +223,11 @@ def finish_simplest(ns, dists, sp, data: np.ndarray, reach_tot: np.ndarray, betw
     """Post-scale (source subsets) and the result object of centrality_simplest."""
     from .centrality import CentralitySimplestResult
 
-    node_indices = ns.node_indices()
+    node_indices = ns._node_index_array()
     if betweenness and sp.is_source_indexed and sp.sample_probability is None and sp.n_sources > 0:
         scale = sp.n_live / sp.n_sources
         if scale != 1.0:
-            idx = np.asarray(node_indices, np.int64)
-            data[3][:, idx] *= scale
+            data[3][:, node_indices] *= scale
     ns._progress = sp.n_sources
     res = CentralitySimplestResult(dists, ns.node_keys_py(), node_indices, data)
     if track:

@@ -574,17 +574,28 @@ class NetworkStructure:
     def street_node_count(self) -> int:
         return int(((self._exists.view() == 1) & (self._transport.view() == 0)).sum())
 
+    def _node_index_array(self) -> np.ndarray:
+        """Indices of the existing nodes as a read-only int64 array, cached until the graph changes."""
+        c = self._cache.get("node_idx")
+        if c is None:
+            c = np.nonzero(self._exists.view())[0].astype(np.int64)
+            c.setflags(write=False)
+            self._cache["node_idx"] = c
+        return c
+
     def node_indices(self) -> list[int]:
-        return np.nonzero(self._exists.view())[0].tolist()
+        return self._node_index_array().tolist()
 
     def street_node_indices(self) -> list[int]:
         return np.nonzero((self._exists.view() == 1) & (self._transport.view() == 0))[0].tolist()
 
     def node_keys_py(self) -> list[Any]:
-        idx = np.nonzero(self._exists.view())[0]
-        if self._keys is None:
-            return idx.tolist()
-        return [self._keys[i] for i in idx]
+        c = self._cache.get("node_keys")
+        if c is None:
+            idx = self._node_index_array()
+            c = idx.tolist() if self._keys is None else [self._keys[i] for i in idx]
+            self._cache["node_keys"] = c
+        return list(c)
 
     @property
     def node_xs(self) -> list[float]:
