@@ -362,7 +362,7 @@ def run_gpu(args):
                         zip(("search", "sort", "replay", "closeness", "sigma", "backward", "reset"), ph)},
         "clocks": clk,
     }
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu:  # the CPU baseline is reported at N = 1 only
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(ns, dists, n_nodes, args.cpu_seconds).items()
                                 if k != "seconds"}
     if rank == 0:
