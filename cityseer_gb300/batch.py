@@ -52,7 +52,7 @@ class Batch:
                 wt, el = sp.src_wt, sp.eligible
             else:
                 a = ns.arrays()
-                idx = np.asarray(ns.node_indices(), np.int64)
+                idx = ns._node_index_array()
                 proc = idx[a["live"][idx] == 1].astype(np.int32)
                 wt = np.zeros(max(csr.n_bound, 1), np.float32)
                 el = np.zeros(max(csr.n_bound, 1), np.uint8)
@@ -201,13 +201,13 @@ class Batch:
                 if jb["betweenness"] and sp.is_source_indexed and sp.n_sources > 0:
                     sc = sp.n_live / sp.n_sources
                     if sc != 1.0:
-                        idx = np.asarray(ns.node_indices(), np.int64)
+                        idx = ns._node_index_array()
                         data[5][:, idx] *= sc
                         data[6][:, idx] *= sc
-                res = CentralityShortestResult(jb["d"], ns.node_keys_py(), ns.node_indices(), data)
+                res = CentralityShortestResult(jb["d"], ns.node_keys_py(), ns._node_index_array(), data)
                 if sp.is_source_indexed:
                     res.sampled_source_count = sp.sampled_count
             else:
-                res = CentralitySegmentResult(jb["d"], ns.node_keys_py(), ns.node_indices(), data)
+                res = CentralitySegmentResult(jb["d"], ns.node_keys_py(), ns._node_index_array(), data)
             out.append(res)
         return out
