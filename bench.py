@@ -124,11 +124,14 @@ def cpu_baseline(ns, dists, n_total: int, target_seconds: float, nthreads: int |
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
 
-    from cityseer_gb300 import common
-
-    d, b, s = common.pair_distances_betas_time(1.33333, distances=dists)
+    # thresholds from the oracle's own restatement of pair_distances_betas_time
+    # (rust/src/common.rs:239-270), so that this leg loads no code of the library it is compared with
+    d = [int(x) for x in dists]
+    b = oracle.betas_from_distances(d)
+    s = oracle.seconds_from_distances(d, 1.33333)
     og = oracle.OracleGraph(ns)
-    nthreads = nthreads or (os.cpu_count() or 1)
+    # rayon's pool in the reference runs on all cores but one (rust/src/lib.rs:21-33)
+    nthreads = nthreads or oracle.default_threads()
     plan = oracle.all_sources_plan(ns)
     allsrc = plan["sources"]
 
@@ -159,27 +162,38 @@ def cpu_baseline(ns, dists, n_total: int, target_seconds: float, nthreads: int |
     }
 
 
-def traffic_ratio():
-    """DRAM bytes per algorithmic byte of primal_kernel, from the committed ncu summary."""
-    p = ROOT / "profiles" / "primal_kernel_lattice160_shortest.md"
+def traffic_ratio(kernel: str = "primal_sync_kernel"):
+    """DRAM bytes per algorithmic byte of the timed kernel, from the ncu figures kept in
+    profiles/traffic.json (one capture of that kernel on a smaller lattice of the same recipe)."""
     try:
-        for line in p.read_text().splitlines():
-            if line.startswith("traffic_per_alg_byte:"):
-                return float(line.split(":")[1])
-    except OSError:
-        pass
-    return None
+        return float(json.loads((ROOT / "profiles" / "traffic.json").read_text())[kernel]["traffic_per_alg_byte"])
+    except (OSError, KeyError, ValueError, TypeError):
+        return None
 
 
 def flush_l2(buf):
     buf.add_(1.0)
 
 
+def loaded_native_libraries():
+    """Shared objects of this repository mapped into the process (from /proc/self/maps)."""
+    found = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if line.strip() else ""
+                if path.endswith(".so") and path.startswith(str(ROOT)):
+                    found.add(str(Path(path).relative_to(ROOT)))
+    except OSError:
+        pass
+    return sorted(found)
+
+
 def run_reference(args):
     ws, rank, _ = _dist_env()
     if rank != 0:
         return
-    ns, dists = build_workload(args.side)
+    ns, dists = build_workload(args.side)  # numpy graph store only: no device code is loaded
     n = ns.node_count()
     times = []
     for i in range(args.warmup + args.steps):
@@ -205,6 +219,7 @@ def run_reference(args):
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": times[-1]["cores"], "kind": times[-1]["kind"],
                          "sample": f"{len(times)} timed steps of: " + times[-1]["sample"]},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "native_libraries": loaded_native_libraries(),
     }
     print(json.dumps(line), flush=True)
 
@@ -307,8 +322,8 @@ def run_gpu(args):
         "unit": "GB/s",
         "frac": achieved / peak,
         "traffic": (traffic_ratio() * alg_bytes) if traffic_ratio() else None,
-        "traffic_note": "DRAM bytes per launch scaled from the 160x160 ncu capture "
-                        "(profiles/primal_kernel_lattice160_shortest.md) by algorithmic bytes",
+        "traffic_note": "DRAM bytes per launch: the ncu traffic per algorithmic byte of a smaller lattice "
+                        "(profiles/traffic.json) times this launch's algorithmic bytes",
         "peak_kind": peak_kind,
         "alg_bytes_per_launch": alg_bytes,
         "edges_relaxed": int(e_relax),

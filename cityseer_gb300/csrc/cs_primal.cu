@@ -1935,11 +1935,16 @@ cs_status cs_tree_shortest(const cs_primal_graph *g, int32_t n_queries, const in
 //  - All calls share the array and it keeps the previous call's contents; each call therefore
 //    re-initialises the state that must start clean.  Calls that overlap on the GPU (two streams,
 //    two host threads) race on the array: issue them one after another.
-//  - The first call on a device looks up the array's device address with cudaGetSymbolAddress
-//    while that device is current; make that first call before any stream capture begins.
+//  - Every call looks up the array's device address with cudaGetSymbolAddress while the
+//    caller's device and context are current, so the address always belongs to the context the
+//    call runs in (a context the host application created itself, or one re-created after
+//    cudaDeviceReset).  The lookup allocates nothing.
+//  - With lazy module loading (the CUDA default since 12.2) this file's device code, and with it
+//    the 64 MiB array, is loaded on the first use of any of its kernels or of the array on a
+//    device: if this entry point is that first use, the reservation happens inside the call.
+//    Callers that must not see it there make one call (of any entry point) while setting up,
+//    before the device's memory is handed to their pool and before any stream capture.
 // ==========================================================================================
-#include <mutex>
-
 namespace {
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
 }  // namespace
@@ -1947,23 +1952,12 @@ constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
 static __device__ __align__(256) unsigned char cs_noalloc_scratch[kNoAllocScratchBytes];
 
 namespace {
-std::mutex g_noalloc_mu;
-void *g_noalloc_ptr[128] = {};
-
 cs_status noalloc_scratch_address(void **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-    if (dev < 0 || dev >= 128) return fail(CS_ERR_ARG, "device ordinal out of range");
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, cs_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
-        if (!p) return fail(CS_ERR_CUDA, "static scratch has no device address");
-        g_noalloc_ptr[dev] = p;
-    }
-    *out = g_noalloc_ptr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, cs_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
+    if (!p) return fail(CS_ERR_CUDA, "static scratch has no device address");
+    *out = p;
     return CS_OK;
 }
 }  // namespace
@@ -2008,9 +2002,15 @@ extern "C" cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, co
     const Layout lay = layout(g->n_bound, slots, cap, P, L);
     plan.workspace_bytes = lay.total;
     cudaStream_t s = (cudaStream_t)stream;
-    // the array keeps whatever the previous call (or module load, which zeroes it) left there
+    // The array keeps whatever the previous call left there (another graph's dense state or
+    // compact scratch, or the remains of a call that failed midway), and this call's regions sit
+    // at offsets set by its own node bound and threshold count.  Put every region that must start
+    // clean into its clean state: the header, the dense per-slot state and the [3][K][n_bound]
+    // closeness bucket.  The compact per-source arrays are written before they are read.
     e = cudaMemsetAsync(ws, 0, 256, s);
     if (e != cudaSuccess) return cuda_fail(e, "static scratch header reset");
+    e = cudaMemsetAsync((char *)ws + lay.bucket_off, 0, sizeof(double) * 3 * (size_t)q->k * (size_t)g->n_bound, s);
+    if (e != cudaSuccess) return cuda_fail(e, "static scratch bucket reset");
     st = reset_dense((char *)ws + lay.dense_off, lay.dense_stride, g->n_bound, slots, s);
     if (st != CS_OK) return st;
     return run_primal(g, q, &plan, ws, kNoAllocScratchBytes, out, stream, cs::MODE_SHORTEST, 0, nullptr, nullptr,

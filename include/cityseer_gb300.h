@@ -206,12 +206,15 @@ cs_status cs_centrality_shortest(const cs_primal_graph *g, const cs_query *q, co
  * when they call (a host application that owns all device memory through its own pool, a plugin
  * with a fixed memory budget, code that must not block or fail on an allocation).  It has no
  * counterpart in the reference: the Rust code allocates per call.  Its scratch is one static 64 MiB
- * device array reserved when the library's CUDA module loads; no workspace is passed and nothing
- * is allocated.  Same inputs, outputs and results as cs_centrality_shortest.  Graphs whose single
- * search needs more than 64 MiB of scratch are rejected with CS_ERR_ARG.  All calls share the array:
- * calls that overlap on the GPU race, so issue them one after another.  The first call on each
- * device looks up the array's address (cudaGetSymbolAddress) with that device current; make it
- * before any stream capture. */
+ * device array, held by every GPU that loads the library's device code until the process exits;
+ * no workspace is passed and nothing is allocated.  Same inputs, outputs and results as
+ * cs_centrality_shortest.  Graphs whose single search needs more than 64 MiB of scratch are
+ * rejected with CS_ERR_ARG.  All calls share the array and each call clears what must start at
+ * zero; calls that overlap on the GPU race, so issue them one after another.  Every call looks up
+ * the array's address (cudaGetSymbolAddress) in the caller's current device and context.  Under
+ * lazy module loading (the CUDA default) the device code, and with it the array, is loaded on the
+ * first call into this library on a device: make one call while setting up, before the device's
+ * memory goes to the caller's pool and before any stream capture. */
 cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, const cs_query *q, cs_outputs out, void *stream);
 
 /* Replaces NetworkStructure.centrality_simplest (rust/src/centrality.rs:1880-2132) on a dual graph.

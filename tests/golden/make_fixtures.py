@@ -6,7 +6,7 @@ Reads (as text, with the ast module; nothing from the reference is imported or e
   tests/rustalgos/test_centrality.py  golden vectors asserted in test_local_centrality_all and the
                                       expected paths of test_shortest_path_trees
 
-Usage: python tests/golden/make_fixtures.py [REFERENCE_ROOT]
+Usage: python tests/golden/make_fixtures.py REFERENCE_ROOT   (the cityseer-api source tree)
 """
 from __future__ import annotations
 
@@ -133,4 +133,6 @@ def main(ref: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_fixtures.py <cityseer-api source root>")
+    main(Path(sys.argv[1]))

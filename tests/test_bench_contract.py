@@ -24,3 +24,7 @@ def test_reference_arm_line():
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert line["config"]["workload"]
+    # the reference arm times the oracle alone: the library under test is never loaded
+    libs = line["native_libraries"]
+    assert any(x.endswith("libcs_oracle.so") for x in libs), libs
+    assert not any("libcsgpu" in x for x in libs), libs
