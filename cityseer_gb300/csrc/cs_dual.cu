@@ -51,10 +51,11 @@ struct DSlot {
     int32_t *vb;
     uint32_t *rk;  // [cap] sorted route bits
     int32_t *ord;  // [cap] sorted states
-    float *rB, *sB, *sig, *nbR, *nbS;  // [cap] replayed route, seconds, sigma; node best route/seconds
+    float *rB, *sB, *nbR, *nbS;  // [cap] replayed route and seconds; node best route/seconds
+    double *sig;  // [cap] path counts (f64, as the reference's sigma)
     uint8_t *np;
     int32_t *pr;  // [cap * DPM]
-    float *dl;    // [cap * K]
+    double *dl;   // [cap * K] dependencies (f64, as the reference's delta)
     int32_t *hp;  // exact-mode heap: [2 cap] (route bits, state) pairs interleaved
 };
 
@@ -62,10 +63,11 @@ __host__ __device__ inline size_t compact_bytes_d(size_t cap, int K) {
     size_t b = 0;
     b += 4 * al256(cap * 4);        // rl kb vb ord
     b += 3 * al256(cap * 32);       // qa qb qf
-    b += 6 * al256(cap * 4);        // rk rB sB sig nbR nbS
+    b += 5 * al256(cap * 4);        // rk rB sB nbR nbS
+    b += al256(cap * 8);            // sig
     b += al256(cap);                // np
     b += al256(cap * 4 * DPM);      // pr
-    b += al256(cap * 4 * (size_t)K);  // dl
+    b += al256(cap * 8 * (size_t)K);  // dl
     b += al256(cap * 16);           // hp
     return b;
 }
@@ -88,12 +90,12 @@ __host__ __device__ inline DSlot dslot(char *dense, size_t dense_stride, char *c
     s.rk = (uint32_t *)(c + o); o += al256(cap * 4);
     s.rB = (float *)(c + o); o += al256(cap * 4);
     s.sB = (float *)(c + o); o += al256(cap * 4);
-    s.sig = (float *)(c + o); o += al256(cap * 4);
+    s.sig = (double *)(c + o); o += al256(cap * 8);
     s.nbR = (float *)(c + o); o += al256(cap * 4);
     s.nbS = (float *)(c + o); o += al256(cap * 4);
     s.np = (uint8_t *)(c + o); o += al256(cap);
     s.pr = (int32_t *)(c + o); o += al256(cap * 4 * DPM);
-    s.dl = (float *)(c + o); o += al256(cap * 4 * (size_t)K);
+    s.dl = (double *)(c + o); o += al256(cap * 8 * (size_t)K);
     s.hp = (int32_t *)(c + o); o += al256(cap * 16);
     return s;
 }
@@ -589,21 +591,22 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
         while (done != FULL) {
             const bool ready = !mine && ((pm & ~done) == 0u);
             if (ready) {
-                float route, secs, sg;
+                float route, secs;
+                double sg;
                 int np = 0;
                 if (is_src) {
                     route = 0.0f;
                     secs = 0.0f;
-                    sg = 1.0f;
+                    sg = 1.0;
                 } else {
                     gather_doffers(p, s, V, i, R, o, bad);
                     const unsigned pmask = dreplay(p, o, route, secs);
-                    sg = 0.0f;
+                    sg = 0.0;
 #pragma unroll
                     for (int j = 0; j < DPM; j++) {
                         if ((pmask >> j) & 1u) {
                             s.pr[(size_t)i * DPM + np] = o.pos[j];
-                            sg = __fadd_rn(sg, s.sig[o.pos[j]]);
+                            sg = __dadd_rn(sg, s.sig[o.pos[j]]);
                             np++;
                         }
                     }
@@ -702,9 +705,9 @@ __device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, in
     }
     if (!p.betweenness) return;
     // backward sweep over states, K lanes (rust/src/centrality.rs:2036-2096)
-    float *dl = s.dl;
+    double *dl = s.dl;
     for (int i = lane; i < R; i += 32)
-        for (int q = 0; q < K; q++) dl[(size_t)i * K + q] = 0.0f;
+        for (int q = 0; q < K; q++) dl[(size_t)i * K + q] = 0.0;
     __syncwarp();
     const bool unit_wt = (wt == 1.0f);
     const double wtd = (double)wt;
@@ -731,52 +734,55 @@ __device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, in
             if (ready) {
                 const int V = s.ord[i];
                 const int v = V >> 1;
-                const float sw = s.sig[i];
+                const double sw = s.sig[i];
                 const float secs = s.sB[i];
                 const float route = s.rB[i];
                 const float best = s.nbR[i], bsecs = s.nbS[i];
                 // sibling state for the seed split
                 const uint32_t as = s.aux[V ^ 1];
                 const int isib = (as != 0u && as <= (uint32_t)R) ? (int)as - 1 : -1;
-                const float sig_sib = isib >= 0 ? s.sig[isib] : 0.0f;
+                const double sig_sib = isib >= 0 ? s.sig[isib] : 0.0;
                 const float secs_sib = isib >= 0 ? s.sB[isib] : 0.0f;
                 const float route_sib = isib >= 0 ? s.rB[isib] : 0.0f;
-                const float pair = __ldg(&p.eligible[v]) ? 0.5f : 1.0f;
-                float fr[DPM];
+                const double pair = __ldg(&p.eligible[v]) ? 0.5 : 1.0;
+                // predecessor factors sigma_v / sigma_w in f64 (1 exactly when the counts agree)
+                double fr[DPM];
 #pragma unroll
                 for (int r = 0; r < DPM; r++) {
-                    fr[r] = 0.0f;
+                    fr[r] = 0.0;
                     if (r < np) {
-                        const float sv = s.sig[pl[r]];
-                        fr[r] = (sv == sw) ? 1.0f : __fdiv_rn(sv, sw);
+                        const double sv = s.sig[pl[r]];
+                        fr[r] = (sv == sw) ? 1.0 : __ddiv_rn(sv, sw);
                     }
                 }
-                float *dli = dl + (size_t)i * K;
+                double *dli = dl + (size_t)i * K;
                 for (int k = 0; k < K; k++) {
                     const float thr = p.sk[k];
                     if (!(secs <= thr)) continue;  // include_state: agg_seconds <= threshold
-                    if (sw == 0.0f) continue;
-                    float seed = 0.0f;
+                    if (sw == 0.0) continue;
+                    double seed = 0.0;
                     if (v != src && isfinite(best) && isfinite(bsecs) && bsecs <= thr) {
-                        const bool me = sw != 0.0f && secs <= thr && route <= __fmul_rn(best, one_tol);
-                        const bool sib = isib >= 0 && sig_sib != 0.0f && secs_sib <= thr &&
+                        const bool me = sw != 0.0 && secs <= thr && route <= __fmul_rn(best, one_tol);
+                        const bool sib = isib >= 0 && sig_sib != 0.0 && secs_sib <= thr &&
                                          route_sib <= __fmul_rn(best, one_tol);
                         if (me) {
-                            const float tot = sib ? __fadd_rn(sw, sig_sib) : sw;
-                            seed = __fmul_rn(pair, __fdiv_rn(sw, tot));
+                            // the seed splits the pair count over the best states by sigma
+                            // (rust/src/centrality.rs:2066-2077), in f64
+                            const double tot = sib ? __dadd_rn(sw, sig_sib) : sw;
+                            seed = (tot == sw) ? pair : __dmul_rn(pair, __ddiv_rn(sw, tot));
                         }
                     }
-                    const float dep = __fadd_rn(seed, __ldcg(&dli[k]));
-                    if (dep == 0.0f) continue;
+                    const double dep = __dadd_rn(seed, __ldcg(&dli[k]));
+                    if (dep == 0.0) continue;
 #pragma unroll
                     for (int r = 0; r < DPM; r++) {
-                        if (r >= np || fr[r] == 0.0f) continue;
-                        atomicAdd(&dl[(size_t)pl[r] * K + k], __fmul_rn(fr[r], dep));
+                        if (r >= np || fr[r] == 0.0) continue;
+                        atomicAdd(&dl[(size_t)pl[r] * K + k], fr[r] == 1.0 ? dep : __dmul_rn(fr[r], dep));
                     }
                     if (v == src) continue;
-                    const float credit = __fadd_rn(dep, -seed);
-                    if (credit > 0.0f)
-                        atomicAdd(p.out + ((size_t)3 * K + k) * N + v, unit_wt ? f2d(credit) : f2d(credit) * wtd);
+                    const double credit = __dadd_rn(dep, -seed);
+                    if (credit > 0.0)
+                        atomicAdd(p.out + ((size_t)3 * K + k) * N + v, unit_wt ? credit : __dmul_rn(credit, wtd));
                 }
                 mine = true;
             }

@@ -146,6 +146,10 @@ struct PrimalParams {
 //    its distance still equals the node's, so no flag atomics are needed to de-duplicate.
 // ------------------------------------------------------------------------------------------
 constexpr int DEG_FAST = 8;  // edges per node loaded together; higher degrees loop
+// Backward sweep: predecessors per lane kept in shared memory (row and f64 factor); a node's
+// further predecessors (high-degree graphs) are read from the per-source scratch.
+constexpr int BW_COLS = 8;
+__host__ __device__ constexpr int bw_cols(int pm) { return pm < BW_COLS ? pm : BW_COLS; }
 
 __device__ __forceinline__ void push_entries(bool first, int route, int v, float c, int &R, int &nnext, int &nfar,
                                              int cap, int qcap, const SlotPtrs &s, uint2 *nxt, unsigned lt) {
@@ -519,7 +523,7 @@ __device__ __forceinline__ float od_weight(const PrimalParams &p, int src, int v
 // pair counts (rust/src/centrality.rs:2495-2507), source weight 1, written to rows 0 and 1.
 template <int PM, int SYNC, bool OD = false>
 CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R, long long *ph,
-                                    int *cnt, int *bw_pl, float *bw_fr) {
+                                    int *cnt, int *bw_pl, double *bw_fr) {
     const int lane = lane_id();
     bool failed = false;
     long long tph = clock64();
@@ -533,13 +537,13 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     for (int q = lane; q < 2 * MAXK; q += 32) cnt[q] = 0;
     __syncwarp();
     // --- one pass over out-edges in settle order, 32 nodes at a time: circuit-rank counts, the
-    // predecessor replay and, with betweenness, sigma (f32 path counts) of the chunk: a node is ready
-    // once its in-chunk predecessors are done.  The same pass zeroes each node's dependency lanes
-    // for the backward sweep.
+    // predecessor replay and, with betweenness, sigma (f64 path counts, as the reference's
+    // BrandesTraversalState.sigma) of the chunk: a node is ready once its in-chunk predecessors are
+    // done.  The same pass zeroes each node's dependency lanes for the backward sweep.
     bool bad = false;
-    float *sig = (float *)s.sig;
-    const int L = p.L;  // 2K floats per node: [0,K) plain, [K,2K) beta-weighted
-    float *dl = (float *)s.dl;
+    double *sig = s.sig;
+    const int L = p.L;  // 2K f64 lanes per node: [0,K) plain, [K,2K) beta-weighted
+    double *dl = s.dl;
     for (int base = 0; base < R; base += 32) {
         const int i = base + lane;
         const bool act = i < R;
@@ -587,12 +591,12 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
         while (done != FULL) {
             const bool ready = !mine && ((blk & ~done) == 0u);
             if (ready) {
-                float sg = (i == 0) ? 1.0f : 0.0f;
+                double sg = (i == 0) ? 1.0 : 0.0;
 #pragma unroll
                 for (int j = 0; j < PM; j++)
-                    if ((pm >> j) & 1u) sg = fadd(sg, sig[nb.pos[j]]);
+                    if ((pm >> j) & 1u) sg = __dadd_rn(sg, sig[nb.pos[j]]);
                 sig[i] = sg;
-                for (int q = 0; q < 2 * K; q++) dl[(size_t)i * L + q] = 0.0f;
+                for (int q = 0; q < 2 * K; q++) dl[(size_t)i * L + q] = 0.0;
                 mine = true;
             }
             __syncwarp();
@@ -658,12 +662,14 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     // (sigma was built in the replay pass)
     phase_mark(ph, 4, tph);
     // --- backward Brandes sweep, all K thresholds in one pass (rust/src/centrality.rs:823-873,
-    // 1782-1835).  Dependencies accumulate in f32: for sources whose paths are unique (sigma == 1)
-    // they are half-integers and exact; otherwise they carry f32 rounding (well inside 1e-5).
+    // 1782-1835), in the reference's f64: path counts, predecessor factors sigma_v / sigma_w, seeds
+    // (pair count, and pair count * exp(-beta * cost) with the product and exp in f64) and
+    // dependencies.
     __syncwarp();
     const bool unit_wt = (wt == 1.0f);
     const double wtd = (double)wt;
     const int nchunks = failed ? 0 : (Rb + 31) / 32;
+    constexpr int BW = (PM < BW_COLS) ? PM : BW_COLS;  // predecessors kept in this lane's shared column
     for (int ch = nchunks - 1; ch >= 0; ch--) {
         const int base = ch * 32;
         const int i = base + lane;
@@ -683,45 +689,55 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
             if (ready) {
                 const int v = s.ord[i];
                 const float cost = route_cost(s.sd[i], p.speed);
-                const float sw = sig[i];
-                float pair;
-                if constexpr (OD) pair = od_weight(p, src, v);
-                else pair = __ldg(&p.eligible[v]) ? 0.5f : 1.0f;
-                // predecessor rows and sigma fractions go to this lane's shared-memory column, so
-                // that the push loop below is a plain (not unrolled) loop over the np predecessors
+                const double sw = sig[i];
+                double pair;
+                if constexpr (OD) pair = (double)od_weight(p, src, v);
+                else pair = __ldg(&p.eligible[v]) ? 0.5 : 1.0;
+                // predecessor rows and factors go to this lane's shared-memory column, so that the
+                // push loop below is a plain (not unrolled) loop over the np predecessors
 #pragma unroll
-                for (int r = 0; r < PM; r++) {
+                for (int r = 0; r < BW; r++) {
                     if (r < np) {
-                        const float sv = sig[pl[r]];
+                        const double sv = sig[pl[r]];
                         bw_pl[r * 32 + lane] = pl[r];
-                        bw_fr[r * 32 + lane] = (sv == sw) ? 1.0f : __fdiv_rn(sv, sw);
+                        bw_fr[r * 32 + lane] = (sv == sw) ? 1.0 : __ddiv_rn(sv, sw);
                     }
                 }
-                float *dli = dl + (size_t)i * L;
+                double *dli = dl + (size_t)i * L;
                 const int k0 = first_k(p, cost);
+                const double cost_d = (double)cost;
                 for (int k = k0; k < K; k++) {
-                    if (sw == 0.0f) break;
-                    const float seed = (i == 0) ? 0.0f : pair;
-                    const float seedb = (i == 0) ? 0.0f : fmul(pair, expf(fmul(-p.beta[k], cost)));
-                    const float dep = fadd(seed, __ldcg(&dli[k]));
-                    const float depb = fadd(seedb, __ldcg(&dli[K + k]));
-                    if (dep == 0.0f && depb == 0.0f) continue;
+                    if (sw == 0.0) break;
+                    const double seed = (i == 0) ? 0.0 : pair;
+                    const double seedb = (i == 0) ? 0.0 : __dmul_rn(pair, exp(__dmul_rn(-(double)p.beta[k], cost_d)));
+                    const double dep = __dadd_rn(seed, __ldcg(&dli[k]));
+                    const double depb = __dadd_rn(seedb, __ldcg(&dli[K + k]));
+                    if (dep == 0.0 && depb == 0.0) continue;
 #pragma unroll 1
                     for (int r = 0; r < np; r++) {
-                        const float f = bw_fr[r * 32 + lane];
-                        if (f == 0.0f) continue;
-                        float *pd = dl + (size_t)bw_pl[r * 32 + lane] * L;
-                        atomicAdd(&pd[k], fmul(f, dep));
-                        atomicAdd(&pd[K + k], fmul(f, depb));
+                        int q;
+                        double f;
+                        if (r < BW) {
+                            q = bw_pl[r * 32 + lane];
+                            f = bw_fr[r * 32 + lane];
+                        } else {  // beyond the shared column (high-degree graphs): from the scratch
+                            q = s.pr[(size_t)i * P + r];
+                            const double sv = sig[q];
+                            f = (sv == sw) ? 1.0 : __ddiv_rn(sv, sw);
+                        }
+                        if (f == 0.0) continue;
+                        double *pd = dl + (size_t)q * L;
+                        atomicAdd(&pd[k], f == 1.0 ? dep : __dmul_rn(f, dep));
+                        atomicAdd(&pd[K + k], f == 1.0 ? depb : __dmul_rn(f, depb));
                     }
                     if (v == src) continue;
-                    const float credit = __fadd_rn(dep, -seed);
-                    const float creditb = __fadd_rn(depb, -seedb);
+                    const double credit = __dadd_rn(dep, -seed);
+                    const double creditb = __dadd_rn(depb, -seedb);
                     constexpr size_t row_b = OD ? 0 : 5;
-                    if (credit > 0.0f)
-                        atomicAdd(p.out + (row_b * K + k) * N + v, unit_wt ? f2d(credit) : f2d(credit) * wtd);
-                    if (creditb > 0.0f)
-                        atomicAdd(p.out + ((row_b + 1) * K + k) * N + v, unit_wt ? f2d(creditb) : f2d(creditb) * wtd);
+                    if (credit > 0.0)
+                        atomicAdd(p.out + (row_b * K + k) * N + v, unit_wt ? credit : __dmul_rn(credit, wtd));
+                    if (creditb > 0.0)
+                        atomicAdd(p.out + ((row_b + 1) * K + k) * N + v, unit_wt ? creditb : __dmul_rn(creditb, wtd));
                 }
                 mine = true;
             }
@@ -1017,7 +1033,7 @@ CS_PHASE_INLINE __device__ void tree_rows(const PrimalParams &p, const SlotPtrs 
 // instruction-cache footprint, to what that mode runs); -1 dispatches on p.mode at run time.
 template <int PM, int MODE>
 __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs &s, int li, int src, uint32_t *hist,
-                                           int *cnt, int *bw_pl, float *bw_fr, long long *ph, long long &relaxed,
+                                           int *cnt, int *bw_pl, double *bw_fr, long long *ph, long long &relaxed,
                                            long long &settled) {
     const int lane = lane_id();
     long long t0 = clock64();
@@ -1098,8 +1114,8 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
     __shared__ int cnt_all[8][2 * MAXK];
     __shared__ long long ph_all[8][8];
     // backward sweep: each lane's predecessor rows and sigma fractions (column-major per warp)
-    __shared__ int bw_pl_all[8][PM * 32];
-    __shared__ float bw_fr_all[8][PM * 32];
+    __shared__ int bw_pl_all[8][bw_cols(PM) * 32];
+    __shared__ double bw_fr_all[8][bw_cols(PM) * 32];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
@@ -1135,8 +1151,8 @@ __global__ void __launch_bounds__(WPB * 32, MINB) primal_sync_kernel(const Prima
     __shared__ uint32_t hist_all[WPB][256];
     __shared__ int cnt_all[WPB][2 * MAXK];
     __shared__ long long ph_all[WPB][8];
-    __shared__ int bw_pl_all[WPB][PM * 32];
-    __shared__ float bw_fr_all[WPB][PM * 32];
+    __shared__ int bw_pl_all[WPB][bw_cols(PM) * 32];
+    __shared__ double bw_fr_all[WPB][bw_cols(PM) * 32];
     __shared__ long long blk_base[WPB / GW];
     __shared__ unsigned blk_err[WPB / GW];
     const int lane = lane_id();
@@ -1263,8 +1279,8 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
     __shared__ int cnt_all[8][2 * MAXK];
     __shared__ long long ph_all[8][8];
     // backward sweep: each lane's predecessor rows and sigma fractions (column-major per warp)
-    __shared__ int bw_pl_all[8][PM * 32];
-    __shared__ float bw_fr_all[8][PM * 32];
+    __shared__ int bw_pl_all[8][bw_cols(PM) * 32];
+    __shared__ double bw_fr_all[8][bw_cols(PM) * 32];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
@@ -1308,8 +1324,8 @@ __global__ void __launch_bounds__(256, MINB) batch_sync_kernel(const PrimalParam
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][2 * MAXK];
     __shared__ long long ph_all[8][8];
-    __shared__ int bw_pl_all[8][PM * 32];
-    __shared__ float bw_fr_all[8][PM * 32];
+    __shared__ int bw_pl_all[8][bw_cols(PM) * 32];
+    __shared__ double bw_fr_all[8][bw_cols(PM) * 32];
     __shared__ long long blk_base;
     __shared__ unsigned blk_err;
     const int lane = lane_id();

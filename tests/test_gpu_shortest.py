@@ -12,10 +12,10 @@ ROWS = ("node_density", "node_farness", "node_cycles", "node_harmonic", "node_be
 # Integer-valued sums are exact in any order.  Betweenness is a sum of half-integers when every
 # source's shortest paths are unique (sigma == 1), exact then (bit-exact test on tie-free sources
 # below); where the reference's 1e-4 near-tie rule splits paths (sigma > 1) the dependencies are
-# non-dyadic fractions that the kernel carries in f32, so they agree to ~1e-7 (checked to 1e-6, the
-# contract being 1e-5 relative for float sums).
+# non-dyadic fractions.  The kernel carries path counts, factors, seeds and dependencies in f64 as
+# the reference does, so only the summation order differs: 1e-9 relative.
 EXACT = {"node_density", "node_cycles"}
-RTOL_ORDER = 1e-6
+RTOL_ORDER = 1e-9
 
 
 def _compare(ns, res, ref, dists, exact_rows=EXACT, what="", betw_exact=False):
@@ -164,7 +164,7 @@ def test_capacity_overflow_is_retried_inside_the_call():
     idx = np.asarray(ns.node_indices())
     for m, name in enumerate(ROWS):
         for i, dist in enumerate(d):
-            np.testing.assert_allclose(got[m, i][idx], getattr(want, name)[dist], rtol=1e-6, atol=1e-9)
+            np.testing.assert_allclose(got[m, i][idx], getattr(want, name)[dist], rtol=1e-9, atol=1e-9)
 
 
 @pytest.mark.gpu

@@ -41,7 +41,7 @@ def _run(ns, dists, exact=False, **kw):
             if name == "node_density":
                 np.testing.assert_array_equal(got[dist], want, err_msg=f"{name}[{dist}]")
             elif name == "node_betweenness":
-                assert_close_sums(got[dist], want, rtol=1e-6, atol=1e-9, what=f"{name}[{dist}]")
+                assert_close_sums(got[dist], want, rtol=1e-9, atol=1e-9, what=f"{name}[{dist}]")  # f64 sigma and dependencies
             else:
                 assert_close_sums(got[dist], want, what=f"{name}[{dist}]")
     return res
