@@ -93,6 +93,7 @@ class Plan(C.Structure):
         ("variant", C.c_int32),
         ("max_degree", C.c_int32),
         ("n_bound", C.c_int32),
+        ("cta_blocks", C.c_int32),
         ("workspace_bytes", C.c_size_t),
     ]
 
@@ -225,6 +226,7 @@ SIGNATURES = {
         C.c_int32,
         [C.POINTER(PrimalGraph), C.POINTER(Query), Outputs, _ptr],
     ),
+    "cs_debug_seed_exp": (C.c_int32, [_ptr, _ptr, _ptr, _ptr, C.c_int64, _ptr]),
 }
 
 _lib = None

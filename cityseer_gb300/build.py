@@ -19,9 +19,9 @@ BUILD_DIR = PKG_DIR / "_build"
 LIB_PATH = BUILD_DIR / "libcsgpu.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CUDA_SOURCES = ["cs_primal.cu", "cs_dual.cu"]
+CUDA_SOURCES = ["cs_primal.cu", "cs_dual.cu", "cs_cta.cu"]
 CXX_SOURCES = ["cs_host.cpp"]
-HEADERS = ["cs_common.cuh", "cs_sort.cuh"]
+HEADERS = ["cs_common.cuh", "cs_sort.cuh", "cs_seed.cuh", "cs_cta.cuh"]
 
 
 def _nvcc() -> str:

@@ -66,6 +66,17 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
+// f32 -> f64 by integer ops: keeps the conversion off GB300's narrow FP64 pipe.  Exact for
+// every finite f32; zeros, subnormals, infinities and NaN take the hardware conversion.
+__device__ __forceinline__ double f2d(float x) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    const uint32_t lo = b << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 __device__ __forceinline__ void raise_err(WsHeader *h, unsigned code, unsigned where) {
     if (atomicCAS(&h->err, 0u, code) == 0u) h->err_where = where;
 }

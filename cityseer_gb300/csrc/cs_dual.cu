@@ -534,15 +534,6 @@ __device__ __forceinline__ void node_best(const DualParams &p, const DSlot &s, i
     }
 }
 
-__device__ __forceinline__ double f2d(float x) {
-    const uint32_t b = __float_as_uint(x);
-    const uint32_t e = (b >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)x;
-    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-    const uint32_t lo = b << 29;
-    return __hiloint2double((int)hi, (int)lo);
-}
-
 __device__ __forceinline__ int first_ks(const DualParams &p, float secs) {
     int k = 0;
     while (k < p.k && !(secs <= p.sk[k])) k++;
@@ -554,7 +545,10 @@ __device__ __forceinline__ int first_ks(const DualParams &p, float secs) {
 // Returns 0 when the replay is exact, 1 when some replayed route differs from the search's key (the
 // keys are then rewritten with the replayed values, so that sorting them again gives the next
 // settle-order estimate), 2 when the replayed seconds would reach a state the search did not.
-__device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, bool &bad, bool rewrite) {
+// check_reach: run the reach check even when every replayed value equals its key (the keys were
+// rewritten by an earlier round, and the search never relaxed from the rewritten seconds).
+__device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, bool &bad, bool rewrite,
+                           bool check_reach) {
     const int lane = lane_id();
     bool mismatch = false;
     // The replay recomputes every state's (route, seconds) from its offers in settle order, as the
@@ -634,7 +628,7 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
         }
     }
     if (__any_sync(FULL, mismatch)) return 1;
-    if (!__any_sync(FULL, secs_diff)) return 0;
+    if (!check_reach && !__any_sync(FULL, secs_diff)) return 0;
     __syncwarp();
     // reach check with the replayed seconds: every in-cutoff offer must land on a reached state
     bool escape = false;
@@ -844,7 +838,8 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
         __syncwarp();
         for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
         __syncwarp();
-        rr = dual_replay(p, s, src, R, bad, !exact);
+        // after a round that rewrote keys, lower rewritten seconds may reach states the search cut
+        rr = dual_replay(p, s, src, R, bad, !exact, it > 0);
         __syncwarp();
     }
     const bool ok = rr == 0;

@@ -37,6 +37,8 @@
 #include <vector>
 
 #include "cs_common.cuh"
+#include "cs_cta.cuh"
+#include "cs_seed.cuh"
 #include "cs_sort.cuh"
 
 namespace cs {
@@ -465,17 +467,6 @@ __device__ __forceinline__ void phase_mark(long long *ph, int idx, long long &t)
     t = now;
 }
 
-// f32 -> f64 by integer ops: keeps the conversion off GB300's narrow FP64 pipe.  Exact for
-// every finite f32; zeros, subnormals, infinities and NaN take the hardware conversion.
-__device__ __forceinline__ double f2d(float x) {
-    const uint32_t b = __float_as_uint(x);
-    const uint32_t e = (b >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)x;
-    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-    const uint32_t lo = b << 29;
-    return __hiloint2double((int)hi, (int)lo);
-}
-
 // first threshold index k with c <= dk[k] (thresholds strictly increasing), K if none
 __device__ __forceinline__ int first_k(const PrimalParams &p, float c) {
     int k = 0;
@@ -690,9 +681,10 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
                 const int v = s.ord[i];
                 const float cost = route_cost(s.sd[i], p.speed);
                 const double sw = sig[i];
-                double pair;
-                if constexpr (OD) pair = (double)od_weight(p, src, v);
-                else pair = __ldg(&p.eligible[v]) ? 0.5 : 1.0;
+                float pairf;
+                if constexpr (OD) pairf = od_weight(p, src, v);
+                else pairf = __ldg(&p.eligible[v]) ? 0.5f : 1.0f;
+                const double pair = f2d(pairf);
                 // predecessor rows and factors go to this lane's shared-memory column, so that the
                 // push loop below is a plain (not unrolled) loop over the np predecessors
 #pragma unroll
@@ -705,11 +697,10 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
                 }
                 double *dli = dl + (size_t)i * L;
                 const int k0 = first_k(p, cost);
-                const double cost_d = (double)cost;
                 for (int k = k0; k < K; k++) {
                     if (sw == 0.0) break;
                     const double seed = (i == 0) ? 0.0 : pair;
-                    const double seedb = (i == 0) ? 0.0 : __dmul_rn(pair, exp(__dmul_rn(-(double)p.beta[k], cost_d)));
+                    const double seedb = (i == 0 || pairf == 0.0f) ? 0.0 : seed_exp(pairf, p.beta[k], cost);
                     const double dep = __dadd_rn(seed, __ldcg(&dli[k]));
                     const double depb = __dadd_rn(seedb, __ldcg(&dli[K + k]));
                     if (dep == 0.0 && depb == 0.0) continue;
@@ -1500,7 +1491,7 @@ int sm_count() {
 }
 
 struct Layout {
-    size_t hdr_off, failed_off, failed2_off, bucket_off, dense_off, compact_off, compact_total, total;
+    size_t hdr_off, failed_off, failed2_off, bucket_off, dense_off, compact_off, compact_total, cta_off, total;
     size_t dense_stride;
     int fail_cap;
 };
@@ -1509,7 +1500,8 @@ struct Layout {
 // reports CS_ERR_CAPACITY (plan a larger cap)
 int fail_capacity(int n_slots) { return std::max(n_slots, 1 << 18); }
 
-Layout layout(int n_bound, int n_slots, int cap, int P, int L) {
+// cta_blocks: blocks of the block-per-source kernel whose global scratch follows the per-warp regions.
+Layout layout(int n_bound, int n_slots, int cap, int P, int L, int cta_blocks = 0) {
     Layout l;
     l.hdr_off = 0;
     l.failed_off = 256;
@@ -1522,7 +1514,8 @@ Layout layout(int n_bound, int n_slots, int cap, int P, int L) {
     l.compact_total = cs::compact_bytes((size_t)cap, P, L) * (size_t)n_slots;
     // the in-call retry runs at cap = n_bound on the same compact region: keep room for one slot
     l.compact_total = std::max(l.compact_total, cs::compact_bytes((size_t)n_bound, P, L));
-    l.total = l.compact_off + l.compact_total;
+    l.cta_off = cs::al256(l.compact_off + l.compact_total);
+    l.total = l.cta_off + cs::cta::scratch_bytes() * (size_t)std::max(0, cta_blocks);
     return l;
 }
 
@@ -1604,6 +1597,13 @@ bool phase_sync() {
     return !(e && e[0] == '0');
 }
 
+// Block-per-source kernel for shortest-path and OD calls; CS_BLOCK_PER_SOURCE=0 in the environment
+// leaves every source to the per-warp kernel.
+bool block_kernel_enabled() {
+    const char *e = getenv("CS_BLOCK_PER_SOURCE");
+    return !(e && e[0] == '0');
+}
+
 // Settle-order sort: distance buckets by default, CS_SORT=radix selects the LSD radix sort.
 int radix_sort_choice() {
     const char *e = getenv("CS_SORT");
@@ -1679,6 +1679,14 @@ cs_status launch_batch(cs::PrimalParams &p, const cs_plan *plan, const cs_batch_
     return CS_OK;
 }
 
+// Tabulates exp(-j / 256) for the beta-weighted seeds (cs_seed.cuh) on the call's stream.
+cs_status launch_seed_table(cudaStream_t stream) {
+    cs::seed_table_kernel<<<(cs::SEED_TAB + 255) / 256, 256, 0, stream>>>();
+    g_counters[3]++;
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CS_OK : cuda_fail(e, "seed_table_kernel launch");
+}
+
 cs_status reset_dense(char *dense, size_t stride, int n_bound, int n_slots, cudaStream_t stream) {
     const size_t total = (size_t)n_bound * (size_t)n_slots;
     int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)sm_count() * 16);
@@ -1705,7 +1713,9 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     if (plan->lanes < L) return fail(CS_ERR_ARG, "plan was made for fewer thresholds");
     if (plan->n_bound > 0 && plan->n_bound != g->n_bound)
         return fail(CS_ERR_ARG, "plan was made for a graph of another node bound");
-    Layout lay = layout(g->n_bound, plan->n_slots, plan->cap, P, plan->lanes);
+    const bool block = (mode == cs::MODE_SHORTEST || mode == cs::MODE_OD) && plan->cta_blocks > 0 &&
+                       cs::cta::supported(P, K) && block_kernel_enabled();
+    Layout lay = layout(g->n_bound, plan->n_slots, plan->cap, P, plan->lanes, plan->cta_blocks);
     if (ws_bytes < lay.total) return fail(CS_ERR_ARG, "workspace too small for this plan");
     cudaStream_t stream = (cudaStream_t)stream_v;
     char *base = (char *)ws;
@@ -1780,8 +1790,61 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
         e = cudaMemsetAsync(p.bucket, 0, sizeof(double) * 3 * (size_t)K * (size_t)g->n_bound, stream);
         if (e != cudaSuccess) return cuda_fail(e, "bucket reset");
     }
-    st = launch_primal(p, plan, plan->n_slots, stream);
-    if (st != CS_OK) return st;
+    if (p.betweenness && (mode == cs::MODE_SHORTEST || mode == cs::MODE_OD)) {
+        st = launch_seed_table(stream);
+        if (st != CS_OK) return st;
+    }
+    if (block) {
+        // one block per source with its state on chip; the sources it lists (reach or queues beyond
+        // its capacity) run through the per-warp kernel's capacity chain below
+        e = cs::cta::launch_seed_table(stream);
+        if (e != cudaSuccess) return cuda_fail(e, "seed table launch");
+        cs::cta::Params c;
+        memset(&c, 0, sizeof(c));
+        c.n_bound = g->n_bound;
+        c.in_ptr = g->in_ptr_dev;
+        c.in_nb = g->in_nb_dev;
+        c.in_w = g->in_w_dev;
+        c.out_ptr = g->out_ptr_dev;
+        c.out_to = g->out_to_dev;
+        c.out_w = g->out_w_dev;
+        c.out_cnt = g->out_cnt_dev;
+        c.node_w = g->node_w_dev;
+        c.k = K;
+        for (int i = 0; i < K; i++) {
+            c.dk[i] = p.dk[i];
+            c.beta[i] = p.beta[i];
+        }
+        c.maxsec = p.maxsec;
+        c.speed = p.speed;
+        c.tol = p.tol;
+        c.delta = p.delta;
+        c.closeness = p.closeness;
+        c.betweenness = p.betweenness;
+        c.track_reach = p.track_reach;
+        c.od = (mode == cs::MODE_OD) ? 1 : 0;
+        c.src_list = p.src_list;
+        c.n_src = p.n_src;
+        c.src_wt = p.src_wt;
+        c.eligible = p.eligible;
+        c.od_ptr = p.od_ptr;
+        c.od_dst = p.od_dst;
+        c.od_w = p.od_w;
+        c.out = p.out;
+        c.bucket = p.bucket;
+        c.reach = p.reach;
+        c.hdr = p.hdr;
+        c.failed = p.failed;
+        c.fail_cap = p.fail_cap;
+        c.scratch = base + lay.cta_off;
+        c.scratch_stride = cs::cta::scratch_bytes();
+        e = cs::cta::launch(c, plan->cta_blocks, stream);
+        g_counters[3] += 2;
+        if (e != cudaSuccess) return cuda_fail(e, "source_block_kernel launch");
+    } else {
+        st = launch_primal(p, plan, plan->n_slots, stream);
+        if (st != CS_OK) return st;
+    }
     cs::WsHeader h;
     e = cs::read_header(p.hdr, h, stream, poll);
     if (e != cudaSuccess) return cuda_fail(e, "centrality kernel");
@@ -1814,7 +1877,8 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     return CS_OK;
 }
 
-cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t budget, cs_plan *plan) {
+cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t budget, cs_plan *plan,
+                      bool block_kernel = false) {
     const int variant = resolve_variant(plan);
     if (!plan) return fail(CS_ERR_ARG, "plan is NULL");
     int sms = sm_count();
@@ -1827,7 +1891,8 @@ cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t
     if (max_slots > 0) slots = std::min(slots, max_slots);
     if (cap <= 0) cap = std::min(n_bound, 16384);
     cap = std::max(32, std::min(cap, n_bound));
-    auto total_for = [&](int ns) { return layout(n_bound, ns, cap, P, L).total; };
+    const int cta_blocks = block_kernel ? sms : 0;
+    auto total_for = [&](int ns) { return layout(n_bound, ns, cap, P, L, cta_blocks).total; };
     if (budget > 0) {
         while (slots > 8 && (int64_t)total_for(slots) > budget) slots = (slots * 7) / 8;
     }
@@ -1841,6 +1906,7 @@ cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t
     plan->variant = variant;
     plan->max_degree = P;
     plan->n_bound = n_bound;
+    plan->cta_blocks = cta_blocks;
     plan->workspace_bytes = total_for(slots);
     return CS_OK;
 }
@@ -1885,8 +1951,9 @@ cs_status cs_plan_primal(const cs_primal_graph *g, int32_t mode, int32_t k, int3
     const int P = std::max(1, g->max_out_degree);
     const float keep_delta = plan ? plan->delta_seconds : 0.0f;
     if (plan) plan->delta_seconds = keep_delta;
+    const bool block = mode == cs::MODE_SHORTEST && block_kernel_enabled() && cs::cta::supported(P, k);
     return plan_common(g->n_bound, P, lanes_for(mode, mode == cs::MODE_TREE ? 1 : k), cap, max_slots,
-                       mem_budget_bytes, plan);
+                       mem_budget_bytes, plan, block);
 }
 
 cs_status cs_workspace_init(const cs_plan *plan, int32_t n_bound, void *workspace_dev, size_t workspace_bytes,
@@ -2140,6 +2207,8 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
         else runs.push_back({lo, hi, m});
     }
     if (runs.size() > 4) runs.assign(1, Run{0, n_items, -1});
+    st = launch_seed_table(stream);
+    if (st != CS_OK) return st;
     for (const Run &r : runs) {
         if (r.hi <= r.lo) continue;
         e = cudaMemsetAsync(&p.hdr->work_next, 0, sizeof(unsigned long long), stream);
@@ -2237,6 +2306,26 @@ extern "C" cs_status cs_source_weights(const int32_t *sources_dev, int64_t n_sou
     }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CS_OK : cuda_fail(e, "source_weights_kernel launch");
+}
+
+namespace cs {
+__global__ void seed_check_kernel(const float *w, const float *beta, const float *cost, double *out, long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        out[t] = seed_exp(w[t], beta[t], cost[t]);
+}
+}  // namespace cs
+
+extern "C" cs_status cs_debug_seed_exp(const float *w_dev, const float *beta_dev, const float *cost_dev,
+                                       double *out_dev, int64_t n, void *stream) {
+    if (n < 0 || (n > 0 && (!w_dev || !beta_dev || !cost_dev || !out_dev))) return fail(CS_ERR_ARG, "seed check: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    cs_status rc = launch_seed_table(st);
+    if (rc != CS_OK) return rc;
+    if (n == 0) return CS_OK;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+    cs::seed_check_kernel<<<blocks, 256, 0, st>>>(w_dev, beta_dev, cost_dev, out_dev, n);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CS_OK : cuda_fail(e, "seed_check_kernel launch");
 }
 
 extern "C" cs_status cs_abi_sizes(int32_t *out, int32_t n) {

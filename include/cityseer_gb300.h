@@ -106,6 +106,8 @@ typedef struct {
     int32_t variant;      /* register budget: 3 (default), 4 or 2 resident 256-thread blocks per SM */
     int32_t max_degree;   /* batches: largest out-degree over the jobs */
     int32_t n_bound;      /* node bound the slot geometry was sized for (set by the planners) */
+    int32_t cta_blocks;   /* shortest-path plans: blocks of the block-per-source kernel whose scratch
+                             the workspace holds (0: the per-warp kernel serves every source) */
     size_t workspace_bytes;
 } cs_plan;
 
@@ -326,6 +328,13 @@ cs_status cs_abi_sizes(int32_t *out, int32_t n);
 
 /* Number of SMs of the current device (0 on failure). */
 int32_t cs_device_sm_count(void);
+
+/* Diagnostic (no counterpart in the reference): out[i] = w[i] * exp(-(beta[i] * cost[i])) as the
+ * betweenness kernels evaluate the beta-weighted seeds (f64 result of an exact f32 x f32 product,
+ * the exp taken in double-float arithmetic on the f32 pipe); the reference takes the f64 exp
+ * (rust/src/centrality.rs:1806-1808).  All pointers are device arrays of n elements. */
+cs_status cs_debug_seed_exp(const float *w_dev, const float *beta_dev, const float *cost_dev, double *out_dev,
+                            int64_t n, void *stream);
 
 #ifdef __cplusplus
 }

@@ -176,3 +176,30 @@ def test_removed_nodes_and_index_gaps():
     res, ref, _, d = _run(ns, dists)
     assert len(res.node_indices) == ns.node_count()
     _compare(ns, res, ref, d, what="gaps")
+
+
+@pytest.mark.gpu
+def test_beta_seed_exp_f64_accuracy():
+    """The beta-weighted seeds w * exp(-(beta * cost)) of the betweenness kernels against numpy's f64
+    exp of the same exact f32 x f32 product (the reference's arithmetic), over betas 4 / d for
+    d in 100 m .. 20 km and costs 0 .. 2 d, plus out-of-table arguments."""
+    import torch
+
+    from cityseer_gb300 import _native
+
+    rng = np.random.default_rng(3)
+    n = 1 << 20
+    d = rng.uniform(100.0, 20000.0, n)
+    beta = np.round(4.0 / d, 5).astype(np.float32)
+    cost = (rng.uniform(0.0, 2.0, n) * d).astype(np.float32)
+    w = rng.choice(np.array([0.5, 1.0, 0.37, 3.0], np.float32), n)
+    beta[:64] = rng.uniform(0.05, 0.5, 64).astype(np.float32)  # arguments beyond the table (>= 8)
+    dev = torch.device("cuda", 0)
+    tw, tb, tc = (torch.from_numpy(x).to(dev) for x in (w, beta, cost))
+    out = torch.empty(n, dtype=torch.float64, device=dev)
+    _native.check(_native.load().cs_debug_seed_exp(tw.data_ptr(), tb.data_ptr(), tc.data_ptr(), out.data_ptr(), n,
+                                                   None), "cs_debug_seed_exp")
+    got = out.cpu().numpy()
+    want = w.astype(np.float64) * np.exp(-(beta.astype(np.float64) * cost.astype(np.float64)))
+    rel = np.abs(got - want) / np.maximum(want, 1e-200)
+    assert rel.max() < 5e-14, (rel.max(), int(rel.argmax()))
