@@ -380,10 +380,60 @@ def run_gpu(args):
     if rank == 0 and ws == 1 and not args.no_cpu:  # the CPU baseline is reported at N = 1 only
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(ns, dists, n_nodes, args.cpu_seconds).items()
                                 if k != "seconds"}
+    if rank == 0 and ws == 1 and not args.no_extra:
+        # the rest of the headline metric, each leg bounded: batched vs plain, served latency,
+        # simplest paths on the curved lattice's dual
+        centrality.drop_device_state(ns)
+        del out, l2
+        torch.cuda.empty_cache()
+        line.update(extra_legs(args))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def extra_legs(args) -> dict:
+    """Summaries of the batched, served and curved-dual legs for the default bench line."""
+    import torch
+
+    out = {}
+    t0 = time.perf_counter()
+    b = run_batch(argparse.Namespace(**{**vars(args), "graphs": args.extra_graphs, "steps": 3, "warmup": 1,
+                                        "plain_steps": 1}))
+    out["batched"] = {
+        "workload": b["config"]["workload"], "graphs": b["config"]["graphs"],
+        "reduced_from": "the 96-graph batched configuration: its first %d graphs" % b["config"]["graphs"],
+        "items_per_s": b["value"], "plain_items_per_s": b["plain"]["value"],
+        "batched_over_plain": b["batched_over_plain"], "parity_max_rel": b["parity_max_rel"],
+        "ms_per_step": b["ms_per_step"], "plain_ms_per_step": b["plain"]["ms_per_step"],
+        "leg_seconds": round(time.perf_counter() - t0, 1),
+    }
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    sv = run_serve(argparse.Namespace(**{**vars(args), "serve_rates": "500", "serial_seconds": 15.0}))
+    at = sv["sweep"][0]
+    out["served"] = {
+        "workload": sv["config"]["workload"], "rate_req_s": at["rate_req_s"], "requests": at["requests"],
+        "saturated": at["saturated"], "sources_per_s": at["sources_per_s"],
+        "p50_ms_le_1k_sources": at["le_1k_sources"].get("p50_ms"),
+        "p99_ms_le_1k_sources": at["le_1k_sources"].get("p99_ms"),
+        "shortest": at["shortest"], "simplest": at["simplest"],
+        "serial_plain_sources_per_s": sv["serial_plain"]["sources_per_s"],
+        "served_over_serial_sources_per_s": sv["served_over_serial_sources_per_s"],
+        "leg_seconds": round(time.perf_counter() - t0, 1),
+    }
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    c3 = run_c3(argparse.Namespace(**{**vars(args), "side": None, "steps": 2, "warmup": 1}))
+    out["simplest"] = {
+        "workload": c3["config"]["workload"], "dual_nodes": c3["config"]["dual_nodes"],
+        "dual_sources_per_s": c3["value"], "ms_per_step": c3["ms_per_step"],
+        "segment_sources_per_s": c3["segment"]["value"],
+        "sources_redone_exactly": c3["simplest_sources_redone_exactly"],
+        "leg_seconds": round(time.perf_counter() - t0, 1),
+    }
+    return out
 
 
 BATCH_METRIC = "sources/s, 96 mixed-size graphs (2k-150k nodes), shortest + segment: batched vs plain GPU"
@@ -536,7 +586,7 @@ def run_batch(args):
         "gpu_launches": 2,
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 SERVE_METRIC = "served p50/p99 latency and sources/s, 6 resident graphs (50k-1.2M nodes), Poisson arrivals"
@@ -723,7 +773,7 @@ def run_serve(args):
         "setup_s": {"graphs": round(t_build, 1), "server": round(t_setup, 1)},
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_c3(args):
@@ -783,7 +833,7 @@ def run_c3(args):
         "setup_s": round(t_build, 1),
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -806,13 +856,16 @@ def main():
     ap.add_argument("--serial-seconds", type=float, default=60.0)
     ap.add_argument("--graphs", type=int, default=96)
     ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default workload only: skip the batched, served and curved-dual legs")
+    ap.add_argument("--extra-graphs", type=int, default=48, help="graphs of the batched leg in the default line")
     args = ap.parse_args()
     if args.workload == "batch" and args.impl != "reference":
-        run_batch(args)
+        print(json.dumps(run_batch(args)), flush=True)
     elif args.workload == "serve" and args.impl != "reference":
-        run_serve(args)
+        print(json.dumps(run_serve(args)), flush=True)
     elif args.workload == "c3" and args.impl != "reference":
-        run_c3(args)
+        print(json.dumps(run_c3(args)), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:

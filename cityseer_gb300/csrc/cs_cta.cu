@@ -57,17 +57,19 @@ constexpr size_t OFF_SD = OFF_B;                          // f32[RMAX] settle di
 constexpr size_t OFF_SIG = OFF_B + 4ull * RMAX;           // u32[RMAX]: sort slots, then path counts
 constexpr size_t OFF_S = OFF_B + 3 * SZ_Q;                // small region
 constexpr size_t OFF_HIST = OFF_S;                        // u32[NBK]
-constexpr size_t OFF_DONE = OFF_HIST + 4ull * NBK;        // u32[NCH] chunk flags
-constexpr size_t OFF_MSC = OFF_DONE + 4ull * NCH;         // i32[NCH] last successor chunk
-constexpr size_t OFF_CNT = OFF_MSC + 4ull * NCH;          // i32[2 MAXK]
+constexpr size_t OFF_WSUM = OFF_HIST + 4ull * NBK;        // u32[NW] scan partials
+constexpr size_t OFF_CNT = OFF_WSUM + 4ull * NW;          // i32[2 MAXK]
 constexpr size_t OFF_RANKW = OFF_CNT + 8ull * MAXK;       // f32[MAXK]
 constexpr size_t OFF_VARS = OFF_RANKW + 4ull * MAXK;      // block variables
 constexpr size_t SMEM = OFF_VARS + 256;
-// the backward sweep's dependencies overlay the hash table and the settle distances
+// the backward sweep's dependencies and pending-successor counts overlay the hash table and the
+// settle distances
 constexpr size_t OFF_DPLAIN = 0;                          // f64[RMAX]
 constexpr size_t OFF_DBETA = 8ull * RMAX;                 // f64[RMAX]
+constexpr size_t OFF_SCNT = 16ull * RMAX;                 // u8[RMAX], updated as u32 words
 static_assert(3 * SZ_Q >= 8ull * RMAX, "sort buffers exceed the queue region");
-static_assert(OFF_DBETA + 8ull * RMAX <= OFF_SIG, "dependencies overlap the path counts");
+static_assert(OFF_SCNT + RMAX <= OFF_SIG, "backward arrays overlap the path counts");
+static_assert(RMAX % 32 == 0 && RMAX < 65536, "positions are u16 in the predecessor lists");
 static_assert(SMEM <= 232448, "shared memory beyond the per-block limit");
 
 struct Vars {
@@ -208,24 +210,45 @@ __device__ void search(const Params &p, char *sm, Vars &v, long long &relaxed) {
                 relaxed += end - beg;
                 const int deg = end - beg;
                 const int maxdeg = warp_max_i(deg);
+                // the node's first PMAX edges are loaded together, then relaxed
+                int nbs[PMAX];
+                float cs[PMAX];
+#pragma unroll
+                for (int j = 0; j < PMAX; j++) {
+                    nbs[j] = (int)u;
+                    cs[j] = 0.0f;
+                    if (j < deg) {
+                        nbs[j] = __ldg(&p.in_nb[beg + j]);
+                        cs[j] = __fadd_rn(du, __ldg(&p.in_w[beg + j]));
+                    }
+                }
                 for (int j = 0; j < maxdeg; j++) {
+                    int nb = (int)u;
+                    float c = 0.0f;
+                    if (j < PMAX) {
+#pragma unroll
+                        for (int q = 0; q < PMAX; q++)
+                            if (q == j) {
+                                nb = nbs[q];
+                                c = cs[q];
+                            }
+                    } else if (j < deg) {  // high in-degree: one at a time
+                        nb = __ldg(&p.in_nb[beg + j]);
+                        c = __fadd_rn(du, __ldg(&p.in_w[beg + j]));
+                    }
                     bool push_near = false, push_far = false;
                     uint2 out = make_uint2(0u, 0u);
-                    if (j < deg) {
-                        const int nb = __ldg(&p.in_nb[beg + j]);
-                        const float c = __fadd_rn(du, __ldg(&p.in_w[beg + j]));
-                        if ((uint32_t)nb != u && c <= p.maxsec) {
-                            uint32_t old;
-                            const uint32_t cb = __float_as_uint(c);
-                            const int sl = hash_upsert_min(hkey, hval, (uint32_t)nb, cb, old);
-                            if (sl < 0) {
-                                qfail = 1;
-                            } else if (cb < old) {
-                                if (old == (uint32_t)INF_BITS) atomicAdd(&v.R, 1);
-                                out = make_uint2((uint32_t)sl, cb);
-                                push_near = c < T;
-                                push_far = !push_near;
-                            }
+                    if (j < deg && (uint32_t)nb != u && c <= p.maxsec) {
+                        uint32_t old;
+                        const uint32_t cb = __float_as_uint(c);
+                        const int sl = hash_upsert_min(hkey, hval, (uint32_t)nb, cb, old);
+                        if (sl < 0) {
+                            qfail = 1;
+                        } else if (cb < old) {
+                            if (old == (uint32_t)INF_BITS) atomicAdd(&v.R, 1);
+                            out = make_uint2((uint32_t)sl, cb);
+                            push_near = c < T;
+                            push_far = !push_near;
                         }
                     }
                     queue_push(push_near, nxt, &v.nnext, out, qfail);
@@ -335,7 +358,7 @@ __device__ void settle_order(const Params &p, char *sm, Vars &v, float *sd_g, ui
             const uint32_t t = __shfl_up_sync(FULL, inc, o);
             if (lane >= o) inc += t;
         }
-        uint32_t *wsum = (uint32_t *)(sm + OFF_DONE);  // the chunk flags are free here
+        uint32_t *wsum = (uint32_t *)(sm + OFF_WSUM);
         if (lane == 31) wsum[warp] = inc;
         __syncthreads();
         if (warp == 0) {
@@ -497,16 +520,20 @@ __device__ __forceinline__ unsigned replay_preds(const Params &p, const Nb &nb, 
     return pm;
 }
 
-__device__ __forceinline__ bool wait_flag(const uint32_t *flag, Vars &v) {
+// Waits (bounded) until another thread has written a non-zero value at a; returns it (0: gave up,
+// after raising CS_ERR_TIMEOUT).
+__device__ __forceinline__ uint32_t wait_nonzero(const uint32_t *a, Vars &v) {
     long long spins = 0;
-    while (vload(flag) == 0u) {
+    uint32_t x;
+    while ((x = vload(a)) == 0u) {
         if (++spins > SPIN_LIMIT) {
             atomicCAS(&v.err, 0, CS_ERR_TIMEOUT);
-            return false;
+            return 0u;
         }
+        __nanosleep(20);
     }
     __threadfence_block();
-    return true;
+    return x;
 }
 
 __device__ void replay(const Params &p, char *sm, Vars &v, const uint32_t *ord_g, uint16_t *pr_g, uint8_t *np_g) {
@@ -514,16 +541,12 @@ __device__ void replay(const Params &p, char *sm, Vars &v, const uint32_t *ord_g
     const uint32_t *hval = (const uint32_t *)(sm + OFF_HVAL);
     const float *sd = (const float *)(sm + OFF_SD);
     uint32_t *sig = (uint32_t *)(sm + OFF_SIG);
-    uint32_t *done = (uint32_t *)(sm + OFF_DONE);
-    int *msc = (int *)(sm + OFF_MSC);
     int *cnt = (int *)(sm + OFF_CNT);
     const int tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
     const int R = v.R;
     const int nch = (R + 31) / 32;
-    for (int c = tid; c < NCH; c += TPB) {
-        done[c] = 0u;
-        msc[c] = c;
-    }
+    // a path count is at least 1 once written: 0 marks "not yet"
+    for (int i = tid; i < R; i += TPB) sig[i] = 0u;
     for (int q = tid; q < 2 * MAXK; q += TPB) cnt[q] = 0;
     __syncthreads();
     const int K = p.k;
@@ -562,10 +585,7 @@ __device__ void replay(const Params &p, char *sm, Vars &v, const uint32_t *ord_g
                 int r = 0;
 #pragma unroll
                 for (int j = 0; j < PMAX; j++) {
-                    if ((pm >> j) & 1u) {
-                        pr_g[(size_t)i * PMAX + r++] = (uint16_t)nb.pos[j];
-                        atomicMax(&msc[nb.pos[j] >> 5], ch);
-                    }
+                    if ((pm >> j) & 1u) pr_g[(size_t)i * PMAX + r++] = (uint16_t)nb.pos[j];
                 }
                 np_g[i] = (uint8_t)r;
             } else if (act) {
@@ -573,12 +593,12 @@ __device__ void replay(const Params &p, char *sm, Vars &v, const uint32_t *ord_g
             }
         }
         if (!betw) continue;
-        // path counts: wait for the earlier chunks holding this lane's predecessors, then resolve
-        // the in-chunk ones in ballot rounds
+        // path counts: wait for the predecessors in earlier chunks (their counts become non-zero),
+        // then resolve the in-chunk ones in ballot rounds
 #pragma unroll
         for (int j = 0; j < PMAX; j++)
             if (((pm >> j) & 1u) && nb.pos[j] < base) {
-                if (!wait_flag(&done[nb.pos[j] >> 5], v)) pm = 0u;
+                if (!wait_nonzero(&sig[nb.pos[j]], v)) pm = 0u;
             }
         __syncwarp();
         unsigned blk = 0u;
@@ -599,7 +619,7 @@ __device__ void replay(const Params &p, char *sm, Vars &v, const uint32_t *ord_g
                     atomicCAS(&v.fail, 0, F_SIGMA);
                     sg = 0xffffffffull;
                 }
-                sig[i] = (uint32_t)sg;
+                *(volatile uint32_t *)&sig[i] = (uint32_t)sg;
                 mine = true;
             }
             __syncwarp();
@@ -608,8 +628,6 @@ __device__ void replay(const Params &p, char *sm, Vars &v, const uint32_t *ord_g
         }
         if (fin != FULL) bad = true;
         __syncwarp();
-        __threadfence_block();
-        if (lane == 0) *(volatile uint32_t *)&done[ch] = 1u;
     }
     if (bad) atomicCAS(&v.err, 0, CS_ERR_INTERNAL);
     __syncthreads();
@@ -659,16 +677,21 @@ __device__ void closeness(const Params &p, char *sm, Vars &v, const uint32_t *or
 }
 
 // ------------------------------------------------------------------------------------------
-// 5. Backward Brandes sweep, one threshold at a time over the positions within it.
+// 5. Backward Brandes sweep, one threshold at a time over the positions within it.  A node waits
+//    for its pending-successor count (successors within the sweep that have not pushed yet) to
+//    reach zero, then pushes its dependency to its predecessors and decrements theirs.
 // ------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t scnt_get(const uint32_t *w, int i) {
+    return (vload(&w[i >> 2]) >> ((i & 3) * 8)) & 0xffu;
+}
+
 __device__ void backward(const Params &p, char *sm, Vars &v, const uint32_t *ord_g, const float *sd_g,
                          const uint16_t *pr_g, const uint8_t *np_g) {
     const uint32_t *sig = (const uint32_t *)(sm + OFF_SIG);
-    uint32_t *done = (uint32_t *)(sm + OFF_DONE);
-    const int *msc = (const int *)(sm + OFF_MSC);
     const int *cnt = (const int *)(sm + OFF_CNT);
     double *dpl = (double *)(sm + OFF_DPLAIN);
     double *dbe = (double *)(sm + OFF_DBETA);
+    uint32_t *scnt = (uint32_t *)(sm + OFF_SCNT);
     const int tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
     const int K = p.k, N = p.n_bound;
     const int src = v.src;
@@ -685,85 +708,76 @@ __device__ void backward(const Params &p, char *sm, Vars &v, const uint32_t *ord
             dpl[i] = 0.0;
             dbe[i] = 0.0;
         }
-        for (int c = tid; c < nch; c += TPB) done[c] = 0u;
+        for (int w = tid; w < (nk + 3) / 4; w += TPB) scnt[w] = 0u;
+        __syncthreads();
+        // successors of each node within this sweep (a predecessor's position is below its node's)
+        for (int i = tid; i < nk; i += TPB) {
+            const int np = np_g[i];
+            for (int r = 0; r < np; r++) {
+                const int q = pr_g[(size_t)i * PMAX + r];
+                const uint32_t old = atomicAdd(&scnt[q >> 2], 1u << ((q & 3) * 8));
+                // a byte counter holds 255 successors; street graphs have a handful
+                if (((old >> ((q & 3) * 8)) & 0xffu) == 0xffu) atomicCAS(&v.err, 0, CS_ERR_INTERNAL);
+            }
+        }
         __syncthreads();
         const float beta = p.beta[k];
         for (int ch = nch - 1 - warp; ch >= 0; ch -= NW) {
-            const int base = ch * 32;
-            const int i = base + lane;
-            const bool act = i < nk;
-            // this lane's predecessors and its seeds, before the waits
-            const int np = act ? np_g[i] : 0;
-            int pl[PMAX];
-            unsigned pm = 0u;
+            const int i = ch * 32 + lane;
+            if (i < nk) {
+                // predecessors and seeds first, then the wait
+                const int np = np_g[i];
+                int pl[PMAX];
 #pragma unroll
-            for (int r = 0; r < PMAX; r++) {
-                pl[r] = (r < np) ? (int)pr_g[(size_t)i * PMAX + r] : 0;
-                if (r < np && pl[r] >= base) pm |= 1u << (pl[r] - base);
-            }
-            int vtx = 0;
-            double seed = 0.0, seedb = 0.0;
-            if (act && i > 0) {
-                vtx = (int)ord_g[i];
-                const float cost = route_cost(sd_g[i], p.speed);
-                const float pairf = p.od ? od_weight(p, src, vtx) : (__ldg(&p.eligible[vtx]) ? 0.5f : 1.0f);
-                seed = f2d(pairf);
-                seedb = (pairf == 0.0f) ? 0.0 : seed_exp(pairf, beta, cost);
-            } else if (act) {
-                vtx = (int)ord_g[i];
-            }
-            // successors of this chunk's nodes lie in chunks (ch, msc[ch]] within the sweep
-            if (lane == 0) {
-                const int last = min(msc[ch], nch - 1);
-                for (int c = ch + 1; c <= last; c++)
-                    if (!wait_flag(&done[c], v)) break;
-            }
-            __syncwarp();
-            __threadfence_block();
-            bool mine = !act;
-            unsigned fin = __ballot_sync(FULL, mine);
-            int guard = 0;
-            while (fin != FULL) {
-                const unsigned blocked = __reduce_or_sync(FULL, mine ? 0u : pm);
-                const bool ready = !mine && !((blocked >> lane) & 1u);
-                if (ready) {
-                    const double sw = (double)sig[i];
-                    const double dep = __dadd_rn(seed, dpl[i]);
-                    const double depb = __dadd_rn(seedb, dbe[i]);
-                    if (sw != 0.0 && (dep != 0.0 || depb != 0.0)) {
-                        for (int r = 0; r < np; r++) {
-                            const int q = pl[r];
-                            const double sv = (double)sig[q];
-                            if (sv == 0.0) continue;
-                            if (sv == sw) {
-                                atomicAdd(&dpl[q], dep);
-                                atomicAdd(&dbe[q], depb);
-                            } else {
-                                const double f = __ddiv_rn(sv, sw);
-                                atomicAdd(&dpl[q], __dmul_rn(f, dep));
-                                atomicAdd(&dbe[q], __dmul_rn(f, depb));
-                            }
-                        }
-                        if (vtx != src) {
-                            const double credit = __dadd_rn(dep, -seed);
-                            const double creditb = __dadd_rn(depb, -seedb);
-                            if (credit > 0.0)
-                                atomicAdd(p.out + (row_b * K + k) * N + vtx, unit_wt ? credit : __dmul_rn(credit, wtd));
-                            if (creditb > 0.0)
-                                atomicAdd(p.out + ((row_b + 1) * K + k) * N + vtx,
-                                          unit_wt ? creditb : __dmul_rn(creditb, wtd));
+                for (int r = 0; r < PMAX; r++) pl[r] = (r < np) ? (int)pr_g[(size_t)i * PMAX + r] : 0;
+                const int vtx = (int)ord_g[i];
+                double seed = 0.0, seedb = 0.0;
+                if (i > 0) {
+                    const float cost = route_cost(sd_g[i], p.speed);
+                    const float pairf = p.od ? od_weight(p, src, vtx) : (__ldg(&p.eligible[vtx]) ? 0.5f : 1.0f);
+                    seed = f2d(pairf);
+                    seedb = (pairf == 0.0f) ? 0.0 : seed_exp(pairf, beta, cost);
+                }
+                long long spins = 0;
+                while (scnt_get(scnt, i) != 0u) {
+                    if (++spins > SPIN_LIMIT) {
+                        atomicCAS(&v.err, 0, CS_ERR_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(20);
+                }
+                __threadfence_block();
+                const double sw = (double)sig[i];
+                const double dep = __dadd_rn(seed, dpl[i]);
+                const double depb = __dadd_rn(seedb, dbe[i]);
+                const bool push = sw != 0.0 && (dep != 0.0 || depb != 0.0);
+                for (int r = 0; r < np; r++) {
+                    const int q = pl[r];
+                    const double sv = (double)sig[q];
+                    if (push && sv != 0.0) {
+                        if (sv == sw) {
+                            atomicAdd(&dpl[q], dep);
+                            atomicAdd(&dbe[q], depb);
+                        } else {
+                            const double f = __ddiv_rn(sv, sw);
+                            atomicAdd(&dpl[q], __dmul_rn(f, dep));
+                            atomicAdd(&dbe[q], __dmul_rn(f, depb));
                         }
                     }
-                    mine = true;
                 }
-                __syncwarp();
-                fin |= __ballot_sync(FULL, ready);
-                if (++guard > 64) break;
+                __threadfence_block();
+                for (int r = 0; r < np; r++) atomicSub(&scnt[pl[r] >> 2], 1u << ((pl[r] & 3) * 8));
+                if (push && vtx != src) {
+                    const double credit = __dadd_rn(dep, -seed);
+                    const double creditb = __dadd_rn(depb, -seedb);
+                    if (credit > 0.0)
+                        atomicAdd(p.out + (row_b * K + k) * N + vtx, unit_wt ? credit : __dmul_rn(credit, wtd));
+                    if (creditb > 0.0)
+                        atomicAdd(p.out + ((row_b + 1) * K + k) * N + vtx,
+                                  unit_wt ? creditb : __dmul_rn(creditb, wtd));
+                }
             }
-            if (fin != FULL && lane == 0) atomicCAS(&v.err, 0, CS_ERR_INTERNAL);
             __syncwarp();
-            __threadfence_block();
-            if (lane == 0) *(volatile uint32_t *)&done[ch] = 1u;
         }
         __syncthreads();
         if (v.err) return;

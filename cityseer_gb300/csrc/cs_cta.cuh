@@ -14,9 +14,9 @@ constexpr int TPB = 1024;       // threads per block
 constexpr int NW = TPB / 32;    // warps per block
 constexpr int HBITS = 14;
 constexpr int HSIZE = 1 << HBITS;  // hash slots (node -> distance, then node -> settle position)
-constexpr int RMAX = 10752;     // reached nodes per source held on chip (more: the per-warp kernel)
+constexpr int RMAX = 9984;      // reached nodes per source held on chip (more: the per-warp kernel)
 constexpr int NCH = RMAX / 32;  // chunks of 32 settle positions
-constexpr int QCAP = 3584;      // entries per search queue (near, next, far)
+constexpr int QCAP = 3328;      // entries per search queue (near, next, far)
 constexpr int NBK = 1024;       // distance buckets of the settle-order sort
 constexpr int BKMAX = 512;      // largest bucket sorted on chip
 constexpr int PMAX = 8;         // predecessors per node (the graph's maximum out-degree)

@@ -1818,7 +1818,13 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
         c.maxsec = p.maxsec;
         c.speed = p.speed;
         c.tol = p.tol;
-        c.delta = p.delta;
+        // the block kernel's rounds are paced by barriers: wider bands (fewer rounds, more
+        // re-relaxations) suit it; CS_BLOCK_DELTA_SCALE overrides the width factor
+        {
+            const char *ev = getenv("CS_BLOCK_DELTA_SCALE");
+            const float scale = ev ? (float)atof(ev) : 4.0f;
+            c.delta = (scale > 0.0f) ? p.delta * scale : p.delta;
+        }
         c.closeness = p.closeness;
         c.betweenness = p.betweenness;
         c.track_reach = p.track_reach;
