@@ -1598,10 +1598,23 @@ bool phase_sync() {
 }
 
 // Block-per-source kernel for shortest-path and OD calls; CS_BLOCK_PER_SOURCE=0 in the environment
-// leaves every source to the per-warp kernel.
+// leaves every source to the per-warp kernel (plans then hold no scratch for it).
 bool block_kernel_enabled() {
     const char *e = getenv("CS_BLOCK_PER_SOURCE");
     return !(e && e[0] == '0');
+}
+
+// Schedule of one call: one block per source gives a source a whole SM (the lowest latency per
+// source) and one warp per source keeps ~24 sources per SM in flight (the highest throughput).  Calls
+// with at most CS_BLOCK_SOURCES_MAX sources (default: 2 per SM) take the block kernel, larger ones
+// the per-warp kernel; CS_BLOCK_PER_SOURCE=1 forces the block kernel.
+bool block_schedule(long long n_src) {
+    const char *e = getenv("CS_BLOCK_PER_SOURCE");
+    if (e && e[0] == '0') return false;
+    if (e && e[0] == '1') return true;
+    const char *m = getenv("CS_BLOCK_SOURCES_MAX");
+    const long long cap = m ? atoll(m) : 2ll * std::max(1, sm_count());
+    return n_src <= cap;
 }
 
 // Settle-order sort: distance buckets by default, CS_SORT=radix selects the LSD radix sort.
@@ -1714,7 +1727,7 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     if (plan->n_bound > 0 && plan->n_bound != g->n_bound)
         return fail(CS_ERR_ARG, "plan was made for a graph of another node bound");
     const bool block = (mode == cs::MODE_SHORTEST || mode == cs::MODE_OD) && plan->cta_blocks > 0 &&
-                       cs::cta::supported(P, K) && block_kernel_enabled();
+                       cs::cta::supported(P, K) && q && block_schedule(q->n_sources);
     Layout lay = layout(g->n_bound, plan->n_slots, plan->cap, P, plan->lanes, plan->cta_blocks);
     if (ws_bytes < lay.total) return fail(CS_ERR_ARG, "workspace too small for this plan");
     cudaStream_t stream = (cudaStream_t)stream_v;

@@ -203,3 +203,23 @@ def test_beta_seed_exp_f64_accuracy():
     want = w.astype(np.float64) * np.exp(-(beta.astype(np.float64) * cost.astype(np.float64)))
     rel = np.abs(got - want) / np.maximum(want, 1e-200)
     assert rel.max() < 5e-14, (rel.max(), int(rel.argmax()))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schedule", ["0", "1"])
+def test_both_schedules_against_the_oracle(schedule, monkeypatch):
+    """A call runs one warp per source (throughput) or one block per source (latency) by its source
+    count; each schedule, forced for every call, matches the oracle: C1 with every source, a 2%
+    tolerance, sampling weights and a source subset."""
+    monkeypatch.setenv("CS_BLOCK_PER_SOURCE", schedule)
+    p, dists = synth.lattice_config("c1")
+    ns = synth.primal_structure(p)
+    res, ref, _, d = _run(ns, dists)
+    _compare(ns, res, ref, d, what=f"c1 schedule {schedule}")
+    p24, dists24 = synth.lattice_config("c1", side=24)
+    ns24 = synth.primal_structure(p24)
+    res, ref, _, d = _run(ns24, dists24, tolerance=2.0)
+    _compare(ns24, res, ref, d, what=f"tolerance 2% schedule {schedule}")
+    res, ref, reach, d = _run(ns24, dists24, source_indices=list(range(0, 576, 7)))
+    _compare(ns24, res, ref, d, what=f"subset schedule {schedule}")
+    assert res.reachability_totals == [int(x) for x in reach]
