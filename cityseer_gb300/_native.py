@@ -62,6 +62,17 @@ class DualGraph(C.Structure):
     ]
 
 
+class DataMapArrays(C.Structure):
+    """cs_data_map: a data layer's node assignments as device arrays."""
+
+    _fields_ = [
+        ("n_entries", C.c_int32), ("n_assign", C.c_int32), ("n_groups", C.c_int32),
+        ("node_ptr", _ptr), ("assign_entry", _ptr), ("assign_dist", _ptr), ("assign_node", _ptr),
+        ("assign_rank", _ptr), ("entry_group", _ptr), ("entry_class", _ptr), ("group_ptr", _ptr),
+        ("group_assign", _ptr),
+    ]
+
+
 class Query(C.Structure):
     _fields_ = [
         ("k", C.c_int32),
@@ -183,6 +194,11 @@ SIGNATURES = {
     "cs_segment_centrality": (
         C.c_int32,
         [C.POINTER(PrimalGraph), C.POINTER(Query), C.POINTER(Plan), _ptr, C.c_size_t, Outputs, _ptr],
+    ),
+    "cs_accessibility": (
+        C.c_int32,
+        [C.POINTER(PrimalGraph), C.POINTER(DataMapArrays), C.POINTER(Query), _ptr, C.c_int32, C.POINTER(Plan), _ptr,
+         C.c_size_t, _ptr, _ptr, _ptr, _ptr],
     ),
     "cs_tree_shortest": (
         C.c_int32,

@@ -102,7 +102,8 @@ __host__ __device__ inline SlotPtrs slot_ptrs(char *dense, size_t dense_stride, 
 }
 
 // BOTH: batched jobs only.  OD: betweenness seeded by an origin-destination matrix.
-enum Mode { MODE_SHORTEST = 0, MODE_SEGMENT = 1, MODE_TREE = 2, MODE_BOTH = 3, MODE_OD = 4 };
+// ACCESS: accessibility sums over data assigned to the reached nodes.
+enum Mode { MODE_SHORTEST = 0, MODE_SEGMENT = 1, MODE_TREE = 2, MODE_BOTH = 3, MODE_OD = 4, MODE_ACCESS = 5 };
 
 struct PrimalParams {
     cs_primal_graph g;
@@ -140,6 +141,12 @@ struct PrimalParams {
     const int32_t *od_ptr, *od_dst;
     const float *od_w;
     int32_t radix_sort;  // settle-order sort: 0 distance buckets, 1 LSD radix
+    // MODE_ACCESS: the data map (cs_data_map) and the per-class rows
+    cs_data_map dm;
+    float mcw[MAXK];   // max curve weights (clip_wts_curve)
+    float max_dist;    // the largest distance threshold (metres)
+    double *acc_unw, *acc_wt;  // [n_classes][K][n_bound]
+    uint32_t *acc_near;        // [n_classes][n_bound] f32 bits of the nearest distance
 };
 
 // ------------------------------------------------------------------------------------------
@@ -474,6 +481,18 @@ __device__ __forceinline__ int first_k(const PrimalParams &p, float c) {
     return k;
 }
 
+// Dependency lanes of the backward sweep: the node at settle position i holds the lanes of the
+// thresholds it lies within (k >= k0(i)), plain and beta-weighted interleaved, packed in settle
+// order.  Positions are sorted by cost, so k0 steps up at the boundaries nk[k] (positions with cost
+// <= d_k) and the offsets follow from them: lane (i, k, b) sits at lane_index(i) + 2 k + b.
+// nk[] and cum[] (cum[k] = lanes held by the positions below nk[k - 1]) are the warp's shared rows.
+__device__ __forceinline__ int lane_index(int i, int K, const int *nk, const int *cum) {
+    int k0 = 0;
+    while (k0 < K && i >= nk[k0]) k0++;
+    const int lo = k0 ? nk[k0 - 1] : 0;
+    return 2 * (cum[k0] + (i - lo) * (K - k0)) - 2 * k0;
+}
+
 // predecessor positions of the node at position i, in registers
 template <int PM>
 __device__ __forceinline__ int load_preds(const SlotPtrs &s, int i, int P, int *pl) {
@@ -524,8 +543,29 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     const float wt = OD ? 1.0f : __ldg(&p.src_wt[src]);
     const float cycles_wt = OD ? 0.0f : wt / __ldg(&p.g.node_w_dev[src]);
     const bool closeness = !OD && p.closeness;
-    // cnt[0..K): nodes whose first qualifying threshold is k; cnt[MAXK..MAXK+K): same for edges
+    // cnt[0..K): nodes whose first qualifying threshold is k; cnt[MAXK..MAXK+K): same for edges;
+    // cnt[2 MAXK..): nk, the positions with cost <= d_k; cnt[3 MAXK..): cum, lanes below nk[k - 1]
     for (int q = lane; q < 2 * MAXK; q += 32) cnt[q] = 0;
+    int *nk = cnt + 2 * MAXK, *cum = cnt + 3 * MAXK;
+    if (lane < K) {
+        int lo = 0, hi = R;  // first position whose cost exceeds d_k
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (route_cost(s.sd[mid], p.speed) <= p.dk[lane]) lo = mid + 1;
+            else hi = mid;
+        }
+        nk[lane] = lo;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        int acc = 0, prev = 0;
+        for (int k = 0; k < K; k++) {
+            cum[k] = acc;
+            acc += (nk[k] - prev) * (K - k);
+            prev = nk[k];
+        }
+        cum[K] = acc;
+    }
     __syncwarp();
     // --- one pass over out-edges in settle order, 32 nodes at a time: circuit-rank counts, the
     // predecessor replay and, with betweenness, sigma (f64 path counts, as the reference's
@@ -533,8 +573,7 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
     // done.  The same pass zeroes each node's dependency lanes for the backward sweep.
     bool bad = false;
     double *sig = s.sig;
-    const int L = p.L;  // 2K f64 lanes per node: [0,K) plain, [K,2K) beta-weighted
-    double *dl = s.dl;
+    double *dl = s.dl;  // dependency lanes, packed (lane_index)
     for (int base = 0; base < R; base += 32) {
         const int i = base + lane;
         const bool act = i < R;
@@ -587,7 +626,11 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
                 for (int j = 0; j < PM; j++)
                     if ((pm >> j) & 1u) sg = __dadd_rn(sg, sig[nb.pos[j]]);
                 sig[i] = sg;
-                for (int q = 0; q < 2 * K; q++) dl[(size_t)i * L + q] = 0.0;
+                const int li0 = lane_index(i, K, nk, cum);
+                for (int k = first_k(p, route_cost(s.sd[i], p.speed)); k < K; k++) {
+                    dl[li0 + 2 * k] = 0.0;
+                    dl[li0 + 2 * k + 1] = 0.0;
+                }
                 mine = true;
             }
             __syncwarp();
@@ -691,18 +734,18 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
                 for (int r = 0; r < BW; r++) {
                     if (r < np) {
                         const double sv = sig[pl[r]];
-                        bw_pl[r * 32 + lane] = pl[r];
+                        bw_pl[r * 32 + lane] = lane_index(pl[r], K, nk, cum);
                         bw_fr[r * 32 + lane] = (sv == sw) ? 1.0 : __ddiv_rn(sv, sw);
                     }
                 }
-                double *dli = dl + (size_t)i * L;
+                double *dli = dl + lane_index(i, K, nk, cum);
                 const int k0 = first_k(p, cost);
                 for (int k = k0; k < K; k++) {
                     if (sw == 0.0) break;
                     const double seed = (i == 0) ? 0.0 : pair;
                     const double seedb = (i == 0 || pairf == 0.0f) ? 0.0 : seed_exp(pairf, p.beta[k], cost);
-                    const double dep = __dadd_rn(seed, __ldcg(&dli[k]));
-                    const double depb = __dadd_rn(seedb, __ldcg(&dli[K + k]));
+                    const double dep = __dadd_rn(seed, __ldcg(&dli[2 * k]));
+                    const double depb = __dadd_rn(seedb, __ldcg(&dli[2 * k + 1]));
                     if (dep == 0.0 && depb == 0.0) continue;
 #pragma unroll 1
                     for (int r = 0; r < np; r++) {
@@ -712,14 +755,15 @@ CS_PHASE_INLINE __device__ void shortest_accumulate(const PrimalParams &p, const
                             q = bw_pl[r * 32 + lane];
                             f = bw_fr[r * 32 + lane];
                         } else {  // beyond the shared column (high-degree graphs): from the scratch
-                            q = s.pr[(size_t)i * P + r];
-                            const double sv = sig[q];
+                            const int qp = s.pr[(size_t)i * P + r];
+                            const double sv = sig[qp];
                             f = (sv == sw) ? 1.0 : __ddiv_rn(sv, sw);
+                            q = lane_index(qp, K, nk, cum);
                         }
                         if (f == 0.0) continue;
-                        double *pd = dl + (size_t)q * L;
-                        atomicAdd(&pd[k], f == 1.0 ? dep : __dmul_rn(f, dep));
-                        atomicAdd(&pd[K + k], f == 1.0 ? depb : __dmul_rn(f, depb));
+                        double *pd = dl + q;
+                        atomicAdd(&pd[2 * k], f == 1.0 ? dep : __dmul_rn(f, dep));
+                        atomicAdd(&pd[2 * k + 1], f == 1.0 ? depb : __dmul_rn(f, depb));
                     }
                     if (v == src) continue;
                     const double credit = __dadd_rn(dep, -seed);
@@ -1016,6 +1060,63 @@ CS_PHASE_INLINE __device__ void tree_rows(const PrimalParams &p, const SlotPtrs 
 }
 
 // ------------------------------------------------------------------------------------------
+// 4d. Accessibility of one source (rust/src/data.rs:513-602 aggregate_to_src_idx, :688-731).
+//     Over the reached nodes (the search's distances are dijkstra_tree_shortest's), each assigned
+//     entry's total distance (network + assignment, f32); an entry counts when it is the nearest
+//     of its dedupe key (ties: the lower (node seconds, node, rank in the node's list), the
+//     reference keeping the first one it meets), and adds to its class's rows.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void access_accumulate(const PrimalParams &p, const SlotPtrs &s, int src, int R) {
+    const int lane = lane_id();
+    const cs_data_map &dm = p.dm;
+    const int K = p.k, N = p.g.n_bound;
+    const float maxs = p.maxsec;
+    const float max_walk = fmul(maxs, p.speed);
+    for (int i = lane; i < R; i += 32) {
+        const int v = s.rl[i];
+        const float sec = __ldcg(&s.dist[v]);
+        if (!(sec < maxs)) continue;
+        const float net = fmul(sec, p.speed);
+        const int a_end = __ldg(&dm.node_ptr_dev[v + 1]);
+        for (int a = __ldg(&dm.node_ptr_dev[v]); a < a_end; a++) {
+            const float tot = fadd(net, __ldg(&dm.assign_dist_dev[a]));
+            if (!(tot <= max_walk)) continue;
+            const int e = __ldg(&dm.assign_entry_dev[a]);
+            const int grp = __ldg(&dm.entry_group_dev[e]);
+            const int rank = __ldg(&dm.assign_rank_dev[a]);
+            bool win = true;
+            const int g_end = __ldg(&dm.group_ptr_dev[grp + 1]);
+            for (int b = __ldg(&dm.group_ptr_dev[grp]); b < g_end && win; b++) {
+                const int a2 = __ldg(&dm.group_assign_dev[b]);
+                if (a2 == a) continue;
+                const int v2 = __ldg(&dm.assign_node_dev[a2]);
+                const float sec2 = __ldcg(&s.dist[v2]);  // +inf when not reached
+                if (!(sec2 < maxs)) continue;
+                const float tot2 = fadd(fmul(sec2, p.speed), __ldg(&dm.assign_dist_dev[a2]));
+                if (!(tot2 <= max_walk)) continue;
+                if (tot2 < tot) win = false;
+                else if (tot2 == tot) {
+                    const int r2 = __ldg(&dm.assign_rank_dev[a2]);
+                    if (sec2 < sec || (sec2 == sec && (v2 < v || (v2 == v && r2 < rank)))) win = false;
+                }
+            }
+            if (!win) continue;
+            const int c = __ldg(&dm.entry_class_dev[e]);
+            if (c < 0) continue;
+            for (int k = 0; k < K; k++) {
+                if (!(tot <= p.dk[k])) continue;
+                const size_t o = ((size_t)c * K + k) * N + src;
+                atomicAdd(&p.acc_unw[o], 1.0);
+                // clipped_beta_wt (rust/src/common.rs:339-348)
+                const float raw = expf(fmul(-p.beta[k], tot));
+                atomicAdd(&p.acc_wt[o], f2d(__fdiv_rn(fminf(raw, p.mcw[k]), p.mcw[k])));
+                if (p.dk[k] == p.max_dist) atomicMin(&p.acc_near[(size_t)c * N + src], __float_as_uint(tot));
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
 // Persistent kernel: each warp owns one scratch slot and pulls sources until the list is empty.
 // ------------------------------------------------------------------------------------------
 // One source on this warp's slot: search, sort, mode-specific accumulation, scratch reset.
@@ -1046,6 +1147,15 @@ __device__ __forceinline__ bool run_source(const PrimalParams &p, const SlotPtrs
         }
         __syncwarp();
         return false;
+    }
+    if constexpr (MODE == MODE_ACCESS) {
+        // no settle order needed: the reached list and the distances suffice
+        access_accumulate(p, s, src, R);
+        __syncwarp();
+        for (int i = lane; i < R; i += 32) s.dist[s.rl[i]] = __int_as_float(INF_BITS);
+        __syncwarp();
+        settled += R;
+        return true;
     }
     warp_sort(p, s, R, dmax, hist);
     __syncwarp();
@@ -1102,7 +1212,7 @@ __device__ __forceinline__ void flush_counters(const PrimalParams &p, long long 
 template <int PM, int MINB, int MODE>
 __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p) {
     __shared__ uint32_t hist_all[8][256];
-    __shared__ int cnt_all[8][2 * MAXK];
+    __shared__ int cnt_all[8][4 * MAXK + 2];
     __shared__ long long ph_all[8][8];
     // backward sweep: each lane's predecessor rows and sigma fractions (column-major per warp)
     __shared__ int bw_pl_all[8][bw_cols(PM) * 32];
@@ -1140,7 +1250,7 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
 template <int PM, int MINB, int WPB, int GW>
 __global__ void __launch_bounds__(WPB * 32, MINB) primal_sync_kernel(const PrimalParams p) {
     __shared__ uint32_t hist_all[WPB][256];
-    __shared__ int cnt_all[WPB][2 * MAXK];
+    __shared__ int cnt_all[WPB][4 * MAXK + 2];
     __shared__ long long ph_all[WPB][8];
     __shared__ int bw_pl_all[WPB][bw_cols(PM) * 32];
     __shared__ double bw_fr_all[WPB][bw_cols(PM) * 32];
@@ -1267,7 +1377,7 @@ template <int PM, int MINB, int MODE>
 __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams base, const cs_batch_job *jobs,
                                                           int n_jobs, long long item_lo, long long item_hi) {
     __shared__ uint32_t hist_all[8][256];
-    __shared__ int cnt_all[8][2 * MAXK];
+    __shared__ int cnt_all[8][4 * MAXK + 2];
     __shared__ long long ph_all[8][8];
     // backward sweep: each lane's predecessor rows and sigma fractions (column-major per warp)
     __shared__ int bw_pl_all[8][bw_cols(PM) * 32];
@@ -1313,7 +1423,7 @@ template <int PM, int MINB>
 __global__ void __launch_bounds__(256, MINB) batch_sync_kernel(const PrimalParams base, const cs_batch_job *jobs,
                                                                int n_jobs, long long item_lo, long long item_hi) {
     __shared__ uint32_t hist_all[8][256];
-    __shared__ int cnt_all[8][2 * MAXK];
+    __shared__ int cnt_all[8][4 * MAXK + 2];
     __shared__ long long ph_all[8][8];
     __shared__ int bw_pl_all[8][bw_cols(PM) * 32];
     __shared__ double bw_fr_all[8][bw_cols(PM) * 32];
@@ -1651,6 +1761,7 @@ cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, c
     if (p.mode == cs::MODE_SHORTEST) launch_primal_mode<cs::MODE_SHORTEST>(p, p.P, minb, blocks, stream);
     else if (p.mode == cs::MODE_SEGMENT) launch_primal_mode<cs::MODE_SEGMENT>(p, p.P, minb, blocks, stream);
     else if (p.mode == cs::MODE_OD) launch_primal_mode<cs::MODE_OD>(p, p.P, minb, blocks, stream);
+    else if (p.mode == cs::MODE_ACCESS) launch_primal_mode<cs::MODE_ACCESS>(p, p.P, minb, blocks, stream);
     else launch_primal_mode<cs::MODE_TREE>(p, p.P, minb, blocks, stream);
     g_counters[3]++;
     cudaError_t e = cudaGetLastError();
@@ -2016,6 +2127,87 @@ cs_status cs_tree_shortest(const cs_primal_graph *g, int32_t n_queries, const in
     cs_outputs o{nullptr, nullptr};
     return run_primal(g, nullptr, plan, workspace_dev, workspace_bytes, o, stream, cs::MODE_TREE, row_cap, count_dev,
                       node_dev, agg_seconds_dev, pred_dev, src_dev, n_queries, max_seconds, speed_m_s, true);
+}
+
+cs_status cs_accessibility(const cs_primal_graph *g, const cs_data_map *dm, const cs_query *q,
+                           const float *max_curve_wts, int32_t n_classes, const cs_plan *plan, void *workspace_dev,
+                           size_t workspace_bytes, double *unweighted_dev, double *weighted_dev,
+                           uint32_t *nearest_dev, void *stream) {
+    cs_status st = validate_primal(g);
+    if (st != CS_OK) return st;
+    if (!dm || !q || !max_curve_wts || !plan || !workspace_dev) return fail(CS_ERR_ARG, "accessibility: NULL argument");
+    if (q->k < 1 || q->k > CS_MAX_THRESHOLDS) return fail(CS_ERR_ARG, "threshold count out of range");
+    if (n_classes < 0) return fail(CS_ERR_ARG, "accessibility: negative class count");
+    if (q->n_sources > 0 && (!dm->node_ptr_dev || !dm->assign_entry_dev || !dm->assign_dist_dev ||
+                             !dm->assign_node_dev || !dm->assign_rank_dev || !dm->entry_group_dev ||
+                             !dm->entry_class_dev || !dm->group_ptr_dev || !dm->group_assign_dev))
+        return fail(CS_ERR_ARG, "accessibility: data map array is NULL");
+    if (n_classes > 0 && q->n_sources > 0 && (!unweighted_dev || !weighted_dev || !nearest_dev))
+        return fail(CS_ERR_ARG, "accessibility: output is NULL");
+    for (int i = 0; i < q->k; i++)
+        if (!(max_curve_wts[i] > 0.0f && max_curve_wts[i] <= 1.0f))
+            return fail(CS_ERR_ARG, "Max curve weight must be in the range [0, 1].");
+    const int P = std::max(1, g->max_out_degree);
+    Layout lay = layout(g->n_bound, plan->n_slots, plan->cap, P, plan->lanes, plan->cta_blocks);
+    if (workspace_bytes < lay.total) return fail(CS_ERR_ARG, "workspace too small for this plan");
+    if (plan->n_bound > 0 && plan->n_bound != g->n_bound)
+        return fail(CS_ERR_ARG, "plan was made for a graph of another node bound");
+    cudaStream_t stream_c = (cudaStream_t)stream;
+    char *base = (char *)workspace_dev;
+    cs::PrimalParams p;
+    memset(&p, 0, sizeof(p));
+    p.g = *g;
+    p.k = q->k;
+    uint32_t maxs = 0, maxd = 0;
+    for (int i = 0; i < q->k; i++) {
+        p.dk[i] = (float)q->distances[i];
+        p.beta[i] = q->betas[i];
+        p.mcw[i] = max_curve_wts[i];
+        maxs = std::max(maxs, q->seconds[i]);
+        maxd = std::max(maxd, q->distances[i]);
+    }
+    p.max_dist = (float)maxd;
+    p.speed = q->speed_m_s;
+    if (!(p.speed > 0.0f) || !std::isfinite(p.speed)) return fail(CS_ERR_ARG, "speed_m_s must be finite and positive");
+    p.tol = cs::TIE_EPSILON;
+    p.maxsec = (float)maxs;
+    p.delta = plan->delta_seconds > 0.0f ? plan->delta_seconds : std::max(1.0f, p.maxsec / 48.0f);
+    p.src_list = q->sources_dev;
+    p.n_src = q->n_sources;
+    p.dm = *dm;
+    p.acc_unw = unweighted_dev;
+    p.acc_wt = weighted_dev;
+    p.acc_near = nearest_dev;
+    p.hdr = (cs::WsHeader *)(base + lay.hdr_off);
+    p.failed = (int32_t *)(base + lay.failed_off);
+    p.fail_cap = lay.fail_cap;
+    p.dense = base + lay.dense_off;
+    p.dense_stride = lay.dense_stride;
+    p.compact = base + lay.compact_off;
+    p.cap = plan->cap;
+    p.P = P;
+    p.L = plan->lanes;
+    p.mode = cs::MODE_ACCESS;
+    p.radix_sort = radix_sort_choice();
+    g_counters[0] = g_counters[1] = g_counters[2] = g_counters[3] = 0;
+    if (p.n_src <= 0 || n_classes == 0) return CS_OK;
+    cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), stream_c);
+    if (e != cudaSuccess) return cuda_fail(e, "workspace header reset");
+    st = launch_primal(p, plan, plan->n_slots, stream_c);
+    if (st != CS_OK) return st;
+    cs::WsHeader h;
+    e = cs::read_header(p.hdr, h, stream_c, true);
+    if (e != cudaSuccess) return cuda_fail(e, "accessibility kernel");
+    if (h.err != 0u) return fail((cs_status)h.err, "device-side check failed (code " + std::to_string(h.err) + ")");
+    if (h.n_failed > 0u) {
+        st = retry_chain(p, plan, lay, base, g->n_bound, P, h, stream_c, true,
+                         [&](cs::PrimalParams &p2, int slots2) { return launch_primal(p2, plan, slots2, stream_c); });
+        if (st != CS_OK) return st;
+    }
+    g_counters[0] = (long long)h.sources_done;
+    g_counters[1] = (long long)h.edges_relaxed;
+    g_counters[2] = (long long)h.nodes_settled;
+    return CS_OK;
 }
 
 }  // extern "C"

@@ -95,6 +95,27 @@ typedef struct {
     const uint8_t *eligible_dev;  /* [n_bound] source_eligible (pair weights 0.5 vs 1.0) */
 } cs_query;
 
+/* A data layer assigned to street nodes (DataMap.node_data_map, rust/src/data.rs:380-510), as
+ * device arrays.  Assignments are indexed a: node_ptr delimits each node's assignments (in the
+ * map's order); assign_entry / assign_dist / assign_node / assign_rank give each one's data entry,
+ * distance to the node (f32 of the f64), node and rank within the node's list.  entry_group is the
+ * entry's dedupe key as a group id, entry_class its land-use class (-1: not an accessibility key);
+ * group_ptr / group_assign list each group's assignments. */
+typedef struct {
+    int32_t n_entries;
+    int32_t n_assign;
+    int32_t n_groups;
+    const int32_t *node_ptr_dev;     /* [n_bound + 1] */
+    const int32_t *assign_entry_dev; /* [n_assign] */
+    const float *assign_dist_dev;    /* [n_assign] */
+    const int32_t *assign_node_dev;  /* [n_assign] */
+    const int32_t *assign_rank_dev;  /* [n_assign] */
+    const int32_t *entry_group_dev;  /* [n_entries] */
+    const int32_t *entry_class_dev;  /* [n_entries] */
+    const int32_t *group_ptr_dev;    /* [n_groups + 1] */
+    const int32_t *group_assign_dev; /* [n_assign] */
+} cs_data_map;
+
 /* Launch plan: how many concurrent per-source searches and how much workspace they need. */
 typedef struct {
     int32_t n_slots;      /* concurrent searches (one warp each) */
@@ -242,6 +263,20 @@ cs_status cs_betweenness_od_shortest(const cs_primal_graph *g, const cs_query *q
  * q->sources_dev lists the live sources (segment centrality has no sampling). */
 cs_status cs_segment_centrality(const cs_primal_graph *g, const cs_query *q, const cs_plan *plan,
                                 void *workspace_dev, size_t workspace_bytes, cs_outputs out, void *stream);
+
+/* Replaces DataMap.accessibility (rust/src/data.rs:605-740) with angular = False: per listed source
+ * (q->sources_dev, the live nodes), a shortest-path search to the largest threshold, then its
+ * reachable entries (aggregate_to_src_idx, :513-602: network + assignment distance within the
+ * threshold, the nearest entry of each dedupe key) summed per class and threshold: unweighted
+ * (count) and weighted (clipped_beta_wt with max_curve_wts[k], common.rs:339-348) rows
+ * [n_classes][k][n_bound], zeroed by the caller, and the nearest distance within the largest
+ * threshold [n_classes][n_bound] as f32 bits, set to +inf by the caller.  q's betas and seconds are
+ * pair_distances_betas_time's; its sampling, closeness and betweenness fields are ignored.  Plans
+ * from cs_plan_primal (mode 2) serve this call. */
+cs_status cs_accessibility(const cs_primal_graph *g, const cs_data_map *dm, const cs_query *q,
+                           const float *max_curve_wts, int32_t n_classes, const cs_plan *plan, void *workspace_dev,
+                           size_t workspace_bytes, double *unweighted_dev, double *weighted_dev,
+                           uint32_t *nearest_dev, void *stream);
 
 /* Replaces NetworkStructure.dijkstra_tree_shortest (rust/src/centrality.rs:1141-1200, 1500-1508)
  * for a batch of sources: per query q, visited nodes in settle order with their agg_seconds and

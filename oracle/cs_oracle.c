@@ -1243,3 +1243,92 @@ int32_t og_sizeof_desc(void) { return (int32_t)sizeof(og_graph_desc); }
 void og_get_slots(const og_graph *g, int32_t *out) {
     memcpy(out, g->slots, sizeof(int32_t) * 2 * (size_t)g->d.n_bound);
 }
+
+/* ------------------------------------------------------------------------------------------ */
+/* Data aggregation (rust/src/data.rs:513-602 aggregate_to_src_idx, :605-740 accessibility).   */
+/* ------------------------------------------------------------------------------------------ */
+/* node_data_map as CSR: per node, its (entry, node_dist) assignments in the map's Vec order
+   (data.rs:484-499); entry_group: the entry's dedupe key as a group id. */
+typedef struct {
+    int64_t n_entries, n_groups;
+    const int64_t *nd_ptr;     /* [n_bound + 1] */
+    const int64_t *nd_entry;   /* [n_assign] */
+    const double *nd_dist;     /* [n_assign] */
+    const int64_t *entry_group;/* [n_entries] */
+} og_data;
+
+/* aggregate_to_src_idx: entry_dist[e] = the reachable entry's total distance (f32), NaN when the
+   entry is not in the result map.  Scratch: group_best [n_groups] f32, group_entry [n_groups]. */
+int64_t og_aggregate(const og_graph *g, const og_data *d, int64_t src, uint32_t max_seconds, float speed,
+                     int32_t angular, float *entry_dist, float *group_best, int64_t *group_entry) {
+    const int64_t n = g->d.n_bound;
+    int64_t *visited = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+    nvisit *tree = (nvisit *)malloc(sizeof(nvisit) * (size_t)(n > 0 ? n : 1));
+    const int64_t nv = angular ? og_tree_simplest(g, src, max_seconds, speed, visited, tree)
+                               : og_tree_shortest(g, src, max_seconds, speed, visited, tree);
+    for (int64_t q = 0; q < d->n_groups; q++) { group_best[q] = INFINITY; group_entry[q] = -1; }
+    for (int64_t e = 0; e < d->n_entries; e++) entry_dist[e] = NAN;
+    const float max_walk_dist = (float)max_seconds * speed;
+    for (int64_t i = 0; i < nv; i++) {
+        const int64_t node = visited[i];
+        const nvisit *nvz = &tree[node];
+        if (nvz->agg_seconds >= (float)max_seconds) continue;
+        for (int64_t a = d->nd_ptr[node]; a < d->nd_ptr[node + 1]; a++) {
+            const int64_t e = d->nd_entry[a];
+            const float network_dist = nvz->agg_seconds * speed;
+            const float total = network_dist + (float)d->nd_dist[a];
+            if (!(total <= max_walk_dist)) continue;
+            const int64_t q = d->entry_group[e];
+            if (group_entry[q] < 0 || total < group_best[q]) {  /* vacant, or strictly better */
+                group_best[q] = total;
+                group_entry[q] = e;
+            }
+        }
+    }
+    int64_t cnt = 0;
+    for (int64_t q = 0; q < d->n_groups; q++)
+        if (group_entry[q] >= 0) { entry_dist[group_entry[q]] = group_best[q]; cnt++; }
+    free(visited);
+    free(tree);
+    return cnt;
+}
+
+/* accessibility (data.rs:605-740) for live sources: entry_class [n_entries] (-1: not an
+   accessibility key), k thresholds (distances, betas, max curve weights), out rows
+   unweighted/weighted [n_classes][k][n_bound] (zeroed) and nearest [n_classes][n_bound] (NaN). */
+int og_accessibility(const og_graph *g, const og_data *d, const int32_t *entry_class, int32_t n_classes, int32_t k,
+                     const uint32_t *distances, const float *betas, const float *mcw, uint32_t max_seconds,
+                     float speed, int32_t angular, double *unweighted, double *weighted, double *nearest) {
+    const int64_t n = g->d.n_bound;
+    uint32_t max_dist = 0;
+    for (int32_t i = 0; i < k; i++) if (distances[i] > max_dist) max_dist = distances[i];
+    float *edist = (float *)malloc(sizeof(float) * (size_t)(d->n_entries > 0 ? d->n_entries : 1));
+    float *gb = (float *)malloc(sizeof(float) * (size_t)(d->n_groups > 0 ? d->n_groups : 1));
+    int64_t *ge = (int64_t *)malloc(sizeof(int64_t) * (size_t)(d->n_groups > 0 ? d->n_groups : 1));
+    for (int64_t src = 0; src < n; src++) {
+        if (!g->d.node_exists[src] || !g->d.live[src]) continue;
+        og_aggregate(g, d, src, max_seconds, speed, angular, edist, gb, ge);
+        for (int64_t e = 0; e < d->n_entries; e++) {
+            const float data_dist = edist[e];
+            if (isnan(data_dist)) continue;
+            const int32_t c = entry_class[e];
+            if (c < 0) continue;
+            for (int32_t i = 0; i < k; i++) {
+                if (!(data_dist <= (float)distances[i])) continue;
+                unweighted[((size_t)c * k + i) * n + src] += 1.0;
+                /* clipped_beta_wt (common.rs:339-348) */
+                const float raw = expf(-betas[i] * data_dist);
+                const float wt = fminf(raw, mcw[i]) / mcw[i];
+                weighted[((size_t)c * k + i) * n + src] += (double)wt;
+                if (distances[i] == max_dist) {
+                    double *cur = &nearest[(size_t)c * n + src];
+                    if (isnan(*cur) || (double)data_dist < *cur) *cur = (double)data_dist;
+                }
+            }
+        }
+    }
+    free(edist);
+    free(gb);
+    free(ge);
+    return 0;
+}

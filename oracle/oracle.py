@@ -382,3 +382,62 @@ def seconds_from_distances(dists, speed):
 
 def default_threads() -> int:
     return max(1, (os.cpu_count() or 2) - 1)
+
+
+class _Data(C.Structure):
+    _fields_ = [("n_entries", C.c_int64), ("n_groups", C.c_int64), ("nd_ptr", _P), ("nd_entry", _P),
+                ("nd_dist", _P), ("entry_group", _P)]
+
+
+def _data_struct(t):
+    keep = {
+        "nd_ptr": np.ascontiguousarray(t["ptr"], np.int64),
+        "nd_entry": np.ascontiguousarray(t["a_entry"], np.int64),
+        "nd_dist": np.ascontiguousarray(t["a_dist"], np.float64),
+        "entry_group": np.ascontiguousarray(t["entry_group"], np.int64),
+    }
+    dd = _Data()
+    dd.n_entries = len(t["keys"])
+    dd.n_groups = int(t["n_groups"])
+    for k, v in keep.items():
+        setattr(dd, k, v.ctypes.data if len(v) else None)
+    return dd, keep
+
+
+def aggregate(og: OracleGraph, t: dict, src: int, max_seconds: int, speed: float, angular: bool = False):
+    """aggregate_to_src_idx (rust/src/data.rs:513-602) on the tables of DataMap._tables: f32 total
+    distance per entry, NaN when not reachable."""
+    L = lib()
+    L.og_aggregate.restype = C.c_int64
+    L.og_aggregate.argtypes = [_P, C.POINTER(_Data), C.c_int64, C.c_uint32, C.c_float, C.c_int32, _P, _P, _P]
+    dd, keep = _data_struct(t)
+    ne, ng = len(t["keys"]), int(t["n_groups"])
+    out = np.zeros(max(ne, 1), np.float32)
+    gb = np.zeros(max(ng, 1), np.float32)
+    ge = np.zeros(max(ng, 1), np.int64)
+    L.og_aggregate(og.h, C.byref(dd), int(src), int(max_seconds), C.c_float(speed), int(bool(angular)),
+                   out.ctypes.data, gb.ctypes.data, ge.ctypes.data)
+    return out[:ne]
+
+
+def accessibility(og: OracleGraph, t: dict, n_classes: int, dists, betas, mcw, max_seconds: int, speed: float,
+                  angular: bool = False):
+    """accessibility (rust/src/data.rs:605-740): unweighted, weighted [C][K][n_bound] and nearest
+    [C][n_bound] (NaN when none) for every live node."""
+    L = lib()
+    L.og_accessibility.restype = C.c_int
+    L.og_accessibility.argtypes = [_P, C.POINTER(_Data), _P, C.c_int32, C.c_int32, _P, _P, _P, C.c_uint32, C.c_float,
+                                   C.c_int32, _P, _P, _P]
+    dd, keep = _data_struct(t)
+    k = len(dists)
+    cls = np.ascontiguousarray(t["entry_class"], np.int32)
+    dist_a = np.ascontiguousarray(dists, np.uint32)
+    beta_a = np.ascontiguousarray(betas, np.float32)
+    mcw_a = np.ascontiguousarray(mcw, np.float32)
+    u = np.zeros((n_classes, k, og.nb))
+    w = np.zeros((n_classes, k, og.nb))
+    n = np.full((n_classes, og.nb), np.nan)
+    L.og_accessibility(og.h, C.byref(dd), cls.ctypes.data, int(n_classes), k, dist_a.ctypes.data, beta_a.ctypes.data,
+                       mcw_a.ctypes.data, int(max_seconds), C.c_float(speed), int(bool(angular)), u.ctypes.data,
+                       w.ctypes.data, n.ctypes.data)
+    return u, w, n

@@ -5,6 +5,7 @@ Reads (as text, with the ast module; nothing from the reference is imported or e
   tests/conftest.py                   diamond / box / parallel_segments fixture graphs
   tests/rustalgos/test_centrality.py  golden vectors asserted in test_local_centrality_all and the
                                       expected paths of test_shortest_path_trees
+  tests/rustalgos/test_data.py        node -> data key targets of test_assign_to_network
 
 Usage: python tests/golden/make_fixtures.py REFERENCE_ROOT   (the cityseer-api source tree)
 """
@@ -120,6 +121,19 @@ def helper_graphs(ref: Path) -> dict:
     return out
 
 
+def data_assignment_targets(ref: Path) -> dict:
+    """The node -> data keys targets asserted by test_assign_to_network
+    (tests/rustalgos/test_data.py): primal_targets and decomp_targets (module-level dicts)."""
+    tree = ast.parse((ref / "tests/rustalgos/test_data.py").read_text())
+    out = {}
+    for st in tree.body:
+        if isinstance(st, ast.Assign) and isinstance(st.targets[0], ast.Name):
+            name = st.targets[0].id
+            if name in ("primal_targets", "decomp_targets"):
+                out[name] = {str(k): v for k, v in _literal(st.value).items()}
+    return out
+
+
 def main(ref: Path) -> None:
     data = {
         "reference": "cityseer-api v4.24.0",
@@ -127,6 +141,7 @@ def main(ref: Path) -> None:
         "conftest": conftest_graphs(ref),
         "centrality": centrality_golden(ref),
         "helpers": helper_graphs(ref),
+        "data_assignment": data_assignment_targets(ref),
     }
     (HERE / "reference_fixtures.json").write_text(json.dumps(data, indent=1))
     print("wrote", HERE / "reference_fixtures.json")
