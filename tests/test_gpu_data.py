@@ -99,3 +99,23 @@ def test_aggregate_to_src_idx_and_angular():
     dmd, lud = _layer(xs, ys, groups, classes)
     dmd.assign_data_to_network(nsd, 400, 6)
     _check(nsd, dmd, lud, [400, 800], angular=True)
+
+
+@pytest.mark.gpu
+def test_compute_accessibilities_columns():
+    from cityseer_gb300.metrics import layers
+
+    g = mock_graph()
+    ns = structure(g)[2]
+    xs, ys, groups, classes = _points(g, 40, 11)
+    data = {"geometry": list(zip(xs, ys)), "landuse": list(classes), "data_id": list(groups)}
+    nodes, _ = layers.compute_accessibilities(data, "landuse", ["a", "z"], None, ns, max_netw_assign_dist=400,
+                                              distances=[400, 800], data_id_col="data_id")
+    dm, lu = _layer(xs, ys, groups, classes)
+    dm.assign_data_to_network(ns, 400, 50)
+    raw = dm.accessibility(ns, lu, ["a", "z"], distances=[400, 800])
+    for key in ("a", "z"):
+        for d in (400, 800):
+            np.testing.assert_array_equal(nodes[f"cc_{key}_{d}_nw"], raw.result[key].unweighted[d])
+            np.testing.assert_allclose(nodes[f"cc_{key}_{d}_wt"], raw.result[key].weighted[d], rtol=1e-12)
+        np.testing.assert_array_equal(nodes[f"cc_{key}_nearest_max_800"], raw.result[key].distance[800])
