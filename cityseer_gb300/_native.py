@@ -243,6 +243,7 @@ SIGNATURES = {
         [C.POINTER(PrimalGraph), C.POINTER(Query), Outputs, _ptr],
     ),
     "cs_debug_seed_exp": (C.c_int32, [_ptr, _ptr, _ptr, _ptr, C.c_int64, _ptr]),
+    "cs_workspace_progress": (C.c_int32, [_ptr, C.POINTER(C.c_int64)]),
 }
 
 _lib = None

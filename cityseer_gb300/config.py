@@ -62,8 +62,9 @@ def log_thresholds(distances=None, betas=None, minutes=None, min_threshold_wt: f
 
 
 def wrap_progress(total: int, rust_struct, partial_func: Callable, desc: str | None = None):
-    """Runs partial_func on a worker thread and polls rust_struct.progress(), re-raising worker
-    exceptions (pysrc/cityseer/config.py:96-130).  Progress is reported when the call returns."""
+    """Runs partial_func on a worker thread and polls rust_struct.progress() meanwhile (live for
+    NetworkStructure calls: the kernels count completed sources on the device), re-raising worker
+    exceptions (pysrc/cityseer/config.py:96-130)."""
     q: Queue = Queue()
 
     def worker():

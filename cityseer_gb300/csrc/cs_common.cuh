@@ -77,6 +77,11 @@ __device__ __forceinline__ double f2d(float x) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
+// Sources completed so far in the current call, counted as they finish (read on a side stream by
+// cs_workspace_progress while the kernels run): the header's pad[PROGRESS_SLOT].
+constexpr int PROGRESS_SLOT = 8;
+__device__ __forceinline__ void count_progress(WsHeader *h) { atomicAdd(&h->pad[PROGRESS_SLOT], 1ull); }
+
 __device__ __forceinline__ void raise_err(WsHeader *h, unsigned code, unsigned where) {
     if (atomicCAS(&h->err, 0u, code) == 0u) h->err_where = where;
 }

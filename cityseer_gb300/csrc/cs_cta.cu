@@ -846,6 +846,7 @@ __global__ void __launch_bounds__(TPB, 1) source_block_kernel(const Params p) {
         ph[5] += t1 - t0;
         settled += v.R;
         done_src++;
+        if (tid == 0) count_progress(p.hdr);
         __syncthreads();
         if (v.err) break;
     }

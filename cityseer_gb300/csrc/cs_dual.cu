@@ -891,7 +891,10 @@ __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
         if (idx >= (unsigned long long)p.n_src) break;
         if (__ldcg(&p.hdr->err) != 0u) break;
         const int li = p.remap ? p.remap[idx] : (int)idx;
-        if (run_dual_source(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], relaxed, settled)) done_src++;
+        if (run_dual_source(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], relaxed, settled)) {
+            done_src++;
+            if (lane_id() == 0) count_progress(p.hdr);
+        }
     }
     flush_dual_counters(p, relaxed, settled, done_src);
 }

@@ -1234,8 +1234,10 @@ __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p)
         if (__ldcg(&p.hdr->err) != 0u) break;
         const int li = p.remap ? p.remap[idx] : (int)idx;
         if (run_source<PM, MODE>(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], bw_pl_all[wib], bw_fr_all[wib],
-                                 ph, relaxed, settled))
+                                 ph, relaxed, settled)) {
             done_src++;
+            if (lane == 0) count_progress(p.hdr);
+        }
     }
     flush_counters(p, ph, relaxed, settled, done_src);
 }
@@ -1321,6 +1323,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB) primal_sync_kernel(const Prima
             }
             settled += R;
             done_src++;
+            if (lane == 0) count_progress(p.hdr);
         }
         __syncwarp();
         phase_mark(ph, 6, t0);
@@ -1411,8 +1414,10 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
         const int li = (int)(item - jobs[jb].item_begin);
         // failures record the global item index
         if (run_source<PM, MODE>(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], bw_pl_all[wib],
-                                 bw_fr_all[wib], ph, relaxed, settled))
+                                 bw_fr_all[wib], ph, relaxed, settled)) {
             done_src++;
+            if (lane == 0) count_progress(base.hdr);
+        }
     }
     flush_counters(base, ph, relaxed, settled, done_src);
 }
@@ -1509,6 +1514,7 @@ __global__ void __launch_bounds__(256, MINB) batch_sync_kernel(const PrimalParam
             }
             settled += R;
             done_src++;
+            if (lane == 0) count_progress(p.hdr);
         }
         __syncwarp();
         phase_mark(ph, 6, t0);
@@ -2539,6 +2545,24 @@ extern "C" cs_status cs_debug_seed_exp(const float *w_dev, const float *beta_dev
     cs::seed_check_kernel<<<blocks, 256, 0, st>>>(w_dev, beta_dev, cost_dev, out_dev, n);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CS_OK : cuda_fail(e, "seed_check_kernel launch");
+}
+
+// Live progress: the completed-source count the kernels keep in the workspace header, copied on a
+// stream of its own (so it does not wait for the call's kernels) into pinned memory of this thread.
+extern "C" cs_status cs_workspace_progress(const void *workspace_dev, int64_t *sources_done) {
+    if (!workspace_dev || !sources_done) return fail(CS_ERR_ARG, "workspace/sources_done is NULL");
+    thread_local unsigned long long *pinned = nullptr;
+    thread_local cudaStream_t side = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!pinned) e = cudaHostAlloc((void **)&pinned, sizeof(unsigned long long), cudaHostAllocDefault);
+    if (e == cudaSuccess && !side) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "progress buffer");
+    const cs::WsHeader *h = (const cs::WsHeader *)workspace_dev;
+    e = cudaMemcpyAsync(pinned, &h->pad[cs::PROGRESS_SLOT], sizeof(unsigned long long), cudaMemcpyDeviceToHost, side);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(side);
+    if (e != cudaSuccess) return cuda_fail(e, "progress read");
+    *sources_done = (int64_t)*pinned;
+    return CS_OK;
 }
 
 extern "C" cs_status cs_abi_sizes(int32_t *out, int32_t n) {

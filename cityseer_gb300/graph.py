@@ -325,7 +325,28 @@ class NetworkStructure:
         self._progress = 0
 
     def progress(self) -> int:
+        """Sources processed by the running centrality call, read live from its workspace on the
+        device (rust/src/graph.rs:387-415); after the call, the sources it processed."""
+        if getattr(self, "_running", False):
+            ws = self._cache.get("wsd" if self._is_dual else "ws")
+            if ws is not None:
+                import ctypes as C
+
+                from . import _native
+
+                n = C.c_int64(0)
+                if _native.load().cs_workspace_progress(ws.ptr, C.byref(n)) == _native.CS_OK:
+                    return int(n.value)
         return self._progress
+
+    def _run(self, fn, *args, **kwargs):
+        """Runs a centrality call with progress() reading the device counter meanwhile."""
+        self._progress = 0
+        self._running = True
+        try:
+            return fn(self, *args, **kwargs)
+        finally:
+            self._running = False
 
     @property
     def is_dual(self) -> bool:
@@ -780,8 +801,8 @@ class NetworkStructure:
                             pbar_disabled=None):
         from . import centrality
 
-        return centrality.centrality_shortest(
-            self, distances=distances, betas=betas, minutes=minutes, compute_closeness=compute_closeness,
+        return self._run(
+            centrality.centrality_shortest, distances=distances, betas=betas, minutes=minutes, compute_closeness=compute_closeness,
             compute_betweenness=compute_betweenness, min_threshold_wt=min_threshold_wt, speed_m_s=speed_m_s,
             tolerance=tolerance, sample_probability=sample_probability, sampling_weights=sampling_weights,
             random_seed=random_seed, source_indices=source_indices, pbar_disabled=pbar_disabled)
@@ -792,8 +813,8 @@ class NetworkStructure:
                             sampling_weights=None, random_seed=None, source_indices=None, pbar_disabled=None):
         from . import centrality
 
-        return centrality.centrality_simplest(
-            self, distances=distances, betas=betas, minutes=minutes, compute_closeness=compute_closeness,
+        return self._run(
+            centrality.centrality_simplest, distances=distances, betas=betas, minutes=minutes, compute_closeness=compute_closeness,
             compute_betweenness=compute_betweenness, min_threshold_wt=min_threshold_wt, speed_m_s=speed_m_s,
             tolerance=tolerance, angular_scaling_unit=angular_scaling_unit,
             farness_scaling_offset=farness_scaling_offset, sample_probability=sample_probability,
@@ -804,8 +825,8 @@ class NetworkStructure:
                            compute_betweenness=None, min_threshold_wt=None, speed_m_s=None, pbar_disabled=None):
         from . import centrality
 
-        return centrality.segment_centrality(
-            self, distances=distances, betas=betas, minutes=minutes, compute_closeness=compute_closeness,
+        return self._run(
+            centrality.segment_centrality, distances=distances, betas=betas, minutes=minutes, compute_closeness=compute_closeness,
             compute_betweenness=compute_betweenness, min_threshold_wt=min_threshold_wt, speed_m_s=speed_m_s,
             pbar_disabled=pbar_disabled)
 

@@ -361,6 +361,12 @@ cs_status cs_last_retries(int64_t *overflowed, int64_t *inexact);
  * cs_dual_batch_job (first n). */
 cs_status cs_abi_sizes(int32_t *out, int32_t n);
 
+/* Live progress of the call running on a workspace (NetworkStructure.progress, rust/src/graph.rs:
+ * 387-415): the sources its kernels have completed so far (a call resets the count when it starts;
+ * sources redone after an overflow count twice).  Reads the workspace header on a stream of its own,
+ * so it can be called from another host thread while the call's kernels run. */
+cs_status cs_workspace_progress(const void *workspace_dev, int64_t *sources_done);
+
 /* Number of SMs of the current device (0 on failure). */
 int32_t cs_device_sm_count(void);
 

@@ -53,3 +53,28 @@ def test_sampled_schedule_runs():
     nodes, _, ns = io.network_structure_from_nx(mock_graph())
     frame = networks.node_centrality_shortest(ns, {}, distances=[500, 20000], sample=True, random_seed=1)
     assert "cc_density_20000" in frame and np.all(np.isfinite(frame["cc_density_500"]))
+
+
+@pytest.mark.gpu
+def test_progress_is_live_during_a_call():
+    """progress() reads the completed-source count from the device while the call runs (the
+    reference's progress counter, rust/src/graph.rs:387-415), and equals the source count after."""
+    import threading
+    import time
+
+    from cityseer_gb300 import synth
+
+    p, dists = synth.lattice_config("c2")
+    ns = synth.primal_structure(p)
+    ns.centrality_shortest(distances=dists, source_indices=[0])  # device state in place
+    seen = []
+    th = threading.Thread(target=lambda: ns.centrality_shortest(distances=dists))
+    th.start()
+    while th.is_alive():
+        seen.append(ns.progress())
+        time.sleep(0.002)
+    th.join()
+    n = ns.node_count()
+    assert ns.progress() == n
+    assert all(0 <= x <= n for x in seen)
+    assert any(0 < x < n for x in seen), seen[:20]
