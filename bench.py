@@ -213,7 +213,7 @@ def run_reference(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32+f64",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "nodes": n, "distances": dists},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": times[-1]["cores"], "kind": times[-1]["kind"],
@@ -356,7 +356,7 @@ def run_gpu(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32+f64",
         "data": "synthetic (seeded jittered lattice, see cityseer_gb300/synth.py)",
         "config": {
             "workload": WORKLOAD,
@@ -561,7 +561,7 @@ def run_batch(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32+f64",
         "data": "synthetic (seeded jittered lattices, cityseer_gb300/synth.py batch_workload)",
         "config": {
             "workload": f"batch{len(graphs)}_mixed_2k_150k",
@@ -760,7 +760,7 @@ def run_serve(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32+f64",
         "data": "synthetic (seeded jittered lattices and their duals, Poisson request streams)",
         "config": {"workload": "serve6_50k_1200k", "graph_nodes": [ns.node_count() for ns in prims.values()],
                    "dual_nodes": [ns.node_count() for ns in duals.values()], "seconds_per_rate": args.serve_seconds,
@@ -824,7 +824,7 @@ def run_c3(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32+f64",
         "data": "synthetic (seeded curved jittered lattice and its dual, see cityseer_gb300/synth.py)",
         "config": {"workload": "c3_curved250", "dual_nodes": nsd.node_count(), "primal_nodes": ns.node_count(),
                    "distances": dists, "timing": "wall clock per public-API call, device synchronised"},
