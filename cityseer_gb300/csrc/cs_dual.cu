@@ -57,6 +57,7 @@ struct DSlot {
     int32_t *pr;  // [cap * DPM]
     double *dl;   // [cap * K] dependencies (f64, as the reference's delta)
     int32_t *hp;  // exact-mode heap: [2 cap] (route bits, state) pairs interleaved
+    uint32_t *lsec;  // widened pass: [2N] least arrival seconds (f32 bits; all ones = none), else null
 };
 
 __host__ __device__ inline size_t compact_bytes_d(size_t cap, int K) {
@@ -97,6 +98,7 @@ __host__ __device__ inline DSlot dslot(char *dense, size_t dense_stride, char *c
     s.pr = (int32_t *)(c + o); o += al256(cap * 4 * DPM);
     s.dl = (double *)(c + o); o += al256(cap * 8 * (size_t)K);
     s.hp = (int32_t *)(c + o); o += al256(cap * 16);
+    s.lsec = nullptr;
     return s;
 }
 
@@ -128,7 +130,9 @@ struct DualParams {
     char *compact;
     int32_t cap;
     int32_t n_slots;
-    int32_t pass;  // 0 = label-correcting pass, 1 = full-capacity retry, 2 = exact heap pass
+    int32_t pass;  // 0 = label-correcting pass, 1 = larger-capacity retry, 2 = exact heap pass,
+                   // 3 = widened label-correcting pass (sources whose replay disagreed)
+    int32_t lsec_slot_off;  // pass 3: slot i keeps its lsec array in slot i + this one's dense key array
     int32_t geo_n; // node bound the workspace's slot geometry was planned for (>= g.n_bound)
     const int32_t *remap;
     int32_t mode;
@@ -256,6 +260,157 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
             const bool live = act && k == ent.y;
             const bool tonear = live && hi_f(k) < T;
             const bool keep = live && !tonear;
+            const unsigned mt = __ballot_sync(FULL, tonear);
+            const unsigned mk = __ballot_sync(FULL, keep);
+            __syncwarp();
+            if (tonear) cur[nn + __popc(mt & lt)] = ent;
+            if (keep) s.qf[nf2 + __popc(mk & lt)] = ent;
+            nn += __popc(mt);
+            nf2 += __popc(mk);
+            __syncwarp();
+        }
+        nnear = nn;
+        nfar = nf2;
+    }
+    __syncwarp();
+    if (overflow) return -1;
+    return R;
+}
+
+// ------------------------------------------------------------------------------------------
+// A (widened, pass 3).  The search of A plus, per state, the least arrival seconds over every path
+// inside the cutoff (s.lsec, f32 bits, route-independent), and every state with such a path joins
+// the reached set.  The reference's seconds for a state are the seconds of one of its paths, so this
+// set contains every state the reference reaches, including those reached only through seconds
+// that its tie window lowered below the search key's.  States reached only through lsec keep
+// KEY_INF (they sort last); the replay gives each its route (+inf when the reference does not reach
+// it) and the replay rounds settle the order.
+// Queue entries: x = state | lsec part << 32 (NO_LSEC: none), y = key part (NO_KEY: none).  An entry
+// is live while either part equals the state's current value; a live entry relaxes both the key and
+// the lsec offers from the state's current values.  Entries with only an lsec part skip the bands.
+// ------------------------------------------------------------------------------------------
+constexpr uint32_t NO_LSEC = 0xffffffffu;
+constexpr unsigned long long NO_KEY = KEY_INF - 1ull;  // a NaN route: never a key
+
+__device__ int dual_search_wide(const DualParams &p, const DSlot &s, int src, long long &relaxed) {
+    const int lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    const int cap = p.cap, qcap = 2 * cap;
+    if (lane == 0) {
+        s.key[2 * src] = 0ull;
+        s.key[2 * src + 1] = 0ull;
+        s.lsec[2 * src] = 0u;
+        s.lsec[2 * src + 1] = 0u;
+        s.rl[0] = 2 * src;
+        s.rl[1] = 2 * src + 1;
+        s.qa[0] = make_ulonglong2((unsigned long long)(2 * src), 0ull);
+        s.qa[1] = make_ulonglong2((unsigned long long)(2 * src + 1), 0ull);
+    }
+    __syncwarp();
+    int R = 2, nnear = 2, nfar = 0;
+    ulonglong2 *cur = s.qa, *nxt = s.qb;
+    float T = p.delta;
+    bool overflow = false;
+    while (true) {
+        while (nnear > 0) {
+            int nnext = 0;
+            for (int base = 0; base < nnear; base += 32) {
+                const int i = base + lane;
+                const bool act = i < nnear;
+                const ulonglong2 ent = act ? cur[i] : make_ulonglong2(0ull, NO_KEY);
+                const int S = (int)(uint32_t)ent.x;
+                const uint32_t nl = (uint32_t)(ent.x >> 32);
+                const unsigned long long kS = act ? __ldcg(&s.key[S]) : KEY_INF;
+                const uint32_t lS = act ? __ldcg(&s.lsec[S]) : NO_LSEC;
+                const bool live = act && ((ent.y != NO_KEY && kS == ent.y) || (nl != NO_LSEC && lS == nl));
+                const int u = S >> 1, e = S & 1;
+                const int beg = live ? __ldg(&p.g.ptr_dev[u]) : 0;
+                const int deg = live ? __ldg(&p.g.ptr_dev[u + 1]) - beg : 0;
+                relaxed += deg;
+                const bool has_key = kS != KEY_INF;
+                const float rU = hi_f(kS), sU = lo_f(kS), lU = __uint_as_float(lS);
+                const int maxdeg = warp_max_i(deg);
+                for (int j = 0; j < maxdeg; j++) {
+                    int V = 0;
+                    unsigned long long nk = KEY_INF;
+                    uint32_t lb = NO_LSEC;
+                    bool impk = false, impl = false, first = false;
+                    float cr = 0.0f;
+                    if (j < deg) {
+                        const int ej = beg + j;
+                        if (__ldg(&p.g.exit_slot_dev[ej]) == 1 - e) {
+                            const float w = __ldg(&p.g.w_dev[ej]);
+                            const float cs_ = has_key ? __fadd_rn(sU, w) : __int_as_float(INF_BITS);
+                            // a key's path is a path too: lsec stays <= the key's seconds
+                            const float ls_ = fminf(__fadd_rn(lU, w), cs_);
+                            if (ls_ <= p.maxsec) {
+                                V = 2 * __ldg(&p.g.to_dev[ej]) + __ldg(&p.g.entry_slot_dev[ej]);
+                                lb = __float_as_uint(ls_);
+                                const uint32_t ol = atomicMin(&s.lsec[V], lb);
+                                impl = lb < ol;
+                                first = impl && ol == NO_LSEC;
+                                if (cs_ <= p.maxsec) {
+                                    cr = cand_route(rU, __ldg(&p.g.ang_dev[ej]), __ldg(&p.g.len_dev[ej]));
+                                    nk = pack(cr, cs_);
+                                    const unsigned long long o = atomicMin(&s.key[V], nk);
+                                    impk = nk < o;
+                                }
+                            }
+                        }
+                    }
+                    const int route = impk ? (cr < T ? 1 : 2) : (impl ? 1 : 0);
+                    const ulonglong2 ne = make_ulonglong2(
+                        (unsigned long long)(uint32_t)V | ((unsigned long long)(impl ? lb : NO_LSEC) << 32),
+                        impk ? nk : NO_KEY);
+                    const unsigned mf = __ballot_sync(FULL, first);
+                    const unsigned mn = __ballot_sync(FULL, route == 1);
+                    const unsigned mr = __ballot_sync(FULL, route == 2);
+                    if (first) {
+                        const int q = R + __popc(mf & lt);
+                        if (q < cap) s.rl[q] = V;
+                    }
+                    if (route == 1) {
+                        const int q = nnext + __popc(mn & lt);
+                        if (q < qcap) nxt[q] = ne;
+                    }
+                    if (route == 2) {
+                        const int q = nfar + __popc(mr & lt);
+                        if (q < qcap) s.qf[q] = ne;
+                    }
+                    R += __popc(mf);
+                    nnext += __popc(mn);
+                    nfar += __popc(mr);
+                }
+            }
+            __syncwarp();
+            if (R > cap || nnext > qcap || nfar > qcap) { overflow = true; break; }
+            ulonglong2 *t = cur; cur = nxt; nxt = t;
+            nnear = nnext;
+        }
+        if (overflow) break;
+        if (nfar == 0) break;
+        float mn = __int_as_float(INF_BITS);
+        for (int i = lane; i < nfar; i += 32) {
+            const ulonglong2 ent = s.qf[i];
+            const unsigned long long k = __ldcg(&s.key[(int)(uint32_t)ent.x]);
+            if (k == ent.y) mn = fminf(mn, hi_f(k));
+        }
+        mn = warp_min_f(mn);
+        const float Told = T;
+        T = (mn == __int_as_float(INF_BITS)) ? Told
+                                             : fmaxf(__fadd_rn(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        int nn = 0, nf2 = 0;
+        for (int base = 0; base < nfar; base += 32) {
+            const int i = base + lane;
+            const bool act = i < nfar;
+            const ulonglong2 ent = act ? s.qf[i] : make_ulonglong2(0ull, NO_KEY);
+            const int S = (int)(uint32_t)ent.x;
+            const uint32_t nl = (uint32_t)(ent.x >> 32);
+            const unsigned long long k = act ? __ldcg(&s.key[S]) : KEY_INF;
+            const bool klive = act && ent.y != NO_KEY && k == ent.y;
+            const bool llive = act && nl != NO_LSEC && __ldcg(&s.lsec[S]) == nl;
+            const bool tonear = (klive && hi_f(k) < T) || (!klive && llive);
+            const bool keep = klive && !tonear;
             const unsigned mt = __ballot_sync(FULL, tonear);
             const unsigned mk = __ballot_sync(FULL, keep);
             __syncwarp();
@@ -610,7 +765,10 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
                 s.sig[i] = sg;
                 s.np[i] = (uint8_t)np;
                 const unsigned long long k = __ldcg(&s.key[V]);
-                if (__float_as_uint(route) != (unsigned)(k >> 32)) {
+                // a widened-pass state without a key that the replay leaves unreached agrees
+                const bool both_unreached = k == KEY_INF && route == __int_as_float(INF_BITS);
+                if (both_unreached) {
+                } else if (__float_as_uint(route) != (unsigned)(k >> 32)) {
                     mismatch = true;
                     if (rewrite) s.key[V] = pack(route, secs);
                 } else if (__float_as_uint(secs) != (unsigned)(k & 0xffffffffull)) {
@@ -802,9 +960,12 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
     const int lane = lane_id();
     const int N2 = 2 * p.g.n_bound;
     const bool exact = (p.pass == 2) || p.force_exact;
+    const bool wide = s.lsec != nullptr;
     int R;
     if (exact) {
         R = dual_exact_search(p, s, src);
+    } else if (wide) {
+        R = dual_search_wide(p, s, src, relaxed);
     } else {
         R = dual_search(p, s, src, relaxed);
     }
@@ -812,6 +973,7 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
         for (int j = lane; j < N2; j += 32) {
             s.key[j] = KEY_INF;
             s.aux[j] = 0u;
+            if (wide) s.lsec[j] = NO_LSEC;
         }
         if (lane == 0) {
             if (p.fail_final) {
@@ -831,7 +993,8 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
     // until the order is consistent (the reference's), else fall back to the exact search.
     bool bad = false;
     int rr = 1;
-    const int rounds = exact ? 1 : max(1, p.replay_rounds);
+    // the widened set's keyless states that the reference reaches take one more round to sort
+    const int rounds = exact ? 1 : max(1, p.replay_rounds) + (wide ? 4 : 0);
     for (int it = 0; it < rounds && rr == 1; it++) {
         if (!exact) warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb,
                                     s.vb, s.rk, s.ord, hist);
@@ -859,6 +1022,7 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
         const int S = s.ord[i];
         s.key[S] = KEY_INF;
         s.aux[S] = 0u;
+        if (wide) s.lsec[S] = NO_LSEC;
     }
     __syncwarp();
     settled += R;
@@ -882,7 +1046,8 @@ __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
     if (slot >= p.n_slots) return;
-    const DSlot s = dslot(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.k, slot, p.geo_n);
+    DSlot s = dslot(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.k, slot, p.geo_n);
+    if (p.pass == 3) s.lsec = (uint32_t *)(p.dense + p.dense_stride * (size_t)(slot + p.lsec_slot_off));
     long long relaxed = 0, settled = 0, done_src = 0;
     while (true) {
         unsigned long long idx = 0;
@@ -946,7 +1111,9 @@ __global__ void __launch_bounds__(256, 2) dual_batch_kernel(const DualParams bas
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
     if (slot >= base.n_slots) return;
-    const DSlot s = dslot(base.dense, base.dense_stride, base.compact, (size_t)base.cap, base.k, slot, base.geo_n);
+    DSlot s = dslot(base.dense, base.dense_stride, base.compact, (size_t)base.cap, base.k, slot, base.geo_n);
+    if (base.pass == 3)
+        s.lsec = (uint32_t *)(base.dense + base.dense_stride * (size_t)(slot + base.lsec_slot_off));
     long long relaxed = 0, settled = 0, done_src = 0;
     DualParams p;
     int cur_job = -1;
@@ -1224,7 +1391,7 @@ int dsm_count() {
 }
 
 struct DLayout {
-    size_t failed_off, failed2_off, inexact_off, bucket_off, dense_off, compact_off, compact_total, total,
+    size_t failed_off, failed2_off, inexact_off, inexact2_off, bucket_off, dense_off, compact_off, compact_total, total,
         dense_stride;
     int fail_cap;
 };
@@ -1235,7 +1402,8 @@ DLayout dlayout(int n_bound, int n_slots, int cap, int K) {
     l.failed_off = 256;
     l.failed2_off = csd::al256(l.failed_off + 4 * (size_t)l.fail_cap);
     l.inexact_off = csd::al256(l.failed2_off + 4 * (size_t)l.fail_cap);
-    l.bucket_off = csd::al256(l.inexact_off + 4 * (size_t)l.fail_cap);
+    l.inexact2_off = csd::al256(l.inexact_off + 4 * (size_t)l.fail_cap);
+    l.bucket_off = csd::al256(l.inexact2_off + 4 * (size_t)l.fail_cap);
     l.dense_off = csd::al256(l.bucket_off + sizeof(double) * 3 * (size_t)K * (size_t)n_bound);
     l.dense_stride = csd::al256((size_t)n_bound * 16) + csd::al256((size_t)n_bound * 8);
     l.compact_off = l.dense_off + l.dense_stride * (size_t)n_slots;
@@ -1292,6 +1460,16 @@ int replay_rounds() {
     return (r >= 1 && r <= 64) ? r : 4;
 }
 
+// Sources whose replay disagreed first run the widened search (pass 3) and only those that still
+// disagree run the exact heap search.  CS_DUAL_WIDE=0 sends them straight to the exact search;
+// CS_DUAL_WIDE=1 runs every source through the widened search (a check of that pass).
+int dual_wide_mode() {
+    const char *e = getenv("CS_DUAL_WIDE");
+    if (e && e[0] == '0') return 0;
+    if (e && e[0] == '1') return 2;
+    return 1;
+}
+
 cs_status dlaunch(csd::DualParams &p, int n_slots, cudaStream_t s) {
     p.n_slots = n_slots;
     csd::dual_kernel<<<(n_slots + 7) / 8, 256, 0, s>>>(p);
@@ -1305,6 +1483,94 @@ cs_status dsync_header(cs::WsHeader *hd, cs::WsHeader &h, cudaStream_t s) {
     if (h.err != 0u)
         return dfail((cs_status)h.err, "device-side check failed (code " + std::to_string(h.err) + " at " +
                                            std::to_string(h.err_where) + ")");
+    return CS_OK;
+}
+
+// The passes of one call after its parameters are set.  The first pass runs every source on every
+// slot.  Sources that overflowed their slot run again at 4x the capacity (then 4x again, up to every
+// state), each level on as many slots as the workspace's compact region holds at that capacity.
+// Sources whose replay disagreed then run the widened search (pass 3, on half the slots: each keeps
+// its lsec array in the key array of a partner slot), and those that still disagree the exact heap
+// search, both starting at the plan's capacity.  wide_mode 2 runs every source through pass 3 in
+// place of the first pass.  launch(params, slots) starts one pass.  n_exact: sources the exact
+// search redid.
+template <class Launch>
+cs_status dual_passes(const csd::DualParams &p, const DLayout &lay, const cs_plan *plan, int K, int N2, long long n_all,
+                      int wide_mode, Launch launch, cudaStream_t s, long long &n_over, long long &n_exact) {
+    char *base = (char *)p.hdr;
+    int32_t *listA = p.failed;
+    int32_t *listB = (int32_t *)(base + lay.failed2_off);
+    int32_t *inexact2 = (int32_t *)(base + lay.inexact2_off);
+    const int half = plan->n_slots / 2;
+    if (half < 1) wide_mode = 0;
+    cs::WsHeader h;
+    memset(&h, 0, sizeof(h));
+    auto chain = [&](int pass, const int32_t *in, long long n_in, int cap0) -> cs_status {
+        int cap_l = std::min(N2, cap0);
+        const int32_t *list = in;
+        while (n_in > 0) {
+            const bool final = cap_l >= N2;
+            int32_t *out_l = (list == listA) ? listB : listA;
+            csd::DualParams p2 = p;
+            p2.pass = pass;
+            p2.cap = cap_l;
+            p2.remap = list;
+            p2.n_src = list ? std::min<long long>(n_in, lay.fail_cap) : n_in;
+            p2.failed = out_l;
+            p2.fail_final = final ? 1 : 0;
+            if (pass == 3) {
+                p2.inexact = inexact2;
+                p2.lsec_slot_off = half;
+            }
+            cudaError_t e2 = cudaMemsetAsync(&p.hdr->work_next2, 0, sizeof(unsigned long long), s);
+            if (e2 == cudaSuccess) e2 = cudaMemsetAsync(&p.hdr->n_failed, 0, sizeof(unsigned), s);
+            if (e2 != cudaSuccess) return dcuda(e2, "retry counter reset");
+            const size_t per = csd::compact_bytes_d((size_t)cap_l, K);
+            long long slots2 = std::min<long long>((long long)(lay.compact_total / per), plan->n_slots);
+            if (pass == 3) slots2 = std::min<long long>(slots2, half);
+            slots2 = std::max<long long>(1, std::min<long long>(slots2, p2.n_src));
+            cs_status st2 = launch(p2, (int)slots2);
+            if (st2 != CS_OK) return st2;
+            cs::WsHeader h2;
+            st2 = dsync_header(p.hdr, h2, s);
+            if (st2 != CS_OK) return st2;
+            h.n_inexact = h2.n_inexact;  // retries may list more disagreeing sources
+            n_in = final ? 0 : (long long)h2.n_failed;
+            list = out_l;
+            cap_l = (int)std::min<long long>(N2, 4ll * cap_l);
+        }
+        return CS_OK;
+    };
+    cs_status st;
+    n_over = 0;
+    if (wide_mode == 2) {
+        st = chain(3, nullptr, n_all, plan->cap);
+        if (st != CS_OK) return st;
+    } else {
+        csd::DualParams p0 = p;
+        st = launch(p0, plan->n_slots);
+        if (st != CS_OK) return st;
+        st = dsync_header(p.hdr, h, s);
+        if (st != CS_OK) return st;
+        n_over = h.n_failed;
+        if (h.n_failed > 0u) {
+            st = chain(1, listA, h.n_failed, 4 * std::max(plan->cap, 16));
+            if (st != CS_OK) return st;
+        }
+    }
+    const int32_t *ex = (wide_mode == 2) ? inexact2 : p.inexact;
+    long long n_ex = std::min<long long>(h.n_inexact, lay.fail_cap);
+    if (wide_mode == 1 && n_ex > 0) {
+        cudaError_t e = cudaMemsetAsync(&p.hdr->n_inexact, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return dcuda(e, "retry counter reset");
+        h.n_inexact = 0;
+        st = chain(3, p.inexact, n_ex, plan->cap);
+        if (st != CS_OK) return st;
+        ex = inexact2;
+        n_ex = std::min<long long>(h.n_inexact, lay.fail_cap);
+    }
+    n_exact = n_ex;
+    if (n_ex > 0) return chain(2, ex, n_ex, plan->cap);
     return CS_OK;
 }
 }  // namespace
@@ -1401,62 +1667,12 @@ cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, cons
     if (e == cudaSuccess && p.closeness)
         e = cudaMemsetAsync(p.bucket, 0, sizeof(double) * 3 * (size_t)K * (size_t)g->n_bound, s);
     if (e != cudaSuccess) return dcuda(e, "workspace reset");
-    st = dlaunch(p, plan->n_slots, s);
+    long long n_over = 0, n_exact = 0;
+    st = dual_passes(
+        p, lay, plan, K, 2 * g->n_bound, p.n_src, dual_wide_mode(),
+        [&](csd::DualParams &pp, int slots) { return dlaunch(pp, slots, s); }, s, n_over, n_exact);
     if (st != CS_OK) return st;
-    cs::WsHeader h;
-    st = dsync_header(p.hdr, h, s);
-    if (st != CS_OK) return st;
-    // Sources that overflowed their slot run again at 4x the capacity (then 4x again, up to every
-    // state), each level on as many slots as the workspace's compact region holds at that
-    // capacity.  Sources whose replay disagreed with the search then run the exact heap search,
-    // starting at the plan's capacity.
-    const int N2 = 2 * g->n_bound;
-    int32_t *listA = p.failed;
-    int32_t *listB = (int32_t *)(base + lay.failed2_off);
-    long long n_retried = 0;
-    auto chain = [&](int pass, const int32_t *in, unsigned n_in, int cap0) -> cs_status {
-        int cap_l = std::min(N2, cap0);
-        const int32_t *list = in;
-        while (n_in > 0u) {
-            const bool final = cap_l >= N2;
-            int32_t *out_l = (list == listA) ? listB : listA;
-            csd::DualParams p2 = p;
-            p2.pass = pass;
-            p2.cap = cap_l;
-            p2.remap = list;
-            p2.n_src = std::min<unsigned>(n_in, (unsigned)lay.fail_cap);
-            p2.failed = out_l;
-            p2.fail_final = final ? 1 : 0;
-            cudaError_t e2 = cudaMemsetAsync(&p.hdr->work_next2, 0, sizeof(unsigned long long), s);
-            if (e2 == cudaSuccess) e2 = cudaMemsetAsync(&p.hdr->n_failed, 0, sizeof(unsigned), s);
-            if (e2 != cudaSuccess) return dcuda(e2, "retry counter reset");
-            const size_t per = csd::compact_bytes_d((size_t)cap_l, K);
-            int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
-            slots2 = std::max(1, std::min<int>(slots2, (int)p2.n_src));
-            cs_status st2 = dlaunch(p2, slots2, s);
-            if (st2 != CS_OK) return st2;
-            cs::WsHeader h2;
-            st2 = dsync_header(p.hdr, h2, s);
-            if (st2 != CS_OK) return st2;
-            n_retried += (long long)p2.n_src;
-            h.n_inexact = h2.n_inexact;  // label-correcting retries may add inexact sources
-            n_in = final ? 0u : h2.n_failed;
-            list = out_l;
-            cap_l = (int)std::min<long long>(N2, 4ll * cap_l);
-        }
-        return CS_OK;
-    };
-    const long long n_over = h.n_failed;
-    if (h.n_failed > 0u) {
-        st = chain(1, listA, h.n_failed, 4 * std::max(plan->cap, 16));
-        if (st != CS_OK) return st;
-    }
-    const long long n_inexact = h.n_inexact;
-    if (h.n_inexact > 0u) {
-        st = chain(2, p.inexact, std::min<unsigned>(h.n_inexact, (unsigned)lay.fail_cap), plan->cap);
-        if (st != CS_OK) return st;
-    }
-    cs_set_retries_internal(n_over, n_inexact);
+    cs_set_retries_internal(n_over, n_exact);
     if (p.closeness) {
         int blocks = std::max(1, std::min((g->n_bound + 255) / 256, dsm_count() * 8));
         csd::dual_bucket_prefix<<<blocks, 256, 0, s>>>(p.bucket, p.out, K, g->n_bound);
@@ -1571,61 +1787,20 @@ cs_status cs_dual_batch_run(const cs_dual_batch_job *jobs_host, const cs_dual_ba
     p.cap = plan->cap;
     cudaError_t e = cudaMemsetAsync(p.hdr, 0, sizeof(cs::WsHeader), s);
     if (e != cudaSuccess) return dcuda(e, "batch reset");
-    if (n_items > 0) {
-        st = dbatch_launch(p, jobs_dev, n_jobs, n_items, plan->n_slots, s);
+    auto launch = [&](csd::DualParams &pp, int slots) {
+        return dbatch_launch(pp, jobs_dev, n_jobs, n_items, slots, s);
+    };
+    if (n_items > 0 && (flags & CS_BATCH_ASYNC)) {
+        // one pass; the caller re-runs listed items (cs_dual_batch_failed)
+        st = launch(p, plan->n_slots);
         if (st != CS_OK) return st;
-    }
-    if (!(flags & CS_BATCH_ASYNC) && n_items > 0) {
-        cs::WsHeader h;
-        st = dsync_header(p.hdr, h, s);
+    } else if (n_items > 0) {
+        // overflowed items at growing capacities, then items whose replay disagreed through the
+        // widened and the exact search (as cs_centrality_simplest)
+        long long n_over = 0, n_exact = 0;
+        st = dual_passes(p, lay, plan, L, 2 * b.max_n, n_items, dual_wide_mode(), launch, s, n_over, n_exact);
         if (st != CS_OK) return st;
-        // overflowed items at growing capacities, then items whose replay disagreed with the exact
-        // heap search (as cs_centrality_simplest)
-        const int N2 = 2 * b.max_n;
-        int32_t *listA = p.failed;
-        int32_t *listB = (int32_t *)(base + lay.failed2_off);
-        auto chain = [&](int pass, const int32_t *in, unsigned n_in, int cap0) -> cs_status {
-            int cap_l = std::min(N2, cap0);
-            const int32_t *list = in;
-            while (n_in > 0u) {
-                const bool final = cap_l >= N2;
-                int32_t *out_l = (list == listA) ? listB : listA;
-                csd::DualParams p2 = p;
-                p2.pass = pass;
-                p2.cap = cap_l;
-                p2.remap = list;
-                p2.n_src = std::min<unsigned>(n_in, (unsigned)lay.fail_cap);
-                p2.failed = out_l;
-                p2.fail_final = final ? 1 : 0;
-                cudaError_t e2 = cudaMemsetAsync(&p.hdr->work_next2, 0, sizeof(unsigned long long), s);
-                if (e2 == cudaSuccess) e2 = cudaMemsetAsync(&p.hdr->n_failed, 0, sizeof(unsigned), s);
-                if (e2 != cudaSuccess) return dcuda(e2, "retry counter reset");
-                const size_t per = csd::compact_bytes_d((size_t)cap_l, L);
-                int slots2 = (int)std::min<size_t>(lay.compact_total / per, (size_t)plan->n_slots);
-                slots2 = std::max(1, std::min<int>(slots2, (int)p2.n_src));
-                cs_status st2 = dbatch_launch(p2, jobs_dev, n_jobs, n_items, slots2, s);
-                if (st2 != CS_OK) return st2;
-                cs::WsHeader h2;
-                st2 = dsync_header(p.hdr, h2, s);
-                if (st2 != CS_OK) return st2;
-                h.n_inexact = h2.n_inexact;
-                n_in = final ? 0u : h2.n_failed;
-                list = out_l;
-                cap_l = (int)std::min<long long>(N2, 4ll * cap_l);
-            }
-            return CS_OK;
-        };
-        const long long n_over = h.n_failed;
-        if (h.n_failed > 0u) {
-            st = chain(1, listA, h.n_failed, 4 * std::max(plan->cap, 16));
-            if (st != CS_OK) return st;
-        }
-        const long long n_inexact = h.n_inexact;
-        if (h.n_inexact > 0u) {
-            st = chain(2, p.inexact, std::min<unsigned>(h.n_inexact, (unsigned)lay.fail_cap), plan->cap);
-            if (st != CS_OK) return st;
-        }
-        cs_set_retries_internal(n_over, n_inexact);
+        cs_set_retries_internal(n_over, n_exact);
     }
     int max_n = 0, n_pref = 0;
     for (int j = 0; j < n_jobs; j++)

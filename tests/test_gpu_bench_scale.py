@@ -143,12 +143,14 @@ def curved_dual():
 
 def _simplest(ns, dists, srcs, exact):
     d, b, s = common.pair_distances_betas_time(SPEED, distances=dists)
-    if exact:
-        os.environ["CS_DUAL_FORCE_EXACT"] = "1"
+    env = {True: "CS_DUAL_FORCE_EXACT", "wide": "CS_DUAL_WIDE"}.get(exact)
+    if env:
+        os.environ[env] = "1"  # every source through the exact heap search / the widened search
     try:
         res = ns.centrality_simplest(distances=dists, source_indices=srcs)
     finally:
-        os.environ.pop("CS_DUAL_FORCE_EXACT", None)
+        if env:
+            os.environ.pop(env)
     sp = prepare_source_sampling(ns, None, None, None, srcs)
     ref, reach = oracle.centrality_simplest(oracle.OracleGraph(ns), d, b, s, plan=oracle.plan_from(sp, ns.node_bound()),
                                             nthreads=oracle.default_threads())
@@ -167,7 +169,7 @@ def _simplest(ns, dists, srcs, exact):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("exact", [False, True])
+@pytest.mark.parametrize("exact", [False, True, "wide"])
 def test_curved250_dual_simplest(curved_dual, exact):
     ns, dists = curved_dual
     _simplest(ns, dists, _strided(ns, 256), exact)

@@ -19,12 +19,14 @@ def _dual(g):
 
 def _run(ns, dists, exact=False, **kw):
     d, b, s = common.pair_distances_betas_time(1.33333, distances=dists)
-    if exact:
-        os.environ["CS_DUAL_FORCE_EXACT"] = "1"
+    env = {True: "CS_DUAL_FORCE_EXACT", "wide": "CS_DUAL_WIDE"}.get(exact)
+    if env:
+        os.environ[env] = "1"  # every source through the exact heap search / the widened search
     try:
         res = ns.centrality_simplest(distances=dists, **kw)
     finally:
-        os.environ.pop("CS_DUAL_FORCE_EXACT", None)
+        if env:
+            os.environ.pop(env)
     sp = prepare_source_sampling(ns, kw.get("sample_probability"), kw.get("sampling_weights"), kw.get("random_seed"),
                                  kw.get("source_indices"))
     ref, reach = oracle.centrality_simplest(oracle.OracleGraph(ns), d, b, s, tol=validate_tolerance(kw.get("tolerance")),
@@ -48,7 +50,7 @@ def _run(ns, dists, exact=False, **kw):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("exact", [False, True])
+@pytest.mark.parametrize("exact", [False, True, "wide"])
 def test_simplest_small_graphs(exact):
     _run(_dual(diamond_graph())[2], [50, 150, 250], exact=exact)
     _run(_dual(mock_graph())[2], [200, 500, 2000, 5000], exact=exact)
@@ -56,7 +58,7 @@ def test_simplest_small_graphs(exact):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("exact", [False, True])
+@pytest.mark.parametrize("exact", [False, True, "wide"])
 def test_simplest_curved_lattice_dual(exact):
     p, dists = synth.lattice_config("c3", side=16)
     _run(synth.dual_structure(p), dists, exact=exact)
