@@ -33,6 +33,8 @@
 
 extern "C" void cs_set_error_internal(const char *msg);
 extern "C" void cs_set_retries_internal(long long overflowed, long long inexact);
+extern "C" void cs_set_phase_internal(const unsigned long long *pad);
+extern "C" void cs_set_counters_internal(long long sources, long long relaxed, long long settled, long long launches);
 
 namespace csd {
 using namespace cs;
@@ -152,6 +154,15 @@ __device__ __forceinline__ unsigned long long pack(float r, float s) {
 // route candidate exactly as rust/src/centrality.rs:665-667 evaluates it
 __device__ __forceinline__ float cand_route(float r, float ang, float len) {
     return __fadd_rn(__fadd_rn(r, ang), __fmul_rn(ANGULAR_TIE_BREAK, len));
+}
+
+// Per-phase cycle counters (the warp's shared-memory row; lane 0 adds): 0 search, 1 sort, 2 replay,
+// 3 node best + closeness, 4 backward sweep, 5 scratch reset, 6 exact heap search; 7 counts replay
+// rounds.
+__device__ __forceinline__ void dphase(long long *ph, int idx, long long &t) {
+    const long long now = clock64();
+    if (lane_id() == 0) ph[idx] += now - t;
+    t = now;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -649,6 +660,43 @@ __device__ __forceinline__ unsigned dreplay(const DualParams &p, const DOff &o, 
     return pm;
 }
 
+// The replay keeps each state's offers (position, or -1; route; seconds) for the node-level best,
+// in the search queues' space (free once the search is done): 8 positions in qa, 8 routes in qb,
+// 8 seconds in qf per settle position.
+__device__ __forceinline__ void store_doffers(const DSlot &s, int i, const DOff &o) {
+    int4 *op = (int4 *)s.qa + 2 * (size_t)i;
+    float4 *cp = (float4 *)s.qb + 2 * (size_t)i;
+    float4 *sp = (float4 *)s.qf + 2 * (size_t)i;
+    int q[DPM];
+#pragma unroll
+    for (int j = 0; j < DPM; j++) q[j] = ((o.valid >> j) & 1u) ? o.pos[j] : -1;
+    op[0] = make_int4(q[0], q[1], q[2], q[3]);
+    op[1] = make_int4(q[4], q[5], q[6], q[7]);
+    cp[0] = make_float4(o.cr[0], o.cr[1], o.cr[2], o.cr[3]);
+    cp[1] = make_float4(o.cr[4], o.cr[5], o.cr[6], o.cr[7]);
+    sp[0] = make_float4(o.cs[0], o.cs[1], o.cs[2], o.cs[3]);
+    sp[1] = make_float4(o.cs[4], o.cs[5], o.cs[6], o.cs[7]);
+}
+
+__device__ __forceinline__ void load_doffers(const DSlot &s, int i, DOff &o) {
+    const int4 *op = (const int4 *)s.qa + 2 * (size_t)i;
+    const float4 *cp = (const float4 *)s.qb + 2 * (size_t)i;
+    const float4 *sp = (const float4 *)s.qf + 2 * (size_t)i;
+    const int4 a = __ldcg(op), b = __ldcg(op + 1);
+    const float4 c = __ldcg(cp), d = __ldcg(cp + 1), e = __ldcg(sp), f = __ldcg(sp + 1);
+    const int q[DPM] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    const float cr[DPM] = {c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
+    const float cs[DPM] = {e.x, e.y, e.z, e.w, f.x, f.y, f.z, f.w};
+    o.valid = 0u;
+#pragma unroll
+    for (int j = 0; j < DPM; j++) {
+        o.pos[j] = q[j];
+        o.cr[j] = cr[j];
+        o.cs[j] = cs[j];
+        if (q[j] >= 0) o.valid |= 1u << j;
+    }
+}
+
 // Node-level best route / seconds (rust/src/centrality.rs:695-703) over offers to both states of
 // the node, in the global settle order of the offering states.  Positions of the states: i0/i1
 // (-1 when unreached).
@@ -657,8 +705,8 @@ __device__ __forceinline__ void node_best(const DualParams &p, const DSlot &s, i
     DOff o0, o1;
     o0.valid = 0u;
     o1.valid = 0u;
-    if (i0 >= 0) gather_doffers(p, s, 2 * v, i0, R, o0, bad);
-    if (i1 >= 0) gather_doffers(p, s, 2 * v + 1, i1, R, o1, bad);
+    if (i0 >= 0) load_doffers(s, i0, o0);
+    if (i1 >= 0) load_doffers(s, i1, o1);
     const float one_plus = 1.0f + TIE_EPSILON, one_minus = 1.0f - TIE_EPSILON;
     best = (v == src) ? 0.0f : __int_as_float(INF_BITS);
     bsecs = best;
@@ -697,9 +745,10 @@ __device__ __forceinline__ int first_ks(const DualParams &p, float secs) {
 
 // Replay + sigma in route order.  Returns false (and sets mismatch) when the replay disagrees with
 // the search's keys.
-// Returns 0 when the replay is exact, 1 when some replayed route differs from the search's key (the
-// keys are then rewritten with the replayed values, so that sorting them again gives the next
-// settle-order estimate), 2 when the replayed seconds would reach a state the search did not.
+// Returns 0 when the replay is exact, 1 when some replayed route differs from the search's key and
+// the replayed routes are out of order (the keys are then rewritten with the replayed values, so
+// that sorting them again gives the next settle-order estimate), 2 when the replayed seconds would
+// reach a state the search did not.
 // check_reach: run the reach check even when every replayed value equals its key (the keys were
 // rewritten by an earlier round, and the search never relaxed from the rewritten seconds).
 __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, bool &bad, bool rewrite,
@@ -717,21 +766,50 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
         const bool act = i < R;
         const int V = act ? s.ord[i] : 0;
         const bool is_src = act && (V >> 1) == src;
-        // in-chunk offerer positions (their rB/sB/sig must be final first)
+        // The state's offers from reached states settled before it: positions and dual edges, found
+        // once; the offer values need the offerers' replayed route and seconds, final once the
+        // in-chunk offerers (pm) are done.
         DOff o;
         o.valid = 0u;
         unsigned pm = 0u;
+        int oid[DPM];
         if (act && !is_src) {
-            // positions only: recomputed after readiness with final values
             const int v = V >> 1, sv = V & 1;
             const int beg = __ldg(&p.g.rptr_dev[v]);
             const int deg = min(__ldg(&p.g.rptr_dev[v + 1]) - beg, DPM);
-            for (int j = 0; j < deg; j++) {
-                const int id = __ldg(&p.g.rid_dev[beg + j]);
-                if (__ldg(&p.g.entry_slot_dev[id]) != sv) continue;
-                const int U = 2 * __ldg(&p.g.rfrom_dev[beg + j]) + (1 - __ldg(&p.g.exit_slot_dev[id]));
-                const uint32_t a = s.aux[U];
-                if (a != 0u && a <= (uint32_t)R && (int)a - 1 < i && (int)a - 1 >= base) pm |= 1u << ((int)a - 1 - base);
+            int us[DPM];
+#pragma unroll
+            for (int j = 0; j < DPM; j++) {
+                oid[j] = (j < deg) ? __ldg(&p.g.rid_dev[beg + j]) : 0;
+                us[j] = (j < deg) ? __ldg(&p.g.rfrom_dev[beg + j]) : 0;
+            }
+            uint32_t aa[DPM];
+#pragma unroll
+            for (int j = 0; j < DPM; j++) {
+                aa[j] = 0u;
+                if (j < deg && __ldg(&p.g.entry_slot_dev[oid[j]]) == sv) {
+                    const int U = 2 * us[j] + (1 - __ldg(&p.g.exit_slot_dev[oid[j]]));
+                    aa[j] = s.aux[U];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < DPM; j++) {
+                o.pos[j] = -1;
+                if (aa[j] > (uint32_t)R) bad = true;
+                if (aa[j] != 0u && aa[j] <= (uint32_t)R && (int)aa[j] - 1 < i) {
+                    const int pu = (int)aa[j] - 1;
+                    o.pos[j] = pu;
+                    o.valid |= 1u << j;
+                    if (pu >= base) pm |= 1u << (pu - base);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < DPM; j++) {
+                o.pos[j] = -1;
+                o.cr[j] = 0.0f;
+                o.cs[j] = 0.0f;
+                oid[j] = 0;
             }
         }
         bool mine = !act;
@@ -748,8 +826,18 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
                     secs = 0.0f;
                     sg = 1.0;
                 } else {
-                    gather_doffers(p, s, V, i, R, o, bad);
-                    const unsigned pmask = dreplay(p, o, route, secs);
+#pragma unroll
+                    for (int j = 0; j < DPM; j++) {
+                        o.cr[j] = 0.0f;
+                        o.cs[j] = 0.0f;
+                        if ((o.valid >> j) & 1u) {
+                            const int pu = o.pos[j];
+                            o.cr[j] = cand_route(__ldcg(&s.rB[pu]), __ldg(&p.g.ang_dev[oid[j]]),
+                                                 __ldg(&p.g.len_dev[oid[j]]));
+                            o.cs[j] = __fadd_rn(__ldcg(&s.sB[pu]), __ldg(&p.g.w_dev[oid[j]]));
+                        }
+                    }
+                const unsigned pmask = dreplay(p, o, route, secs);
                     sg = 0.0;
 #pragma unroll
                     for (int j = 0; j < DPM; j++) {
@@ -764,12 +852,16 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
                 s.sB[i] = secs;
                 s.sig[i] = sg;
                 s.np[i] = (uint8_t)np;
+                store_doffers(s, i, o);
                 const unsigned long long k = __ldcg(&s.key[V]);
                 // a widened-pass state without a key that the replay leaves unreached agrees
                 const bool both_unreached = k == KEY_INF && route == __int_as_float(INF_BITS);
                 if (both_unreached) {
                 } else if (__float_as_uint(route) != (unsigned)(k >> 32)) {
                     mismatch = true;
+                    // diagnostics: replayed route below / above the key, or unreached
+                    const int slot9 = route == __int_as_float(INF_BITS) ? 11 : (route < hi_f(k) ? 9 : 10);
+                    atomicAdd(&p.hdr->pad[slot9], 1ull);
                     if (rewrite) s.key[V] = pack(route, secs);
                 } else if (__float_as_uint(secs) != (unsigned)(k & 0xffffffffull)) {
                     secs_diff = true;
@@ -785,11 +877,41 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
             return 2;
         }
     }
-    if (__any_sync(FULL, mismatch)) return 1;
-    if (!check_reach && !__any_sync(FULL, secs_diff)) return 0;
+    const bool any_mismatch = __any_sync(FULL, mismatch);
     __syncwarp();
-    // reach check with the replayed seconds: every in-cutoff offer must land on a reached state
-    bool escape = false;
+    if (any_mismatch) {
+        // The keys only order the states: the replay ran in the reference's settle order, and is
+        // therefore its result, whenever the finite replayed routes are non-decreasing in that order
+        // (states the replay leaves unreached offer nothing and are inert wherever they sit).
+        // Otherwise the rewritten keys give the next order.
+        bool disorder = false;
+        float run = -1.0f;  // largest finite route of the earlier chunks (routes are >= 0)
+        for (int base = 0; base < R; base += 32) {
+            const int i = base + lane;
+            const float r = i < R ? __ldcg(&s.rB[i]) : -1.0f;
+            const float rf = (r == __int_as_float(INF_BITS)) ? -1.0f : r;
+            float m = rf;  // inclusive running max over the chunk
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float t = __shfl_up_sync(FULL, m, o);
+                if (lane >= o) m = fmaxf(m, t);
+            }
+            float before = __shfl_up_sync(FULL, m, 1);
+            before = fmaxf(lane == 0 ? -1.0f : before, run);
+            if (rf >= 0.0f && rf < before) disorder = true;
+            run = fmaxf(run, __shfl_sync(FULL, m, 31));
+        }
+        if (__any_sync(FULL, disorder)) {
+            if (lane == 0) atomicAdd(&p.hdr->pad[12], 1ull);
+            return 1;
+        }
+    }
+    if (!check_reach && !any_mismatch && !__any_sync(FULL, secs_diff)) return 0;
+    __syncwarp();
+    // reach check with the replayed seconds: every in-cutoff offer must land on a reached state.
+    // After mismatches, a state the replay left unreached may only have been positioned before its
+    // offerers: an in-cutoff offer to it means the order was wrong (another round).
+    bool escape = false, stale = false;
     for (int i = lane; i < R; i += 32) {
         const int U = s.ord[i];
         const int u = U >> 1, e = U & 1;
@@ -799,16 +921,27 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
             if (__ldg(&p.g.exit_slot_dev[ej]) != 1 - e) continue;
             if (__fadd_rn(sU, __ldg(&p.g.w_dev[ej])) > p.maxsec) continue;
             const int V = 2 * __ldg(&p.g.to_dev[ej]) + __ldg(&p.g.entry_slot_dev[ej]);
-            if (s.aux[V] == 0u) escape = true;
+            const uint32_t a = s.aux[V];
+            if (a == 0u) escape = true;
+            else if (any_mismatch && __ldcg(&s.rB[a - 1]) == __int_as_float(INF_BITS)) stale = true;
         }
     }
-    return __any_sync(FULL, escape) ? 2 : 0;
+    if (__any_sync(FULL, stale)) {
+        if (lane == 0) atomicAdd(&p.hdr->pad[13], 1ull);
+        return 1;
+    }
+    if (__any_sync(FULL, escape)) {
+        if (lane == 0) atomicAdd(&p.hdr->pad[14], 1ull);
+        return 2;
+    }
+    return 0;
 }
 
 // ------------------------------------------------------------------------------------------
 // D + E. Node best, closeness, backward sweep.
 // ------------------------------------------------------------------------------------------
-__device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, int R, int *cnt, bool &bad) {
+__device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, int R, int *cnt, bool &bad, long long *ph) {
+    long long tph = clock64();
     const int lane = lane_id();
     const int K = p.k;
     const int N = p.g.n_bound;
@@ -855,6 +988,7 @@ __device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, in
             if (run > 0) atomicAdd(&p.reach[k], (unsigned)run);
         }
     }
+    dphase(ph, 3, tph);
     if (!p.betweenness) return;
     // backward sweep over states, K lanes (rust/src/centrality.rs:2036-2096)
     double *dl = s.dl;
@@ -947,6 +1081,7 @@ __device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, in
             return;
         }
     }
+    dphase(ph, 4, tph);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -956,8 +1091,9 @@ __device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, in
 // Returns true when the source was accumulated; false when it was listed (overflow or a replay
 // that disagreed) for a later pass.  li is what the lists record.
 __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot &s, int li, int src, uint32_t *hist,
-                                                int *cnt, long long &relaxed, long long &settled) {
+                                                int *cnt, long long *ph, long long &relaxed, long long &settled) {
     const int lane = lane_id();
+    long long tph = clock64();
     const int N2 = 2 * p.g.n_bound;
     const bool exact = (p.pass == 2) || p.force_exact;
     const bool wide = s.lsec != nullptr;
@@ -969,6 +1105,7 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
     } else {
         R = dual_search(p, s, src, relaxed);
     }
+    dphase(ph, exact ? 6 : 0, tph);
     if (R < 0) {
         for (int j = lane; j < N2; j += 32) {
             s.key[j] = KEY_INF;
@@ -995,19 +1132,25 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
     int rr = 1;
     // the widened set's keyless states that the reference reaches take one more round to sort
     const int rounds = exact ? 1 : max(1, p.replay_rounds) + (wide ? 4 : 0);
+    int rounds_run = 0;
     for (int it = 0; it < rounds && rr == 1; it++) {
+        rounds_run++;
         if (!exact) warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb,
                                     s.vb, s.rk, s.ord, hist);
         __syncwarp();
         for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
         __syncwarp();
+        dphase(ph, 1, tph);
         // after a round that rewrote keys, lower rewritten seconds may reach states the search cut
         rr = dual_replay(p, s, src, R, bad, !exact, it > 0);
         __syncwarp();
+        dphase(ph, 2, tph);
     }
+    if (lane == 0) ph[7] += rounds_run;
     const bool ok = rr == 0;
     if (ok) {
-        dual_accumulate(p, s, src, R, cnt, bad);
+        dual_accumulate(p, s, src, R, cnt, bad, ph);
+        tph = clock64();
     } else if (lane == 0) {
         if (exact) raise_err(p.hdr, CS_ERR_INTERNAL, 24);  // the exact pass must replay cleanly
         else {
@@ -1025,27 +1168,35 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
         if (wide) s.lsec[S] = NO_LSEC;
     }
     __syncwarp();
+    dphase(ph, 5, tph);
     settled += R;
     return ok;
 }
 
-__device__ __forceinline__ void flush_dual_counters(const DualParams &p, long long relaxed, long long settled,
-                                                    long long done_src) {
+__device__ __forceinline__ void flush_dual_counters(const DualParams &p, const long long *ph, long long relaxed,
+                                                    long long settled, long long done_src) {
     const long long rsum = warp_sum_ll(relaxed);
+    __syncwarp();
     if (lane_id() == 0) {
+        for (int q = 0; q < 8; q++) atomicAdd(&p.hdr->pad[q], (unsigned long long)ph[q]);
         atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
         atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
         atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
     }
 }
 
-__global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) dual_kernel(const DualParams p) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][MAXK];
+    __shared__ long long ph_all[8][8];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
     if (slot >= p.n_slots) return;
+    long long *ph = ph_all[wib];
+    if (lane < 8) ph[lane] = 0;
+    __syncwarp();
     DSlot s = dslot(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.k, slot, p.geo_n);
     if (p.pass == 3) s.lsec = (uint32_t *)(p.dense + p.dense_stride * (size_t)(slot + p.lsec_slot_off));
     long long relaxed = 0, settled = 0, done_src = 0;
@@ -1056,12 +1207,12 @@ __global__ void __launch_bounds__(256, 2) dual_kernel(const DualParams p) {
         if (idx >= (unsigned long long)p.n_src) break;
         if (__ldcg(&p.hdr->err) != 0u) break;
         const int li = p.remap ? p.remap[idx] : (int)idx;
-        if (run_dual_source(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], relaxed, settled)) {
+        if (run_dual_source(p, s, li, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled)) {
             done_src++;
             if (lane_id() == 0) count_progress(p.hdr);
         }
     }
-    flush_dual_counters(p, relaxed, settled, done_src);
+    flush_dual_counters(p, ph, relaxed, settled, done_src);
 }
 
 // Batched form: the (job, source) items of many simplest-path queries (graphs, thresholds, source
@@ -1107,10 +1258,14 @@ __global__ void __launch_bounds__(256, 2) dual_batch_kernel(const DualParams bas
                                                             int n_jobs, long long n_items) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][MAXK];
+    __shared__ long long ph_all[8][8];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
     if (slot >= base.n_slots) return;
+    long long *ph = ph_all[wib];
+    if (lane < 8) ph[lane] = 0;
+    __syncwarp();
     DSlot s = dslot(base.dense, base.dense_stride, base.compact, (size_t)base.cap, base.k, slot, base.geo_n);
     if (base.pass == 3)
         s.lsec = (uint32_t *)(base.dense + base.dense_stride * (size_t)(slot + base.lsec_slot_off));
@@ -1131,10 +1286,10 @@ __global__ void __launch_bounds__(256, 2) dual_batch_kernel(const DualParams bas
             cur_job = jb;
         }
         const int li = (int)(item - jobs[jb].item_begin);
-        if (run_dual_source(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], relaxed, settled))
+        if (run_dual_source(p, s, (int)item, p.src_list[li], hist_all[wib], cnt_all[wib], ph, relaxed, settled))
             done_src++;
     }
-    flush_dual_counters(base, relaxed, settled, done_src);
+    flush_dual_counters(base, ph, relaxed, settled, done_src);
 }
 
 // Closeness prefixes of every job with closeness (blockIdx.y strides the jobs); the bucket is
@@ -1470,9 +1625,17 @@ int dual_wide_mode() {
     return 1;
 }
 
+// Resident 256-thread blocks per SM the dual kernel is compiled for (CS_DUAL_MINB=3: a tighter
+// register budget, more warps in flight).
+int dual_minb() {
+    const char *e = getenv("CS_DUAL_MINB");
+    return (e && e[0] == '3') ? 3 : 2;
+}
+
 cs_status dlaunch(csd::DualParams &p, int n_slots, cudaStream_t s) {
     p.n_slots = n_slots;
-    csd::dual_kernel<<<(n_slots + 7) / 8, 256, 0, s>>>(p);
+    if (dual_minb() == 3) csd::dual_kernel<3><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
+    else csd::dual_kernel<2><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CS_OK : dcuda(e, "dual_kernel launch");
 }
@@ -1587,7 +1750,9 @@ cs_status cs_plan_dual(const cs_dual_graph *g, int32_t mode, int32_t k, int32_t 
     const int sms = dsm_count();
     if (sms <= 0) return dfail(CS_ERR_CUDA, "no CUDA device");
     int bpsm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, csd::dual_kernel, 256, 0);
+    cudaError_t e = dual_minb() == 3
+                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, csd::dual_kernel<3>, 256, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, csd::dual_kernel<2>, 256, 0);
     if (e != cudaSuccess) return dcuda(e, "occupancy query");
     int slots = sms * std::max(1, bpsm) * 8;
     if (max_slots > 0) slots = std::min(slots, max_slots);
@@ -1667,11 +1832,21 @@ cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, cons
     if (e == cudaSuccess && p.closeness)
         e = cudaMemsetAsync(p.bucket, 0, sizeof(double) * 3 * (size_t)K * (size_t)g->n_bound, s);
     if (e != cudaSuccess) return dcuda(e, "workspace reset");
-    long long n_over = 0, n_exact = 0;
+    long long n_over = 0, n_exact = 0, n_launch = 0;
     st = dual_passes(
         p, lay, plan, K, 2 * g->n_bound, p.n_src, dual_wide_mode(),
-        [&](csd::DualParams &pp, int slots) { return dlaunch(pp, slots, s); }, s, n_over, n_exact);
+        [&](csd::DualParams &pp, int slots) {
+            n_launch++;
+            return dlaunch(pp, slots, s);
+        },
+        s, n_over, n_exact);
     if (st != CS_OK) return st;
+    cs::WsHeader hf;
+    st = dsync_header(p.hdr, hf, s);
+    if (st != CS_OK) return st;
+    cs_set_phase_internal(hf.pad);
+    cs_set_counters_internal((long long)hf.sources_done, (long long)hf.edges_relaxed, (long long)hf.nodes_settled,
+                             n_launch + (p.closeness ? 1 : 0));
     cs_set_retries_internal(n_over, n_exact);
     if (p.closeness) {
         int blocks = std::max(1, std::min((g->n_bound + 255) / 256, dsm_count() * 8));

@@ -1569,7 +1569,7 @@ __global__ void fill_dense_kernel(char *dense, size_t dense_stride, int n_bound,
 namespace cs_host {
 thread_local std::string g_last_error;
 thread_local long long g_counters[4] = {0, 0, 0, 0};
-thread_local long long g_phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+thread_local long long g_phase[16] = {};
 }
 
 extern "C" void cs_set_error_internal(const char *msg) { cs_host::g_last_error = msg ? msg : ""; }
@@ -1580,6 +1580,18 @@ thread_local long long g_retries[2] = {0, 0};
 extern "C" void cs_set_retries_internal(long long overflowed, long long inexact) {
     cs_host::g_retries[0] = overflowed;
     cs_host::g_retries[1] = inexact;
+}
+// Phase cycle sums and diagnostics of the last call (the header's pad[0..15]); the dual host code
+// sets them too.
+extern "C" void cs_set_phase_internal(const unsigned long long *pad) {
+    for (int i = 0; i < 16; i++) cs_host::g_phase[i] = (long long)pad[i];
+}
+// Device counters of the last call (sources done, edges relaxed, states settled, launches).
+extern "C" void cs_set_counters_internal(long long sources, long long relaxed, long long settled, long long launches) {
+    cs_host::g_counters[0] = sources;
+    cs_host::g_counters[1] = relaxed;
+    cs_host::g_counters[2] = settled;
+    cs_host::g_counters[3] = launches;
 }
 extern "C" cs_status cs_last_retries(int64_t *overflowed, int64_t *inexact) {
     if (overflowed) *overflowed = cs_host::g_retries[0];
@@ -2010,7 +2022,7 @@ cs_status run_primal(const cs_primal_graph *g, const cs_query *q, const cs_plan 
     g_counters[0] = done;
     g_counters[1] = rel;
     g_counters[2] = set;
-    for (int i = 0; i < 8; i++) cs_host::g_phase[i] = (long long)h.pad[i];
+    for (int i = 0; i < 16; i++) cs_host::g_phase[i] = (long long)h.pad[i];
     cs_set_retries_internal(n_over, 0);
     return CS_OK;
 }
@@ -2068,7 +2080,7 @@ int32_t cs_device_sm_count(void) { return sm_count(); }
 
 cs_status cs_last_phase_cycles(int64_t *cycles, int32_t n) {
     if (!cycles || n < 0) return fail(CS_ERR_ARG, "cycles is NULL");
-    for (int i = 0; i < n && i < 8; i++) cycles[i] = cs_host::g_phase[i];
+    for (int i = 0; i < n && i < 16; i++) cycles[i] = cs_host::g_phase[i];
     return CS_OK;
 }
 

@@ -329,7 +329,13 @@ cs_status cs_batch_failed(void *workspace_dev, const cs_plan *plan, int32_t *ite
 cs_status cs_last_counters(int64_t *sources, int64_t *edges_relaxed, int64_t *nodes_settled, int64_t *launches);
 
 /* Per-phase SM cycles of the last call on this thread, summed over warps: 0 search, 1 sort,
- * 2 predecessor replay, 3 closeness, 4 sigma, 5 backward sweep, 6 scratch reset (n <= 8). */
+ * 2 predecessor replay, 3 closeness, 4 sigma, 5 backward sweep, 6 scratch reset.  After a
+ * simplest-path call: 0 search, 1 sort, 2 replay, 3 node best + closeness, 4 backward sweep,
+ * 5 scratch reset, 6 exact heap search; 7 holds the number of replay rounds instead.  Entries 8-15
+ * (n <= 16) are diagnostics: 8 the live progress count; after a simplest-path call 9-11 the
+ * replayed states whose route came out below / above their search key / unreached, 12-14 the
+ * replay rounds that ended with the routes out of order / an unreached state offered to / a state
+ * reached outside the search's set. */
 cs_status cs_last_phase_cycles(int64_t *cycles, int32_t n);
 
 /* Source-indexed plan built on the device without synchronising (prepare_source_sampling with
