@@ -59,6 +59,8 @@ class DualGraph(C.Structure):
         ("rptr", _ptr),
         ("rfrom", _ptr),
         ("rid", _ptr),
+        ("fwd_pack", _ptr),
+        ("rev_pack", _ptr),
     ]
 
 
@@ -238,6 +240,7 @@ SIGNATURES = {
     "cs_source_weights": (C.c_int32, [_ptr, C.c_int64, _ptr, C.c_int32, _ptr, _ptr, _ptr]),
     "cs_device_sm_count": (C.c_int32, []),
     "cs_last_phase_cycles": (C.c_int32, [_ptr, C.c_int32]),
+    "cs_dual_pack": (C.c_int32, [C.POINTER(DualGraph), _ptr, _ptr, _ptr]),
     "cs_centrality_shortest_noalloc": (
         C.c_int32,
         [C.POINTER(PrimalGraph), C.POINTER(Query), Outputs, _ptr],

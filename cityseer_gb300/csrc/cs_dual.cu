@@ -206,6 +206,7 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
     int R = 2, nnear = 2, nfar = 0;
     ulonglong2 *cur = s.qa, *nxt = s.qb;
     float T = p.delta;
+    float fmn = __int_as_float(INF_BITS);  // this lane's smallest route queued far since the last split
     bool overflow = false;
     while (true) {
         while (nnear > 0) {
@@ -223,26 +224,31 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
                 relaxed += deg;
                 const float rU = hi_f(kS), sU = lo_f(kS);
                 const int maxdeg = warp_max_i(deg);
-                for (int j = 0; j < maxdeg; j++) {
-                    int V = 0;
-                    unsigned long long nk = KEY_INF;
-                    bool imp = false, first = false;
-                    float cr = 0.0f;
-                    if (j < deg) {
-                        const int ej = beg + j;
-                        if (__ldg(&p.g.exit_slot_dev[ej]) == 1 - e) {
-                            const float cs_ = __fadd_rn(sU, __ldg(&p.g.w_dev[ej]));
-                            if (cs_ <= p.maxsec) {
-                                V = 2 * __ldg(&p.g.to_dev[ej]) + __ldg(&p.g.entry_slot_dev[ej]);
-                                cr = cand_route(rU, __ldg(&p.g.ang_dev[ej]), __ldg(&p.g.len_dev[ej]));
-                                nk = pack(cr, cs_);
-                                const unsigned long long o = atomicMin(&s.key[V], nk);
-                                imp = nk < o;
-                                first = imp && o == KEY_INF;
-                            }
-                        }
+                const uint4 *fe = (const uint4 *)p.g.fwd_pack_dev;
+                // four edges at a time: their records load together, then their atomics issue together
+                for (int j0 = 0; j0 < maxdeg; j0 += 4) {
+                    int Vq[4];
+                    float crq[4];
+                    unsigned long long nkq[4], oq[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const uint4 ed = (j0 + q < deg) ? __ldg(&fe[beg + j0 + q]) : make_uint4(0u, 0u, 0u, 0u);
+                        const float cs_ = __fadd_rn(sU, __uint_as_float(ed.y));
+                        const bool ok = j0 + q < deg && (int)(ed.x >> 31) == 1 - e && cs_ <= p.maxsec;
+                        Vq[q] = (int)(ed.x & 0x7fffffffu);
+                        crq[q] = cand_route(rU, __uint_as_float(ed.z), __uint_as_float(ed.w));
+                        nkq[q] = ok ? pack(crq[q], cs_) : KEY_INF;
                     }
-                    dpush(first, imp ? (cr < T ? 1 : 2) : 0, V, nk, R, nnext, nfar, cap, qcap, s, nxt, lt);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) oq[q] = nkq[q] != KEY_INF ? atomicMin(&s.key[Vq[q]], nkq[q]) : KEY_INF;
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const bool imp = nkq[q] < oq[q];
+                        const bool first = imp && oq[q] == KEY_INF;
+                        const int route = imp ? (crq[q] < T ? 1 : 2) : 0;
+                        if (route == 2) fmn = fminf(fmn, crq[q]);
+                        dpush(first, route, Vq[q], nkq[q], R, nnext, nfar, cap, qcap, s, nxt, lt);
+                    }
                 }
             }
             __syncwarp();
@@ -252,25 +258,21 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
         }
         if (overflow) break;
         if (nfar == 0) break;
-        float mn = __int_as_float(INF_BITS);
-        for (int i = lane; i < nfar; i += 32) {
-            const ulonglong2 ent = s.qf[i];
-            const unsigned long long k = __ldcg(&s.key[(int)ent.x]);
-            if (k == ent.y) mn = fminf(mn, hi_f(k));
-        }
-        mn = warp_min_f(mn);
-        const float Told = T;
-        T = (mn == __int_as_float(INF_BITS)) ? Told
-                                             : fmaxf(__fadd_rn(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        // next band from the smallest queued far route (lane minima over the pushes and the entries
+        // the last split kept); one streaming pass by the queued routes, dead entries dropped when
+        // their band runs
+        const float mn = warp_min_f(fmn);
+        T = fmaxf(__fadd_rn(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        fmn = __int_as_float(INF_BITS);
         int nn = 0, nf2 = 0;
         for (int base = 0; base < nfar; base += 32) {
             const int i = base + lane;
             const bool act = i < nfar;
             const ulonglong2 ent = act ? s.qf[i] : make_ulonglong2(0ull, KEY_INF);
-            const unsigned long long k = act ? __ldcg(&s.key[(int)ent.x]) : KEY_INF;
-            const bool live = act && k == ent.y;
-            const bool tonear = live && hi_f(k) < T;
-            const bool keep = live && !tonear;
+            const float r = hi_f(ent.y);
+            const bool tonear = act && r < T;
+            const bool keep = act && !tonear;
+            if (keep) fmn = fminf(fmn, r);
             const unsigned mt = __ballot_sync(FULL, tonear);
             const unsigned mk = __ballot_sync(FULL, keep);
             __syncwarp();
@@ -321,6 +323,7 @@ __device__ int dual_search_wide(const DualParams &p, const DSlot &s, int src, lo
     int R = 2, nnear = 2, nfar = 0;
     ulonglong2 *cur = s.qa, *nxt = s.qb;
     float T = p.delta;
+    float fmn = __int_as_float(INF_BITS);
     bool overflow = false;
     while (true) {
         while (nnear > 0) {
@@ -348,20 +351,20 @@ __device__ int dual_search_wide(const DualParams &p, const DSlot &s, int src, lo
                     bool impk = false, impl = false, first = false;
                     float cr = 0.0f;
                     if (j < deg) {
-                        const int ej = beg + j;
-                        if (__ldg(&p.g.exit_slot_dev[ej]) == 1 - e) {
-                            const float w = __ldg(&p.g.w_dev[ej]);
+                        const uint4 ed = __ldg((const uint4 *)p.g.fwd_pack_dev + beg + j);
+                        if ((int)(ed.x >> 31) == 1 - e) {
+                            const float w = __uint_as_float(ed.y);
                             const float cs_ = has_key ? __fadd_rn(sU, w) : __int_as_float(INF_BITS);
                             // a key's path is a path too: lsec stays <= the key's seconds
                             const float ls_ = fminf(__fadd_rn(lU, w), cs_);
                             if (ls_ <= p.maxsec) {
-                                V = 2 * __ldg(&p.g.to_dev[ej]) + __ldg(&p.g.entry_slot_dev[ej]);
+                                V = (int)(ed.x & 0x7fffffffu);
                                 lb = __float_as_uint(ls_);
                                 const uint32_t ol = atomicMin(&s.lsec[V], lb);
                                 impl = lb < ol;
                                 first = impl && ol == NO_LSEC;
                                 if (cs_ <= p.maxsec) {
-                                    cr = cand_route(rU, __ldg(&p.g.ang_dev[ej]), __ldg(&p.g.len_dev[ej]));
+                                    cr = cand_route(rU, __uint_as_float(ed.z), __uint_as_float(ed.w));
                                     nk = pack(cr, cs_);
                                     const unsigned long long o = atomicMin(&s.key[V], nk);
                                     impk = nk < o;
@@ -370,6 +373,7 @@ __device__ int dual_search_wide(const DualParams &p, const DSlot &s, int src, lo
                         }
                     }
                     const int route = impk ? (cr < T ? 1 : 2) : (impl ? 1 : 0);
+                    if (route == 2) fmn = fminf(fmn, cr);
                     const ulonglong2 ne = make_ulonglong2(
                         (unsigned long long)(uint32_t)V | ((unsigned long long)(impl ? lb : NO_LSEC) << 32),
                         impk ? nk : NO_KEY);
@@ -400,28 +404,19 @@ __device__ int dual_search_wide(const DualParams &p, const DSlot &s, int src, lo
         }
         if (overflow) break;
         if (nfar == 0) break;
-        float mn = __int_as_float(INF_BITS);
-        for (int i = lane; i < nfar; i += 32) {
-            const ulonglong2 ent = s.qf[i];
-            const unsigned long long k = __ldcg(&s.key[(int)(uint32_t)ent.x]);
-            if (k == ent.y) mn = fminf(mn, hi_f(k));
-        }
-        mn = warp_min_f(mn);
-        const float Told = T;
-        T = (mn == __int_as_float(INF_BITS)) ? Told
-                                             : fmaxf(__fadd_rn(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        // as in dual_search: far entries always carry a key part (lsec-only entries go near)
+        const float mn = warp_min_f(fmn);
+        T = fmaxf(__fadd_rn(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        fmn = __int_as_float(INF_BITS);
         int nn = 0, nf2 = 0;
         for (int base = 0; base < nfar; base += 32) {
             const int i = base + lane;
             const bool act = i < nfar;
             const ulonglong2 ent = act ? s.qf[i] : make_ulonglong2(0ull, NO_KEY);
-            const int S = (int)(uint32_t)ent.x;
-            const uint32_t nl = (uint32_t)(ent.x >> 32);
-            const unsigned long long k = act ? __ldcg(&s.key[S]) : KEY_INF;
-            const bool klive = act && ent.y != NO_KEY && k == ent.y;
-            const bool llive = act && nl != NO_LSEC && __ldcg(&s.lsec[S]) == nl;
-            const bool tonear = (klive && hi_f(k) < T) || (!klive && llive);
-            const bool keep = klive && !tonear;
+            const float r = hi_f(ent.y);
+            const bool tonear = act && r < T;
+            const bool keep = act && !tonear;
+            if (keep) fmn = fminf(fmn, r);
             const unsigned mt = __ballot_sync(FULL, tonear);
             const unsigned mk = __ballot_sync(FULL, keep);
             __syncwarp();
@@ -558,45 +553,6 @@ struct DOff {
     float cs[DPM];
     unsigned valid;  // offers settled before the target
 };
-
-// Offers to the state at position i (state V): incoming dual edges of V's node that enter at V's
-// slot, from reached states settled before it.  Needs rB/sB of those states.
-__device__ __forceinline__ void gather_doffers(const DualParams &p, const DSlot &s, int V, int i, int R, DOff &o,
-                                               bool &bad) {
-    const int v = V >> 1, sv = V & 1;
-    const int beg = __ldg(&p.g.rptr_dev[v]);
-    const int deg = min(__ldg(&p.g.rptr_dev[v + 1]) - beg, DPM);
-    o.valid = 0u;
-    int ids[DPM], us[DPM];
-#pragma unroll
-    for (int j = 0; j < DPM; j++) {
-        ids[j] = (j < deg) ? __ldg(&p.g.rid_dev[beg + j]) : 0;
-        us[j] = (j < deg) ? __ldg(&p.g.rfrom_dev[beg + j]) : 0;
-    }
-    uint32_t aa[DPM];
-#pragma unroll
-    for (int j = 0; j < DPM; j++) {
-        aa[j] = 0u;
-        if (j < deg && __ldg(&p.g.entry_slot_dev[ids[j]]) == sv) {
-            const int U = 2 * us[j] + (1 - __ldg(&p.g.exit_slot_dev[ids[j]]));
-            aa[j] = s.aux[U];
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < DPM; j++) {
-        o.pos[j] = -1;
-        o.cr[j] = 0.0f;
-        o.cs[j] = 0.0f;
-        if (aa[j] > (uint32_t)R) bad = true;
-        if (aa[j] != 0u && aa[j] <= (uint32_t)R && (int)aa[j] - 1 < i) {
-            const int pu = (int)aa[j] - 1;
-            o.pos[j] = pu;
-            o.cr[j] = cand_route(s.rB[pu], __ldg(&p.g.ang_dev[ids[j]]), __ldg(&p.g.len_dev[ids[j]]));
-            o.cs[j] = __fadd_rn(s.sB[pu], __ldg(&p.g.w_dev[ids[j]]));
-            o.valid |= 1u << j;
-        }
-    }
-}
 
 __device__ __forceinline__ int dnext(const DOff &o, unsigned todo) {
     int best = -1, bp = 0x7fffffff;
@@ -752,7 +708,7 @@ __device__ __forceinline__ int first_ks(const DualParams &p, float secs) {
 // check_reach: run the reach check even when every replayed value equals its key (the keys were
 // rewritten by an earlier round, and the search never relaxed from the rewritten seconds).
 __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, bool &bad, bool rewrite,
-                           bool check_reach) {
+                           bool check_reach, int start) {
     const int lane = lane_id();
     bool mismatch = false;
     // The replay recomputes every state's (route, seconds) from its offers in settle order, as the
@@ -761,7 +717,7 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
     // reference's seconds are then never larger, so the replay is exact as long as no state the
     // search left unreached is offered within the cutoff by the replayed seconds (checked below).
     bool secs_diff = false;
-    for (int base = 0; base < R; base += 32) {
+    for (int base = start; base < R; base += 32) {
         const int i = base + lane;
         const bool act = i < R;
         const int V = act ? s.ord[i] : 0;
@@ -772,25 +728,18 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
         DOff o;
         o.valid = 0u;
         unsigned pm = 0u;
-        int oid[DPM];
+        const uint4 *re = (const uint4 *)p.g.rev_pack_dev;
+        int rbeg = 0;  // the state's incoming records: re[rbeg + j]
         if (act && !is_src) {
             const int v = V >> 1, sv = V & 1;
-            const int beg = __ldg(&p.g.rptr_dev[v]);
-            const int deg = min(__ldg(&p.g.rptr_dev[v + 1]) - beg, DPM);
-            int us[DPM];
-#pragma unroll
-            for (int j = 0; j < DPM; j++) {
-                oid[j] = (j < deg) ? __ldg(&p.g.rid_dev[beg + j]) : 0;
-                us[j] = (j < deg) ? __ldg(&p.g.rfrom_dev[beg + j]) : 0;
-            }
+            rbeg = __ldg(&p.g.rptr_dev[v]);
+            const int deg = min(__ldg(&p.g.rptr_dev[v + 1]) - rbeg, DPM);
             uint32_t aa[DPM];
 #pragma unroll
             for (int j = 0; j < DPM; j++) {
                 aa[j] = 0u;
-                if (j < deg && __ldg(&p.g.entry_slot_dev[oid[j]]) == sv) {
-                    const int U = 2 * us[j] + (1 - __ldg(&p.g.exit_slot_dev[oid[j]]));
-                    aa[j] = s.aux[U];
-                }
+                const unsigned x = (j < deg) ? __ldg(&re[rbeg + j]).x : 0u;
+                if (j < deg && (int)(x >> 31) == sv) aa[j] = s.aux[x & 0x7fffffffu];
             }
 #pragma unroll
             for (int j = 0; j < DPM; j++) {
@@ -809,7 +758,6 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
                 o.pos[j] = -1;
                 o.cr[j] = 0.0f;
                 o.cs[j] = 0.0f;
-                oid[j] = 0;
             }
         }
         bool mine = !act;
@@ -832,9 +780,9 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
                         o.cs[j] = 0.0f;
                         if ((o.valid >> j) & 1u) {
                             const int pu = o.pos[j];
-                            o.cr[j] = cand_route(__ldcg(&s.rB[pu]), __ldg(&p.g.ang_dev[oid[j]]),
-                                                 __ldg(&p.g.len_dev[oid[j]]));
-                            o.cs[j] = __fadd_rn(__ldcg(&s.sB[pu]), __ldg(&p.g.w_dev[oid[j]]));
+                            const uint4 ed = __ldg(&re[rbeg + j]);
+                            o.cr[j] = cand_route(__ldcg(&s.rB[pu]), __uint_as_float(ed.z), __uint_as_float(ed.w));
+                            o.cs[j] = __fadd_rn(__ldcg(&s.sB[pu]), __uint_as_float(ed.y));
                         }
                     }
                 const unsigned pmask = dreplay(p, o, route, secs);
@@ -909,8 +857,9 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
     if (!check_reach && !any_mismatch && !__any_sync(FULL, secs_diff)) return 0;
     __syncwarp();
     // reach check with the replayed seconds: every in-cutoff offer must land on a reached state.
-    // After mismatches, a state the replay left unreached may only have been positioned before its
-    // offerers: an in-cutoff offer to it means the order was wrong (another round).
+    // After mismatches (in this round or, for the states ahead of start, an earlier one), a state the
+    // replay left unreached may only have been positioned before its offerers: an in-cutoff offer to
+    // it means the order was wrong (another round).
     bool escape = false, stale = false;
     for (int i = lane; i < R; i += 32) {
         const int U = s.ord[i];
@@ -918,12 +867,13 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
         const float sU = s.sB[i];
         const int beg = __ldg(&p.g.ptr_dev[u]), end = __ldg(&p.g.ptr_dev[u + 1]);
         for (int ej = beg; ej < end; ej++) {
-            if (__ldg(&p.g.exit_slot_dev[ej]) != 1 - e) continue;
-            if (__fadd_rn(sU, __ldg(&p.g.w_dev[ej])) > p.maxsec) continue;
-            const int V = 2 * __ldg(&p.g.to_dev[ej]) + __ldg(&p.g.entry_slot_dev[ej]);
+            const uint4 ed = __ldg((const uint4 *)p.g.fwd_pack_dev + ej);
+            if ((int)(ed.x >> 31) != 1 - e) continue;
+            if (__fadd_rn(sU, __uint_as_float(ed.y)) > p.maxsec) continue;
+            const int V = (int)(ed.x & 0x7fffffffu);
             const uint32_t a = s.aux[V];
             if (a == 0u) escape = true;
-            else if (any_mismatch && __ldcg(&s.rB[a - 1]) == __int_as_float(INF_BITS)) stale = true;
+            else if ((any_mismatch || check_reach) && __ldcg(&s.rB[a - 1]) == __int_as_float(INF_BITS)) stale = true;
         }
     }
     if (__any_sync(FULL, stale)) {
@@ -1133,16 +1083,38 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
     // the widened set's keyless states that the reference reaches take one more round to sort
     const int rounds = exact ? 1 : max(1, p.replay_rounds) + (wide ? 4 : 0);
     int rounds_run = 0;
+    int32_t *prev = (int32_t *)s.nbR;  // the previous round's order (nbR is free until the accumulation)
     for (int it = 0; it < rounds && rr == 1; it++) {
         rounds_run++;
-        if (!exact) warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb,
-                                    s.vb, s.rk, s.ord, hist);
-        __syncwarp();
-        for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+        int start = 0;
+        if (!exact) {
+            if (it > 0)
+                for (int i = lane; i < R; i += 32) prev[i] = s.ord[i];
+            __syncwarp();
+            warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb, s.vb, s.rk,
+                            s.ord, hist);
+            __syncwarp();
+            if (it > 0) {
+                // the states ahead of the first moved one keep their place, offers and replayed
+                // values: the next round replays from that one's chunk on
+                start = R;
+                for (int base = 0; base < R; base += 32) {
+                    const int i = base + lane;
+                    const unsigned moved = __ballot_sync(FULL, i < R && __ldcg(&s.ord[i]) != prev[i]);
+                    if (moved) {
+                        start = base + __ffs(moved) - 1;
+                        break;
+                    }
+                }
+                start &= ~31;
+                if (lane == 0) ph[15] += start;
+            }
+        }
+        for (int i = start + lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
         __syncwarp();
         dphase(ph, 1, tph);
         // after a round that rewrote keys, lower rewritten seconds may reach states the search cut
-        rr = dual_replay(p, s, src, R, bad, !exact, it > 0);
+        rr = dual_replay(p, s, src, R, bad, !exact, it > 0, start);
         __syncwarp();
         dphase(ph, 2, tph);
     }
@@ -1179,6 +1151,7 @@ __device__ __forceinline__ void flush_dual_counters(const DualParams &p, const l
     __syncwarp();
     if (lane_id() == 0) {
         for (int q = 0; q < 8; q++) atomicAdd(&p.hdr->pad[q], (unsigned long long)ph[q]);
+        atomicAdd(&p.hdr->pad[15], (unsigned long long)ph[15]);
         atomicAdd(&p.hdr->edges_relaxed, (unsigned long long)rsum);
         atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
         atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
@@ -1189,13 +1162,13 @@ template <int MINB>
 __global__ void __launch_bounds__(256, MINB) dual_kernel(const DualParams p) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][MAXK];
-    __shared__ long long ph_all[8][8];
+    __shared__ long long ph_all[8][16];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
     if (slot >= p.n_slots) return;
     long long *ph = ph_all[wib];
-    if (lane < 8) ph[lane] = 0;
+    if (lane < 16) ph[lane] = 0;
     __syncwarp();
     DSlot s = dslot(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.k, slot, p.geo_n);
     if (p.pass == 3) s.lsec = (uint32_t *)(p.dense + p.dense_stride * (size_t)(slot + p.lsec_slot_off));
@@ -1258,13 +1231,13 @@ __global__ void __launch_bounds__(256, 2) dual_batch_kernel(const DualParams bas
                                                             int n_jobs, long long n_items) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][MAXK];
-    __shared__ long long ph_all[8][8];
+    __shared__ long long ph_all[8][16];
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int slot = (int)((blockIdx.x * (blockDim.x >> 5)) + wib);
     if (slot >= base.n_slots) return;
     long long *ph = ph_all[wib];
-    if (lane < 8) ph[lane] = 0;
+    if (lane < 16) ph[lane] = 0;
     __syncwarp();
     DSlot s = dslot(base.dense, base.dense_stride, base.compact, (size_t)base.cap, base.k, slot, base.geo_n);
     if (base.pass == 3)
@@ -1498,6 +1471,19 @@ __global__ void __launch_bounds__(256) dual_tree_kernel(const DTreeParams p) {
     }
 }
 
+// Packed edge records (one 128-bit load per edge in the searches and the replay).
+__global__ void dual_pack_kernel(const cs_dual_graph g, uint4 *fwd, uint4 *rev) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.n_edges; e += gridDim.x * blockDim.x) {
+        const unsigned ex = g.exit_slot_dev[e], en = g.entry_slot_dev[e];
+        fwd[e] = make_uint4((unsigned)(2 * g.to_dev[e]) + en | (ex << 31), __float_as_uint(g.w_dev[e]),
+                            __float_as_uint(g.ang_dev[e]), __float_as_uint(g.len_dev[e]));
+        const int id = g.rid_dev[e];
+        const unsigned rex = g.exit_slot_dev[id], ren = g.entry_slot_dev[id];
+        rev[e] = make_uint4((unsigned)(2 * g.rfrom_dev[e]) + (1u - rex) | (ren << 31), __float_as_uint(g.w_dev[id]),
+                            __float_as_uint(g.ang_dev[id]), __float_as_uint(g.len_dev[id]));
+    }
+}
+
 __global__ void fill_dual_dense(char *dense, size_t stride, int n_bound, int n_slots) {
     const size_t per = 2 * (size_t)n_bound;
     const size_t total = per * (size_t)n_slots;
@@ -1597,6 +1583,16 @@ cs_status dvalidate(const cs_dual_graph *g) {
     if (g->max_out_degree > csd::DPM)
         return dfail(CS_ERR_ARG, "a dual node has more than 8 incoming or outgoing dual edges (intersections of "
                                  "degree above 5); not supported by the simplest-path kernels");
+    return CS_OK;
+}
+
+// The centrality kernels read the packed edge records.
+cs_status dvalidate_packed(const cs_dual_graph *g) {
+    if (g->n_bound >= (1 << 30)) return dfail(CS_ERR_ARG, "dual graph too large (2^30 nodes or more)");
+    if (g->n_edges > 0 && (!g->fwd_pack_dev || !g->rev_pack_dev))
+        return dfail(CS_ERR_ARG, "dual graph without packed edge records (cs_dual_pack)");
+    if (((uintptr_t)g->fwd_pack_dev | (uintptr_t)g->rev_pack_dev) & 15u)
+        return dfail(CS_ERR_ARG, "packed edge records must be 16-byte aligned");
     return CS_OK;
 }
 
@@ -1740,6 +1736,20 @@ cs_status dual_passes(const csd::DualParams &p, const DLayout &lay, const cs_pla
 
 extern "C" {
 
+cs_status cs_dual_pack(const cs_dual_graph *g, void *fwd_pack_dev, void *rev_pack_dev, void *stream) {
+    cs_status st = dvalidate(g);
+    if (st != CS_OK) return st;
+    if (g->n_bound >= (1 << 30)) return dfail(CS_ERR_ARG, "dual graph too large (2^30 nodes or more)");
+    if (g->n_edges <= 0) return CS_OK;
+    if (!fwd_pack_dev || !rev_pack_dev) return dfail(CS_ERR_ARG, "packed record arrays are NULL");
+    if (((uintptr_t)fwd_pack_dev | (uintptr_t)rev_pack_dev) & 15u)
+        return dfail(CS_ERR_ARG, "packed edge records must be 16-byte aligned");
+    const int blocks = std::max(1, std::min((g->n_edges + 255) / 256, std::max(1, dsm_count()) * 8));
+    csd::dual_pack_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(*g, (uint4 *)fwd_pack_dev, (uint4 *)rev_pack_dev);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CS_OK : dcuda(e, "dual_pack_kernel launch");
+}
+
 cs_status cs_plan_dual(const cs_dual_graph *g, int32_t mode, int32_t k, int32_t cap, int32_t max_slots,
                        int64_t mem_budget_bytes, cs_plan *plan) {
     cs_status st = dvalidate(g);
@@ -1775,6 +1785,7 @@ cs_status cs_plan_dual(const cs_dual_graph *g, int32_t mode, int32_t k, int32_t 
 cs_status cs_centrality_simplest(const cs_dual_graph *g, const cs_query *q, const cs_plan *plan, void *ws,
                                  size_t ws_bytes, cs_outputs out, void *stream_v) {
     cs_status st = dvalidate(g);
+    if (st == CS_OK) st = dvalidate_packed(g);
     if (st != CS_OK) return st;
     if (!q || !plan || !ws) return dfail(CS_ERR_ARG, "query/plan/workspace is NULL");
     const int K = q->k;
@@ -1881,6 +1892,7 @@ cs_status dbatch_shape(const cs_dual_batch_job *jobs, int n_jobs, DBatchShape &b
     b.max_k = 1;
     for (int j = 0; j < n_jobs; j++) {
         cs_status st = dvalidate(&jobs[j].g);
+        if (st == CS_OK) st = dvalidate_packed(&jobs[j].g);
         if (st != CS_OK) return st;
         if (jobs[j].k < 1 || jobs[j].k > CS_MAX_THRESHOLDS) return dfail(CS_ERR_ARG, "threshold count out of range");
         if (!jobs[j].out_dev) return dfail(CS_ERR_ARG, "job without out_dev");

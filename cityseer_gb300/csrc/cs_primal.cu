@@ -206,6 +206,7 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
     int R = 1, nnear = 1, nfar = 0;
     uint2 *cur = s.qa, *nxt = s.qb;
     float T = p.delta;
+    float fmn = __int_as_float(INF_BITS);  // this lane's smallest distance queued far since the last split
     bool overflow = false;
     while (true) {
         while (nnear > 0) {
@@ -245,6 +246,7 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
                     if (j >= maxdeg) break;
                     const bool imp = (j < deg) && vv[j] != u && cc[j] <= p.maxsec && __float_as_int(cc[j]) < old[j];
                     const int route = imp ? (cc[j] < T ? 1 : 2) : 0;
+                    if (route == 2) fmn = fminf(fmn, cc[j]);
                     push_entries(imp && old[j] == INF_BITS, route, vv[j], cc[j], R, nnext, nfar, cap, qcap, s, nxt,
                                  lt);
                 }
@@ -262,7 +264,9 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
                             first = imp && o == INF_BITS;
                         }
                     }
-                    push_entries(first, imp ? (c < T ? 1 : 2) : 0, v, c, R, nnext, nfar, cap, qcap, s, nxt, lt);
+                    const int route = imp ? (c < T ? 1 : 2) : 0;
+                    if (route == 2) fmn = fminf(fmn, c);
+                    push_entries(first, route, v, c, R, nnext, nfar, cap, qcap, s, nxt, lt);
                 }
             }
             __syncwarp();
@@ -272,27 +276,22 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
         }
         if (overflow) break;
         if (nfar == 0) break;
-        // Next band starts at the smallest live pending distance.
-        float mn = __int_as_float(INF_BITS);
-        for (int i = lane; i < nfar; i += 32) {
-            const uint2 ent = s.qf[i];
-            const float d = __ldcg(&dist[ent.x]);
-            if (__float_as_uint(d) == ent.y) mn = fminf(mn, d);
-        }
-        mn = warp_min_f(mn);
-        const float Told = T;
-        // next band: [mn, mn + delta); strictly above mn even when delta is below mn's ulp
-        T = (mn == __int_as_float(INF_BITS)) ? Told
-                                             : fmaxf(fadd(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        // Next band: [mn, mn + delta) from the smallest queued far distance (the lanes' minima over
+        // the pushes and over the entries the last split kept), strictly above mn even when delta is
+        // below mn's ulp.  One streaming pass over the far queue, by the queued distances: entries
+        // that died since they were queued are dropped when their band runs.
+        const float mn = warp_min_f(fmn);
+        T = fmaxf(fadd(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        fmn = __int_as_float(INF_BITS);
         int nn = 0, nf2 = 0;
         for (int base = 0; base < nfar; base += 32) {
             const int i = base + lane;
             const bool act = i < nfar;
             const uint2 ent = act ? s.qf[i] : make_uint2(0u, 0u);
-            const float d = act ? __ldcg(&dist[ent.x]) : 0.0f;
-            const bool live = act && __float_as_uint(d) == ent.y;
-            const bool tonear = live && d < T;
-            const bool keep = live && !tonear;
+            const float d = __uint_as_float(ent.y);
+            const bool tonear = act && d < T;
+            const bool keep = act && !tonear;
+            if (keep) fmn = fminf(fmn, d);
             const unsigned mt = __ballot_sync(FULL, tonear);
             const unsigned mk = __ballot_sync(FULL, keep);
             __syncwarp();

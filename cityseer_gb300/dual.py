@@ -97,6 +97,7 @@ class DualCSR:
         self.rfrom = t(src[ro], np.int32)
         self.rid = t(pos_in_fwd[ro], np.int32)
         self._w: dict[float, torch.Tensor] = {}
+        self._pack: dict[float, tuple[torch.Tensor, torch.Tensor]] = {}
 
     def w(self, speed: float) -> torch.Tensor:
         k = float(np.float32(speed))
@@ -107,7 +108,33 @@ class DualCSR:
             self._w[k] = hit
         return hit
 
+    def packed(self, speed: float) -> tuple[torch.Tensor, torch.Tensor]:
+        """The packed 16-byte forward and reverse edge records at this speed (cs_dual_pack)."""
+        k = float(np.float32(speed))
+        hit = self._pack.get(k)
+        if hit is None:
+            m = max(1, self.m)
+            fwd = torch.empty((m, 4), dtype=torch.int32, device=self.device)
+            rev = torch.empty((m, 4), dtype=torch.int32, device=self.device)
+            g = self._plain(speed)
+            g.fwd_pack = fwd.data_ptr()
+            g.rev_pack = rev.data_ptr()
+            stream = torch.cuda.current_stream(self.device)
+            _native.check(_native.load().cs_dual_pack(C.byref(g), fwd.data_ptr(), rev.data_ptr(),
+                                                      stream.cuda_stream), "cs_dual_pack")
+            stream.synchronize()  # callers launch on other streams too (the served lanes)
+            hit = (fwd, rev)
+            self._pack[k] = hit
+        return hit
+
     def struct(self, speed: float) -> _native.DualGraph:
+        g = self._plain(speed)
+        fwd, rev = self.packed(speed)
+        g.fwd_pack = fwd.data_ptr()
+        g.rev_pack = rev.data_ptr()
+        return g
+
+    def _plain(self, speed: float) -> _native.DualGraph:
         g = _native.DualGraph()
         g.n_bound = self.n_bound
         g.n_edges = self.m

@@ -73,6 +73,13 @@ typedef struct {
     const int32_t *rptr_dev;    /* [n_bound + 1] incoming edges (reverse CSR of the same edges) */
     const int32_t *rfrom_dev;   /* [n_edges] source node of each incoming edge */
     const int32_t *rid_dev;     /* [n_edges] index of that edge in the forward arrays */
+    /* Packed 16-byte edge records (cs_dual_pack), required by the centrality calls (the tree calls
+     * read the plain arrays): fwd_pack [n_edges] in forward order = target state (2 to + entry_slot)
+     * | exit_slot << 31, then the f32 bits of w, angle_sum and length; rev_pack [n_edges] in reverse
+     * order = offering state (2 from + 1 - exit_slot) | entry_slot << 31, w, angle_sum, length.
+     * 16-byte aligned; n_bound < 2^30. */
+    const void *fwd_pack_dev;
+    const void *rev_pack_dev;
 } cs_dual_graph;
 
 /* One centrality call.  Thresholds are the reference's resolved (distances, betas, seconds)
@@ -207,6 +214,11 @@ cs_status cs_edge_travel_seconds(int64_t n_edges, const int32_t *src, const int3
  * mode: 0 = centrality_shortest, 1 = segment_centrality, 2 = trees (isochrones). */
 cs_status cs_plan_primal(const cs_primal_graph *g, int32_t mode, int32_t k, int32_t cap, int32_t max_slots,
                          int64_t mem_budget_bytes, cs_plan *plan);
+/* Fills a dual CSR's packed edge records (cs_dual_graph.fwd_pack_dev / rev_pack_dev, each
+ * [n_edges] x 16 bytes, 16-byte aligned) from its plain arrays, w_dev included: one record per edge
+ * so that a search reads an edge with one 128-bit load.  Stream-ordered. */
+cs_status cs_dual_pack(const cs_dual_graph *g, void *fwd_pack_dev, void *rev_pack_dev, void *stream);
+
 cs_status cs_plan_dual(const cs_dual_graph *g, int32_t mode, int32_t k, int32_t cap, int32_t max_slots,
                        int64_t mem_budget_bytes, cs_plan *plan);
 
@@ -335,7 +347,8 @@ cs_status cs_last_counters(int64_t *sources, int64_t *edges_relaxed, int64_t *no
  * (n <= 16) are diagnostics: 8 the live progress count; after a simplest-path call 9-11 the
  * replayed states whose route came out below / above their search key / unreached, 12-14 the
  * replay rounds that ended with the routes out of order / an unreached state offered to / a state
- * reached outside the search's set. */
+ * reached outside the search's set, 15 the states that later replay rounds kept from the round
+ * before. */
 cs_status cs_last_phase_cycles(int64_t *cycles, int32_t n);
 
 /* Source-indexed plan built on the device without synchronising (prepare_source_sampling with
