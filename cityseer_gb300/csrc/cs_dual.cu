@@ -708,9 +708,10 @@ __device__ __forceinline__ int first_ks(const DualParams &p, float secs) {
 // check_reach: run the reach check even when every replayed value equals its key (the keys were
 // rewritten by an earlier round, and the search never relaxed from the rewritten seconds).
 __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, bool &bad, bool rewrite,
-                           bool check_reach, int start) {
+                           bool check_reach, int start, int &first_change) {
     const int lane = lane_id();
     bool mismatch = false;
+    int change = R;  // this lane's lowest position a rewritten key can move a state to or from
     // The replay recomputes every state's (route, seconds) from its offers in settle order, as the
     // reference's heap search does.  Routes must equal the search's (then the settle order is the
     // reference's).  Seconds may differ where near-tied offers arrived in another order: the
@@ -810,7 +811,19 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
                     // diagnostics: replayed route below / above the key, or unreached
                     const int slot9 = route == __int_as_float(INF_BITS) ? 11 : (route < hi_f(k) ? 9 : 10);
                     atomicAdd(&p.hdr->pad[slot9], 1ull);
-                    if (rewrite) s.key[V] = pack(route, secs);
+                    if (rewrite) {
+                        s.key[V] = pack(route, secs);
+                        // the rewritten state leaves position i for one at or after the first sorted
+                        // key not below its new route (s.rk holds the sorted keys)
+                        const uint32_t nb = __float_as_uint(route);
+                        int lo = 0, hi = min(i, R);
+                        while (lo < hi) {
+                            const int mid = (lo + hi) >> 1;
+                            if (__ldcg(&s.rk[mid]) < nb) lo = mid + 1;
+                            else hi = mid;
+                        }
+                        change = min(change, lo);
+                    }
                 } else if (__float_as_uint(secs) != (unsigned)(k & 0xffffffffull)) {
                     secs_diff = true;
                 }
@@ -826,6 +839,7 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
         }
     }
     const bool any_mismatch = __any_sync(FULL, mismatch);
+    first_change = -warp_max_i(-change);
     __syncwarp();
     if (any_mismatch) {
         // The keys only order the states: the replay ran in the reference's settle order, and is
@@ -1084,23 +1098,32 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
     const int rounds = exact ? 1 : max(1, p.replay_rounds) + (wide ? 4 : 0);
     int rounds_run = 0;
     int32_t *prev = (int32_t *)s.nbR;  // the previous round's order (nbR is free until the accumulation)
+    int first_change = 0;
+    auto key_of = [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); };
     for (int it = 0; it < rounds && rr == 1; it++) {
         rounds_run++;
         int start = 0;
         if (!exact) {
-            if (it > 0)
-                for (int i = lane; i < R; i += 32) prev[i] = s.ord[i];
-            __syncwarp();
-            warp_radix_sort(R, s.rl, [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); }, s.kb, s.vb, s.rk,
-                            s.ord, hist);
+            if (it == 0) {
+                warp_radix_sort(R, s.rl, key_of, s.kb, s.vb, s.rk, s.ord, hist);
+            } else {
+                // Only the keys the last round rewrote changed, and no state ahead of first_change
+                // moves: the suffix from there is sorted again (from its current order, which holds
+                // the same states), the prefix keeps its order and sorted keys.
+                const int p0 = max(0, min(first_change, R));
+                for (int i = p0 + lane; i < R; i += 32) prev[i] = s.ord[i];
+                __syncwarp();
+                if (p0 < R) warp_radix_sort(R - p0, s.ord + p0, key_of, s.kb, s.vb, s.rk + p0, s.ord + p0, hist);
+            }
             __syncwarp();
             if (it > 0) {
                 // the states ahead of the first moved one keep their place, offers and replayed
                 // values: the next round replays from that one's chunk on
+                const int p0 = max(0, min(first_change, R));
                 start = R;
-                for (int base = 0; base < R; base += 32) {
+                for (int base = p0 & ~31; base < R; base += 32) {
                     const int i = base + lane;
-                    const unsigned moved = __ballot_sync(FULL, i < R && __ldcg(&s.ord[i]) != prev[i]);
+                    const unsigned moved = __ballot_sync(FULL, i >= p0 && i < R && __ldcg(&s.ord[i]) != prev[i]);
                     if (moved) {
                         start = base + __ffs(moved) - 1;
                         break;
@@ -1114,7 +1137,7 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
         __syncwarp();
         dphase(ph, 1, tph);
         // after a round that rewrote keys, lower rewritten seconds may reach states the search cut
-        rr = dual_replay(p, s, src, R, bad, !exact, it > 0, start);
+        rr = dual_replay(p, s, src, R, bad, !exact, it > 0, start, first_change);
         __syncwarp();
         dphase(ph, 2, tph);
     }
