@@ -1250,7 +1250,8 @@ __device__ __forceinline__ void djob_params(const DualParams &base, const cs_dua
     p.bucket = j.bucket_dev;
 }
 
-__global__ void __launch_bounds__(256, 2) dual_batch_kernel(const DualParams base, const cs_dual_batch_job *jobs,
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) dual_batch_kernel(const DualParams base, const cs_dual_batch_job *jobs,
                                                             int n_jobs, long long n_items) {
     __shared__ uint32_t hist_all[8][256];
     __shared__ int cnt_all[8][MAXK];
@@ -1644,11 +1645,12 @@ int dual_wide_mode() {
     return 1;
 }
 
-// Resident 256-thread blocks per SM the dual kernel is compiled for (CS_DUAL_MINB=3: a tighter
-// register budget, more warps in flight).
+// Resident 256-thread blocks per SM the dual kernels are compiled for: 3 (24 warps per SM; on the
+// 124,500-node curved dual 5% faster at 2 km and 8% at 5 km than 2 blocks, despite register
+// spills); CS_DUAL_MINB=2 selects the 2-block build.
 int dual_minb() {
     const char *e = getenv("CS_DUAL_MINB");
-    return (e && e[0] == '3') ? 3 : 2;
+    return (e && e[0] == '2') ? 2 : 3;
 }
 
 cs_status dlaunch(csd::DualParams &p, int n_slots, cudaStream_t s) {
@@ -1930,7 +1932,8 @@ cs_status dbatch_shape(const cs_dual_batch_job *jobs, int n_jobs, DBatchShape &b
 cs_status dbatch_launch(csd::DualParams &p, const cs_dual_batch_job *jobs_dev, int n_jobs, long long n_items, int slots,
                         cudaStream_t s) {
     p.n_slots = slots;
-    csd::dual_batch_kernel<<<(slots + 7) / 8, 256, 0, s>>>(p, jobs_dev, n_jobs, n_items);
+    if (dual_minb() == 3) csd::dual_batch_kernel<3><<<(slots + 7) / 8, 256, 0, s>>>(p, jobs_dev, n_jobs, n_items);
+    else csd::dual_batch_kernel<2><<<(slots + 7) / 8, 256, 0, s>>>(p, jobs_dev, n_jobs, n_items);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CS_OK : dcuda(e, "dual_batch_kernel launch");
 }
