@@ -215,12 +215,15 @@ class Server:
     graphs: {graph id: primal NetworkStructure}; duals: {graph id: dual NetworkStructure} for
     simplest-path queries.  max_distance / max_thresholds bound the queries the slot geometry is
     planned for.  wave_cost is the source budget of one wave in units of a max-distance source
-    (default: one per search slot)."""
+    (default: one per search slot).  primal_hbm_frac / dual_hbm_frac: the share of the free HBM at
+    start that each of the two primal / dual lanes' workspaces may take; dual_slots caps the dual
+    lanes' slots."""
 
     def __init__(self, graphs: dict, duals: dict | None = None, *, speed_m_s: float = WALKING_SPEED,
                  max_distance: int = 5000, max_thresholds: int = 4, hbm_budget_bytes: int | None = None,
                  wave_cost: float | None = None, max_jobs_per_wave: int = 512, age_ms: float = 100.0,
-                 keep_results: bool = True, dual_slots: int = 608, cap: int = 0, max_slots: int = 0):
+                 keep_results: bool = True, dual_slots: int = 608, cap: int = 0, max_slots: int = 0,
+                 primal_hbm_frac: float = 0.12, dual_hbm_frac: float = 0.17):
         if not torch.cuda.is_available():
             raise RuntimeError("the served form needs a CUDA device")
         self.lib = _native.load()
@@ -268,7 +271,8 @@ class Server:
                 dummy[i].out = 1
                 dummy[i].compute_closeness = 0
             plan = _native.Plan()
-            _native.check(self.lib.cs_batch_plan(dummy, len(self.graphs), self.cap, max_slots, int(free0 * 0.12),
+            _native.check(self.lib.cs_batch_plan(dummy, len(self.graphs), self.cap, max_slots,
+                                                 int(free0 * primal_hbm_frac),
                                                  C.byref(plan)), "cs_batch_plan")
             self.kinds["primal"] = _Kind("primal", self.lib, _native.BatchJob, plan,
                                          lambda st, pl=plan: Workspace(pl, pl.n_bound, dev, stream=st), dev,
@@ -286,7 +290,7 @@ class Server:
                 djobs[i].compute_closeness = 0
             dplan = _native.Plan()
             slots = min(dual_slots, max_slots) if max_slots > 0 else dual_slots
-            _native.check(self.lib.cs_dual_batch_plan(djobs, len(self.duals), dcap, slots, int(free0 * 0.17),
+            _native.check(self.lib.cs_dual_batch_plan(djobs, len(self.duals), dcap, slots, int(free0 * dual_hbm_frac),
                                                       C.byref(dplan)), "cs_dual_batch_plan")
             self.kinds["dual"] = _Kind("dual", self.lib, _native.DualBatchJob, dplan,
                                        lambda st, pl=dplan: dual.DualWorkspace(pl, pl.n_bound, dev, stream=st), dev,
