@@ -361,7 +361,7 @@ cs_status cs_source_weights(const int32_t *sources_dev, int64_t n_sources, const
  * cs_batch_* does for the primal.  cs_dual_batch_run with CS_BATCH_ASYNC neither synchronises nor
  * redoes anything; cs_dual_batch_failed then lists the items that overflowed or whose replay
  * disagreed (they contributed nothing; run them again as a synchronous batch, which redoes them at
- * growing capacities and with the exact heap search). */
+ * growing capacities, then with the widened and the exact heap search). */
 cs_status cs_dual_batch_prepare(cs_dual_batch_job *jobs_host, int32_t n_jobs, int64_t *n_items);
 cs_status cs_dual_batch_plan(const cs_dual_batch_job *jobs_host, int32_t n_jobs, int32_t cap, int32_t max_slots,
                              int64_t mem_budget_bytes, cs_plan *plan);
