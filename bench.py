@@ -431,6 +431,8 @@ def extra_legs(args) -> dict:
         "dual_sources_per_s": c3["value"], "ms_per_step": c3["ms_per_step"],
         "segment_sources_per_s": c3["segment"]["value"],
         "sources_redone_exactly": c3["simplest_sources_redone_exactly"],
+        "phase_share": c3["simplest_phase_share"],
+        "replay_rounds_per_source": c3["simplest_replay_rounds_per_source"],
         "leg_seconds": round(time.perf_counter() - t0, 1),
     }
     return out
@@ -810,6 +812,13 @@ def run_c3(args):
     t_simp = timed(lambda: nsd.centrality_simplest(distances=dists))
     over, inexact = C.c_int64(), C.c_int64()
     _native.load().cs_last_retries(C.byref(over), C.byref(inexact))
+    # per-phase SM cycles of the last simplest-path call (summed over warps) and its replay rounds
+    ph = (C.c_int64 * 16)()
+    _native.load().cs_last_phase_cycles(ph, 16)
+    tot = max(1, sum(ph[:7]))
+    names = ("search", "sort", "replay", "node_best_closeness", "backward", "reset", "exact_search")
+    dual_phases = {k: round(ph[i] / tot, 4) for i, k in enumerate(names)}
+    rounds = ph[7] / max(1, nsd.node_count())
     t_seg = timed(lambda: ns.segment_centrality(distances=dists))
     clk = clocks.stop()
     line = {
@@ -830,6 +839,8 @@ def run_c3(args):
                    "distances": dists, "timing": "wall clock per public-API call, device synchronised"},
         "segment": {"value": n_seg / t_seg, "unit": "sources/s", "ms_per_step": t_seg * 1000.0},
         "simplest_sources_redone_exactly": int(inexact.value),
+        "simplest_phase_share": dual_phases,
+        "simplest_replay_rounds_per_source": round(rounds, 3),
         "setup_s": round(t_build, 1),
         "clocks": clk,
     }
