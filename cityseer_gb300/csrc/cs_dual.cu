@@ -40,6 +40,9 @@ namespace csd {
 using namespace cs;
 
 constexpr unsigned long long KEY_INF = 0xffffffffffffffffull;
+// The key of a reached state whose every offer was withdrawn (a NaN route, above every real key and
+// below KEY_INF): it offers nothing, a new offer replaces it, and it is not reached a second time.
+constexpr unsigned long long KEY_WITHDRAWN = KEY_INF - 2ull;
 constexpr int DPM = 8;  // max incoming / outgoing dual edges per state handled in registers
 
 __host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -173,32 +176,70 @@ __device__ __forceinline__ void dpush(bool first, int route, int V, unsigned lon
     const unsigned mf = __ballot_sync(FULL, first);
     const unsigned mn = __ballot_sync(FULL, route == 1);
     const unsigned mr = __ballot_sync(FULL, route == 2);
+    // a first touch's entry carries the state's discovery index + 1 in its upper half (else 0)
+    unsigned long long x = (unsigned long long)(uint32_t)V;
     if (first) {
         const int q = R + __popc(mf & lt);
-        if (q < cap) s.rl[q] = V;
+        if (q < cap) {
+            s.rl[q] = V;
+            s.aux[V] = (uint32_t)(q + 1);  // discovery index during the search (the sort rewrites it)
+            ((unsigned long long *)s.sig)[q] = KEY_INF;  // the key V last relaxed with (none yet)
+            x |= (unsigned long long)(q + 1) << 32;
+        }
     }
     if (route == 1) {
         const int q = nn + __popc(mn & lt);
-        if (q < qcap) nxt[q] = make_ulonglong2((unsigned long long)V, key);
+        if (q < qcap) nxt[q] = make_ulonglong2(x, key);
     }
     if (route == 2) {
         const int q = nf + __popc(mr & lt);
-        if (q < qcap) s.qf[q] = make_ulonglong2((unsigned long long)V, key);
+        if (q < qcap) s.qf[q] = make_ulonglong2(x, key);
     }
     R += __popc(mf);
     nn += __popc(mn);
     nf += __popc(mr);
 }
 
+// A state's key recomputed from its offerers' current keys (the lexicographic least in-cutoff offer;
+// KEY_INF when none remains).
+__device__ __noinline__ unsigned long long dual_rekey(const DualParams &p, const DSlot &s, int V) {
+    const int v = V >> 1, sv = V & 1;
+    const int beg = __ldg(&p.g.rptr_dev[v]), end = __ldg(&p.g.rptr_dev[v + 1]);
+    const uint4 *re = (const uint4 *)p.g.rev_pack_dev;
+    unsigned long long best = KEY_INF;
+    for (int k = beg; k < end; k++) {
+        const uint4 ed = __ldg(&re[k]);
+        if ((int)(ed.x >> 31) != sv) continue;
+        const unsigned long long kU = __ldcg(&s.key[ed.x & 0x7fffffffu]);
+        if (kU == KEY_INF) continue;
+        const float cs_ = __fadd_rn(lo_f(kU), __uint_as_float(ed.y));
+        if (!(cs_ <= p.maxsec)) continue;
+        const unsigned long long o = pack(cand_route(hi_f(kU), __uint_as_float(ed.z), __uint_as_float(ed.w)), cs_);
+        best = o < best ? o : best;
+    }
+    return best;
+}
+
 __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long long &relaxed) {
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
     const int cap = p.cap, qcap = 2 * cap;
+    // The key each reached state last relaxed with (by discovery index, in the sigma array, free until
+    // the replay): when a state relaxes again with a key whose offer along an edge is now cut or worse,
+    // a target whose key still equals the old offer holds a withdrawn offer, and its key is recomputed
+    // from its offerers' current keys (raised, if nothing better remains) and relaxed again, so that
+    // the withdrawal reaches its own targets.  A per-source budget bounds the withdrawals; past it the
+    // search only lowers keys (and terminates), and the replay rounds settle what is left.
+    unsigned long long *lastk = (unsigned long long *)s.sig;
     if (lane == 0) {
         s.key[2 * src] = 0ull;
         s.key[2 * src + 1] = 0ull;
         s.rl[0] = 2 * src;
         s.rl[1] = 2 * src + 1;
+        s.aux[2 * src] = 1u;
+        s.aux[2 * src + 1] = 2u;
+        lastk[0] = KEY_INF;
+        lastk[1] = KEY_INF;
         s.qa[0] = make_ulonglong2((unsigned long long)(2 * src), 0ull);
         s.qa[1] = make_ulonglong2((unsigned long long)(2 * src + 1), 0ull);
     }
@@ -207,6 +248,8 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
     ulonglong2 *cur = s.qa, *nxt = s.qb;
     float T = p.delta;
     float fmn = __int_as_float(INF_BITS);  // this lane's smallest route queued far since the last split
+    int withdrawals = 0;                   // warp-uniform
+    const int max_withdrawals = cap;
     bool overflow = false;
     while (true) {
         while (nnear > 0) {
@@ -215,14 +258,23 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
                 const int i = base + lane;
                 ulonglong2 ent = make_ulonglong2(0ull, KEY_INF);
                 if (i < nnear) ent = cur[i];
-                const int S = (int)ent.x;
+                const int S = (int)(uint32_t)ent.x;
+                const uint32_t qi = (uint32_t)(ent.x >> 32);  // discovery index + 1 of a first touch's entry
                 const unsigned long long kS = (i < nnear) ? __ldcg(&s.key[S]) : KEY_INF;
                 const bool live = (i < nnear) && kS == ent.y;
+                // a first touch's entry knows the state's discovery index; later entries look it up
+                const uint32_t aS = (live && qi == 0u) ? __ldcg(&s.aux[S]) : qi;
                 const int u = S >> 1, e = S & 1;
                 const int beg = live ? __ldg(&p.g.ptr_dev[u]) : 0;
                 const int deg = live ? __ldg(&p.g.ptr_dev[u + 1]) - beg : 0;
+                const bool track = live && aS != 0u && aS <= (uint32_t)cap;
+                const unsigned long long lk = track ? __ldcg(&lastk[aS - 1]) : KEY_INF;
                 relaxed += deg;
                 const float rU = hi_f(kS), sU = lo_f(kS);
+                const float rL = hi_f(lk), sL = lo_f(lk);
+                // withdrawals only from a state relaxing again (it has a last key), within the budget
+                const bool again = lk != KEY_INF && withdrawals < max_withdrawals;
+                int tried = 0;
                 const int maxdeg = warp_max_i(deg);
                 const uint4 *fe = (const uint4 *)p.g.fwd_pack_dev;
                 // four edges at a time: their records load together, then their atomics issue together
@@ -245,11 +297,33 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
                     for (int q = 0; q < 4; q++) {
                         const bool imp = nkq[q] < oq[q];
                         const bool first = imp && oq[q] == KEY_INF;
-                        const int route = imp ? (crq[q] < T ? 1 : 2) : 0;
-                        if (route == 2) fmn = fminf(fmn, crq[q]);
-                        dpush(first, route, Vq[q], nkq[q], R, nnext, nfar, cap, qcap, s, nxt, lt);
+                        unsigned long long pk = nkq[q];
+                        int route = imp ? (crq[q] < T ? 1 : 2) : 0;
+                        if (again && !imp && j0 + q < deg) {
+                            // the offer this edge carried at the state's last relaxation (record re-read)
+                            const uint4 ed = __ldg(&fe[beg + j0 + q]);
+                            const float ocs = __fadd_rn(sL, __uint_as_float(ed.y));
+                            if ((int)(ed.x >> 31) == 1 - e && ocs <= p.maxsec) {
+                                const unsigned long long ok =
+                                    pack(cand_route(rL, __uint_as_float(ed.z), __uint_as_float(ed.w)), ocs);
+                                // withdrawn: cut now, or worse than before, and still the target's key
+                                if ((nkq[q] == KEY_INF || nkq[q] > ok) && __ldcg(&s.key[Vq[q]]) == ok) {
+                                    tried++;
+                                    unsigned long long kn = dual_rekey(p, s, Vq[q]);
+                                    if (kn == KEY_INF) kn = KEY_WITHDRAWN;  // reached before: not a first touch again
+                                    if (kn != ok && atomicCAS(&s.key[Vq[q]], ok, kn) == ok) {
+                                        pk = kn;
+                                        route = (kn == KEY_WITHDRAWN || hi_f(kn) < T) ? 1 : 2;
+                                    }
+                                }
+                            }
+                        }
+                        if (route == 2) fmn = fminf(fmn, hi_f(pk));
+                        dpush(first, route, Vq[q], pk, R, nnext, nfar, cap, qcap, s, nxt, lt);
                     }
                 }
+                withdrawals += (int)__reduce_add_sync(FULL, (unsigned)tried);
+                if (track) lastk[aS - 1] = kS;
             }
             __syncwarp();
             if (R > cap || nnext > qcap || nfar > qcap) { overflow = true; break; }
@@ -804,7 +878,7 @@ __device__ int dual_replay(const DualParams &p, const DSlot &s, int src, int R, 
                 store_doffers(s, i, o);
                 const unsigned long long k = __ldcg(&s.key[V]);
                 // a widened-pass state without a key that the replay leaves unreached agrees
-                const bool both_unreached = k == KEY_INF && route == __int_as_float(INF_BITS);
+                const bool both_unreached = (k == KEY_INF || k == KEY_WITHDRAWN) && route == __int_as_float(INF_BITS);
                 if (both_unreached) {
                 } else if (__float_as_uint(route) != (unsigned)(k >> 32)) {
                     mismatch = true;
