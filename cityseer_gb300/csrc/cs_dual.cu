@@ -221,6 +221,7 @@ __device__ __noinline__ unsigned long long dual_rekey(const DualParams &p, const
 }
 
 __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long long &relaxed) {
+    const float maxsec_ = p.maxsec, delta_ = p.delta;  // in registers (p may live in shared memory)
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
     const int cap = p.cap, qcap = 2 * cap;
@@ -246,7 +247,7 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
     __syncwarp();
     int R = 2, nnear = 2, nfar = 0;
     ulonglong2 *cur = s.qa, *nxt = s.qb;
-    float T = p.delta;
+    float T = delta_;
     float fmn = __int_as_float(INF_BITS);  // this lane's smallest route queued far since the last split
     int withdrawals = 0;                   // warp-uniform
     const int max_withdrawals = cap;
@@ -286,7 +287,7 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
                     for (int q = 0; q < 4; q++) {
                         const uint4 ed = (j0 + q < deg) ? __ldg(&fe[beg + j0 + q]) : make_uint4(0u, 0u, 0u, 0u);
                         const float cs_ = __fadd_rn(sU, __uint_as_float(ed.y));
-                        const bool ok = j0 + q < deg && (int)(ed.x >> 31) == 1 - e && cs_ <= p.maxsec;
+                        const bool ok = j0 + q < deg && (int)(ed.x >> 31) == 1 - e && cs_ <= maxsec_;
                         Vq[q] = (int)(ed.x & 0x7fffffffu);
                         crq[q] = cand_route(rU, __uint_as_float(ed.z), __uint_as_float(ed.w));
                         nkq[q] = ok ? pack(crq[q], cs_) : KEY_INF;
@@ -303,7 +304,7 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
                             // the offer this edge carried at the state's last relaxation (record re-read)
                             const uint4 ed = __ldg(&fe[beg + j0 + q]);
                             const float ocs = __fadd_rn(sL, __uint_as_float(ed.y));
-                            if ((int)(ed.x >> 31) == 1 - e && ocs <= p.maxsec) {
+                            if ((int)(ed.x >> 31) == 1 - e && ocs <= maxsec_) {
                                 const unsigned long long ok =
                                     pack(cand_route(rL, __uint_as_float(ed.z), __uint_as_float(ed.w)), ocs);
                                 // withdrawn: cut now, or worse than before, and still the target's key
@@ -336,7 +337,7 @@ __device__ int dual_search(const DualParams &p, const DSlot &s, int src, long lo
         // the last split kept); one streaming pass by the queued routes, dead entries dropped when
         // their band runs
         const float mn = warp_min_f(fmn);
-        T = fmaxf(__fadd_rn(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        T = fmaxf(__fadd_rn(mn, delta_), __int_as_float(__float_as_int(mn) + 1));
         fmn = __int_as_float(INF_BITS);
         int nn = 0, nf2 = 0;
         for (int base = 0; base < nfar; base += 32) {
@@ -380,6 +381,7 @@ constexpr uint32_t NO_LSEC = 0xffffffffu;
 constexpr unsigned long long NO_KEY = KEY_INF - 1ull;  // a NaN route: never a key
 
 __device__ int dual_search_wide(const DualParams &p, const DSlot &s, int src, long long &relaxed) {
+    const float maxsec_ = p.maxsec, delta_ = p.delta;  // in registers (p may live in shared memory)
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
     const int cap = p.cap, qcap = 2 * cap;
@@ -396,7 +398,7 @@ __device__ int dual_search_wide(const DualParams &p, const DSlot &s, int src, lo
     __syncwarp();
     int R = 2, nnear = 2, nfar = 0;
     ulonglong2 *cur = s.qa, *nxt = s.qb;
-    float T = p.delta;
+    float T = delta_;
     float fmn = __int_as_float(INF_BITS);
     bool overflow = false;
     while (true) {
@@ -431,13 +433,13 @@ __device__ int dual_search_wide(const DualParams &p, const DSlot &s, int src, lo
                             const float cs_ = has_key ? __fadd_rn(sU, w) : __int_as_float(INF_BITS);
                             // a key's path is a path too: lsec stays <= the key's seconds
                             const float ls_ = fminf(__fadd_rn(lU, w), cs_);
-                            if (ls_ <= p.maxsec) {
+                            if (ls_ <= maxsec_) {
                                 V = (int)(ed.x & 0x7fffffffu);
                                 lb = __float_as_uint(ls_);
                                 const uint32_t ol = atomicMin(&s.lsec[V], lb);
                                 impl = lb < ol;
                                 first = impl && ol == NO_LSEC;
-                                if (cs_ <= p.maxsec) {
+                                if (cs_ <= maxsec_) {
                                     cr = cand_route(rU, __uint_as_float(ed.z), __uint_as_float(ed.w));
                                     nk = pack(cr, cs_);
                                     const unsigned long long o = atomicMin(&s.key[V], nk);
@@ -480,7 +482,7 @@ __device__ int dual_search_wide(const DualParams &p, const DSlot &s, int src, lo
         if (nfar == 0) break;
         // as in dual_search: far entries always carry a key part (lsec-only entries go near)
         const float mn = warp_min_f(fmn);
-        T = fmaxf(__fadd_rn(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        T = fmaxf(__fadd_rn(mn, delta_), __int_as_float(__float_as_int(mn) + 1));
         fmn = __int_as_float(INF_BITS);
         int nn = 0, nf2 = 0;
         for (int base = 0; base < nfar; base += 32) {
@@ -1341,7 +1343,9 @@ __global__ void __launch_bounds__(256, MINB) dual_batch_kernel(const DualParams 
     if (base.pass == 3)
         s.lsec = (uint32_t *)(base.dense + base.dense_stride * (size_t)(slot + base.lsec_slot_off));
     long long relaxed = 0, settled = 0, done_src = 0;
-    DualParams p;
+    // the warp's job parameters in shared memory (a local copy would sit in the stack frame)
+    __shared__ DualParams pj_all[8];
+    DualParams &p = pj_all[wib];
     int cur_job = -1;
     while (true) {
         unsigned long long idx = 0;
@@ -1353,7 +1357,8 @@ __global__ void __launch_bounds__(256, MINB) dual_batch_kernel(const DualParams 
         const long long item = base.remap ? (long long)base.remap[idx] : (long long)idx;
         const int jb = djob_of(jobs, n_jobs, item);
         if (jb != cur_job) {
-            djob_params(base, jobs[jb], p);
+            if (lane == 0) djob_params(base, jobs[jb], p);
+            __syncwarp();
             cur_job = jb;
         }
         const int li = (int)(item - jobs[jb].item_begin);

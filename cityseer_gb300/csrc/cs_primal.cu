@@ -196,6 +196,7 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
     const int32_t *__restrict__ in_ptr = p.g.in_ptr_dev;
     const int32_t *__restrict__ in_nb = p.g.in_nb_dev;
     const float *__restrict__ in_w = p.g.in_w_dev;
+    const float maxsec = p.maxsec, delta = p.delta;  // in registers (p may live in shared memory)
     float *dist = s.dist;
     if (lane == 0) {
         dist[src] = 0.0f;
@@ -205,7 +206,7 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
     __syncwarp();
     int R = 1, nnear = 1, nfar = 0;
     uint2 *cur = s.qa, *nxt = s.qb;
-    float T = p.delta;
+    float T = delta;
     float fmn = __int_as_float(INF_BITS);  // this lane's smallest distance queued far since the last split
     bool overflow = false;
     while (true) {
@@ -237,14 +238,14 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
 #pragma unroll
                 for (int j = 0; j < DEG_FAST; j++) {
                     old[j] = 0;
-                    if (j < deg && vv[j] != u && cc[j] <= p.maxsec)
+                    if (j < deg && vv[j] != u && cc[j] <= maxsec)
                         old[j] = atomicMin((int *)&dist[vv[j]], __float_as_int(cc[j]));
                 }
                 const int maxdeg = warp_max_i(deg);
 #pragma unroll
                 for (int j = 0; j < DEG_FAST; j++) {
                     if (j >= maxdeg) break;
-                    const bool imp = (j < deg) && vv[j] != u && cc[j] <= p.maxsec && __float_as_int(cc[j]) < old[j];
+                    const bool imp = (j < deg) && vv[j] != u && cc[j] <= maxsec && __float_as_int(cc[j]) < old[j];
                     const int route = imp ? (cc[j] < T ? 1 : 2) : 0;
                     if (route == 2) fmn = fminf(fmn, cc[j]);
                     push_entries(imp && old[j] == INF_BITS, route, vv[j], cc[j], R, nnext, nfar, cap, qcap, s, nxt,
@@ -258,7 +259,7 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
                     if (j < deg) {
                         v = __ldg(&in_nb[beg + j]);
                         c = fadd(du, __ldg(&in_w[beg + j]));
-                        if (v != u && c <= p.maxsec) {
+                        if (v != u && c <= maxsec) {
                             const int o = atomicMin((int *)&dist[v], __float_as_int(c));
                             imp = __float_as_int(c) < o;
                             first = imp && o == INF_BITS;
@@ -281,7 +282,7 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
         // below mn's ulp.  One streaming pass over the far queue, by the queued distances: entries
         // that died since they were queued are dropped when their band runs.
         const float mn = warp_min_f(fmn);
-        T = fmaxf(fadd(mn, p.delta), __int_as_float(__float_as_int(mn) + 1));
+        T = fmaxf(fadd(mn, delta), __int_as_float(__float_as_int(mn) + 1));
         fmn = __int_as_float(INF_BITS);
         int nn = 0, nf2 = 0;
         for (int base = 0; base < nfar; base += 32) {
@@ -305,7 +306,7 @@ CS_PHASE_INLINE __device__ int warp_search(const PrimalParams &p, const SlotPtrs
         nfar = nf2;
     }
     __syncwarp();
-    dmax = fminf(T, p.maxsec);
+    dmax = fminf(T, maxsec);
     if (overflow) return -1;  // the slot's dense state is dirty: the caller resets it
     return R;
 }
@@ -1394,8 +1395,11 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
     long long relaxed = 0, settled = 0, done_src = 0;
     long long *ph = ph_all[wib];
     if (lane < 8) ph[lane] = 0;
+    // the warp's job parameters live in shared memory: a local copy of the (large) parameter block
+    // sits in the stack frame, and its loads then miss L1 under the kernel's global traffic
+    __shared__ PrimalParams pj_all[8];
+    PrimalParams &p = pj_all[wib];
     __syncwarp();
-    PrimalParams p;
     int cur_job = -1;
     while (true) {
         unsigned long long idx = 0;
@@ -1407,7 +1411,8 @@ __global__ void __launch_bounds__(256, MINB) batch_kernel(const PrimalParams bas
         const long long item = base.remap ? (long long)base.remap[idx] : item_lo + (long long)idx;
         const int jb = job_of(jobs, n_jobs, item);
         if (jb != cur_job) {
-            job_params(base, jobs[jb], p);
+            if (lane == 0) job_params(base, jobs[jb], p);
+            __syncwarp();
             cur_job = jb;
         }
         const int li = (int)(item - jobs[jb].item_begin);
@@ -1445,7 +1450,8 @@ __global__ void __launch_bounds__(256, MINB) batch_sync_kernel(const PrimalParam
     if (lane < 8) ph[lane] = 0;
     __syncwarp();
     const long long n = item_hi - item_lo;
-    PrimalParams p;
+    __shared__ PrimalParams pj_all[8];  // the warps' job parameters (as in batch_kernel)
+    PrimalParams &p = pj_all[wib];
     int cur_job = -1;
     while (true) {
         if (threadIdx.x == 0) {
@@ -1464,13 +1470,15 @@ __global__ void __launch_bounds__(256, MINB) batch_sync_kernel(const PrimalParam
         if (mine) {
             const int jb = job_of(jobs, n_jobs, item);
             if (jb != cur_job) {
-                job_params(base, jobs[jb], p);
+                if (lane == 0) job_params(base, jobs[jb], p);
+                __syncwarp();
                 cur_job = jb;
             }
             li = (int)(item - jobs[jb].item_begin);
             src = p.src_list[li];
         } else if (cur_job < 0) {
-            job_params(base, jobs[0], p);  // an idle warp still runs the phases (R = 0)
+            if (lane == 0) job_params(base, jobs[0], p);  // an idle warp still runs the phases (R = 0)
+            __syncwarp();
             cur_job = 0;
         }
         long long t0 = clock64();
@@ -2462,6 +2470,7 @@ cs_status cs_batch_run(const cs_batch_job *jobs_host, const cs_batch_job *jobs_d
         g_counters[0] = (long long)h.sources_done;
         g_counters[1] = (long long)h.edges_relaxed;
         g_counters[2] = (long long)h.nodes_settled;
+        for (int i = 0; i < 16; i++) g_phase[i] = (long long)h.pad[i];
     }
     int max_n = 0, n_pref = 0;
     for (int j = 0; j < n_jobs; j++) {
