@@ -991,11 +991,15 @@ __device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, in
     // node best (the lane of the lower-positioned state of each node) + closeness
     const size_t KN = (size_t)K * N;
     const double wt_d = f2d(wt);
+    // per position, for the backward sweep: the sibling state's position + 1 and the node's
+    // eligibility in the top bit (the sort's key scratch is free by now)
+    uint32_t *info = s.kb;
     for (int i = lane; i < R; i += 32) {
         const int V = s.ord[i];
         const int v = V >> 1;
         const uint32_t as = s.aux[V ^ 1];
         const int isib = (as != 0u && as <= (uint32_t)R) ? (int)as - 1 : -1;
+        info[i] = (uint32_t)(isib + 1) | (__ldg(&p.eligible[v]) ? 0x80000000u : 0u);
         if (isib >= 0 && isib < i) continue;
         const int i0 = (V & 1) ? isib : i;
         const int i1 = (V & 1) ? i : isib;
@@ -1064,13 +1068,13 @@ __device__ void dual_accumulate(const DualParams &p, const DSlot &s, int src, in
                 const float secs = s.sB[i];
                 const float route = s.rB[i];
                 const float best = s.nbR[i], bsecs = s.nbS[i];
-                // sibling state for the seed split
-                const uint32_t as = s.aux[V ^ 1];
-                const int isib = (as != 0u && as <= (uint32_t)R) ? (int)as - 1 : -1;
+                // sibling state for the seed split, and the pair weight
+                const uint32_t inf = __ldcg(&info[i]);
+                const int isib = (int)(inf & 0x7fffffffu) - 1;
                 const double sig_sib = isib >= 0 ? s.sig[isib] : 0.0;
                 const float secs_sib = isib >= 0 ? s.sB[isib] : 0.0f;
                 const float route_sib = isib >= 0 ? s.rB[isib] : 0.0f;
-                const double pair = __ldg(&p.eligible[v]) ? 0.5 : 1.0;
+                const double pair = (inf >> 31) ? 0.5 : 1.0;
                 // predecessor factors sigma_v / sigma_w in f64 (1 exactly when the counts agree)
                 double fr[DPM];
 #pragma unroll
