@@ -173,3 +173,12 @@ def _simplest(ns, dists, srcs, exact):
 def test_curved250_dual_simplest(curved_dual, exact):
     ns, dists = curved_dual
     _simplest(ns, dists, _strided(ns, 256), exact)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("exact", [False, "wide"])
+def test_curved250_dual_simplest_at_5km(curved_dual, exact):
+    """The full curved dual at 2 and 5 km, where most sources relax states whose offers a later
+    relaxation withdraws and replay rounds are most frequent: every row against the oracle."""
+    ns, _ = curved_dual
+    _simplest(ns, [2000, 5000], _strided(ns, 48), exact)
