@@ -117,3 +117,25 @@ def test_batch_rejects_bad_jobs():
         Batch([dict(ns=gs[0], mode="shortest", distances=list(range(100, 1800, 100)))])
     with pytest.raises(KeyError):
         Batch([dict(ns=gs[0], mode="angular", distances=[500])])
+
+
+def test_autotuned_schedule_matches_default(tmp_path, monkeypatch):
+    """The autotuner times every (band width, register budget) candidate on a sample of sources and
+    caches the fastest; a batch built from the cached schedule gives the same rows as the default
+    schedule's plain calls."""
+    from cityseer_gb300 import autotune, centrality
+
+    monkeypatch.setenv("CS_AUTOTUNE_CACHE", str(tmp_path / "autotune.json"))
+    gs = _graphs()
+    spec = dict(ns=gs[1], mode="shortest", distances=[400, 900])
+    res = autotune.tune(spec["ns"], "shortest", spec["distances"], sample=256)
+    assert res["tuned"] and len(res["trials"]) == len(autotune.DELTA_MULTS) * len(autotune.VARIANTS)
+    csr = centrality._primal_csr(spec["ns"])
+    from cityseer_gb300.common import pair_distances_betas_time
+
+    d, _, s = pair_distances_betas_time(1.33333, distances=spec["distances"])
+    hit = autotune.lookup(spec["ns"], csr, "shortest", d, s, 1.33333)
+    assert hit["tuned"] and hit["variant"] == res["variant"]
+    b = Batch([spec])
+    b.run()
+    _check(b.results()[0], spec, "tuned batch")
