@@ -1728,17 +1728,19 @@ int dual_wide_mode() {
     return 1;
 }
 
-// Resident 256-thread blocks per SM the dual kernels are compiled for: 3 (24 warps per SM; on the
-// 124,500-node curved dual 5% faster at 2 km and 8% at 5 km than 2 blocks, despite register
-// spills); CS_DUAL_MINB=2 selects the 2-block build.
+// Resident 256-thread blocks per SM the dual kernels are compiled for: 4 (32 warps per SM, 64
+// registers).  On the 124,500-node curved dual the memory latency the extra warps hide outweighs their
+// register spills: 224k sources/s at 2 km against 211k with 3 blocks and 152k with 2 (30.9k, 30.4k
+// and 26k at 5 km).  CS_DUAL_MINB=2 or 3 selects the other builds.
 int dual_minb() {
     const char *e = getenv("CS_DUAL_MINB");
-    return (e && e[0] == '2') ? 2 : 3;
+    return (e && e[0] == '2') ? 2 : ((e && e[0] == '3') ? 3 : 4);
 }
 
 cs_status dlaunch(csd::DualParams &p, int n_slots, cudaStream_t s) {
     p.n_slots = n_slots;
-    if (dual_minb() == 3) csd::dual_kernel<3><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
+    if (dual_minb() == 4) csd::dual_kernel<4><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
+    else if (dual_minb() == 3) csd::dual_kernel<3><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
     else csd::dual_kernel<2><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CS_OK : dcuda(e, "dual_kernel launch");
@@ -1868,9 +1870,10 @@ cs_status cs_plan_dual(const cs_dual_graph *g, int32_t mode, int32_t k, int32_t 
     const int sms = dsm_count();
     if (sms <= 0) return dfail(CS_ERR_CUDA, "no CUDA device");
     int bpsm = 0;
-    cudaError_t e = dual_minb() == 3
-                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, csd::dual_kernel<3>, 256, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, csd::dual_kernel<2>, 256, 0);
+    const int mb = dual_minb();
+    cudaError_t e = mb == 4   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, csd::dual_kernel<4>, 256, 0)
+                    : mb == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, csd::dual_kernel<3>, 256, 0)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, csd::dual_kernel<2>, 256, 0);
     if (e != cudaSuccess) return dcuda(e, "occupancy query");
     int slots = sms * std::max(1, bpsm) * 8;
     if (max_slots > 0) slots = std::min(slots, max_slots);
@@ -2015,7 +2018,8 @@ cs_status dbatch_shape(const cs_dual_batch_job *jobs, int n_jobs, DBatchShape &b
 cs_status dbatch_launch(csd::DualParams &p, const cs_dual_batch_job *jobs_dev, int n_jobs, long long n_items, int slots,
                         cudaStream_t s) {
     p.n_slots = slots;
-    if (dual_minb() == 3) csd::dual_batch_kernel<3><<<(slots + 7) / 8, 256, 0, s>>>(p, jobs_dev, n_jobs, n_items);
+    if (dual_minb() == 4) csd::dual_batch_kernel<4><<<(slots + 7) / 8, 256, 0, s>>>(p, jobs_dev, n_jobs, n_items);
+    else if (dual_minb() == 3) csd::dual_batch_kernel<3><<<(slots + 7) / 8, 256, 0, s>>>(p, jobs_dev, n_jobs, n_items);
     else csd::dual_batch_kernel<2><<<(slots + 7) / 8, 256, 0, s>>>(p, jobs_dev, n_jobs, n_items);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CS_OK : dcuda(e, "dual_batch_kernel launch");
