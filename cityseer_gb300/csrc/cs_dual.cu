@@ -1730,8 +1730,8 @@ int dual_wide_mode() {
 
 // Resident 256-thread blocks per SM the dual kernels are compiled for: 4 (32 warps per SM, 64
 // registers).  On the 124,500-node curved dual the memory latency the extra warps hide outweighs their
-// register spills: 224k sources/s at 2 km against 211k with 3 blocks and 152k with 2 (30.9k, 30.4k
-// and 26k at 5 km).  CS_DUAL_MINB=2 or 3 selects the other builds.
+// register spills: 224k sources/s at 2 km against 211k with 3 blocks (30.9k and 30.4k at 5 km); 3
+// blocks had beaten 2 by 5% and 8%.  CS_DUAL_MINB=2 or 3 selects the other builds.
 int dual_minb() {
     const char *e = getenv("CS_DUAL_MINB");
     return (e && e[0] == '2') ? 2 : ((e && e[0] == '3') ? 3 : 4);
