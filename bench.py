@@ -366,7 +366,10 @@ def run_gpu(args):
             "sources_per_step": n_src,
             "l2": "flushed between timed steps (256 MB write)",
             "parallelism": f"replicas x{ws}",
-            "slots": int(wsp.plan.n_slots),
+            # search slots of the shortest-path launches (plans sized for the 4-block budget hold
+            # more; the block-synchronous shortest-path kernel runs with 3 blocks per SM)
+            "slots": int(min(wsp.plan.n_slots, lib.cs_device_sm_count() * 3 * 8)
+                         if wsp.plan.variant == 0 else wsp.plan.n_slots),
             "cap": int(wsp.plan.cap),
             "delta_s": float(wsp.plan.delta_seconds),
         },

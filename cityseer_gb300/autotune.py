@@ -65,7 +65,9 @@ def key_of(csr, mode: str, secs, k: int) -> str:
 
 
 def default(csr, speed: float) -> dict:
-    return {"delta": 2.0 * csr.median_edge_seconds(speed), "variant": 3, "tuned": False}
+    # variant 0: the library's register budget per mode (3 blocks per SM for shortest paths, 4 for
+    # segments)
+    return {"delta": 2.0 * csr.median_edge_seconds(speed), "variant": 0, "tuned": False}
 
 
 def lookup(ns, csr, mode: str, d, s, speed: float) -> dict:

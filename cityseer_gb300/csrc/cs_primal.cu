@@ -1709,13 +1709,27 @@ cs_status validate_primal(const cs_primal_graph *g) {
 }
 
 // Register budget of the P <= 8 kernels: 4 resident 256-thread blocks per SM (64 registers), 3
-// (80 registers) or 2 (128 registers).  A plan's variant field selects it; 0 means the default
-// (4: the block-synchronous shortest-path kernel is memory-latency bound and gains from the extra
-// warps), which the environment variable CS_MIN_BLOCKS_PER_SM (2, 3 or 4) overrides.
-int resolve_variant(const cs_plan *plan) {
+// (80 registers) or 2 (128 registers).  A plan's variant field (2-4) or the environment variable
+// CS_MIN_BLOCKS_PER_SM selects one for every launch.  Otherwise (variant 0) plans are sized for 4
+// blocks, the most slots, and each launch picks by mode: 3 for shortest-path and OD centrality (on the
+// 202,500-node lattice 4 blocks ran 395 ms per pass against 372 ms with 3, the spills of the
+// dependency pass outweighing the extra warps), 4 for segments, trees and accessibility (segment
+// centrality on the 250x250 curved lattice: 2.67M sources/s against 2.49M with 3).
+int requested_variant(const cs_plan *plan) {
     if (plan && plan->variant >= 2 && plan->variant <= 4) return plan->variant;
     const char *e = getenv("CS_MIN_BLOCKS_PER_SM");
-    return (e && e[0] >= '2' && e[0] <= '4') ? e[0] - '0' : 3;
+    return (e && e[0] >= '2' && e[0] <= '4') ? e[0] - '0' : 0;
+}
+// the budget a plan's slot count is sized for
+int resolve_variant(const cs_plan *plan) {
+    const int v = requested_variant(plan);
+    return v ? v : 4;
+}
+// the budget one launch of a mode runs with
+int launch_variant(const cs_plan *plan, int mode) {
+    const int v = requested_variant(plan);
+    if (v) return v;
+    return (mode == cs::MODE_SHORTEST || mode == cs::MODE_OD) ? 3 : 4;
 }
 
 cudaError_t occupancy_blocks(int P, int variant, int *bpsm) {
@@ -1782,9 +1796,14 @@ void launch_primal_mode(const cs::PrimalParams &p, int P, int minb, int blocks, 
 cs_status launch_primal(cs::PrimalParams &p, const cs_plan *plan, int n_slots, cudaStream_t stream) {
     const int tpb = 256;
     const int wpb = tpb / 32;
-    const int blocks = (n_slots + wpb - 1) / wpb;
+    const int minb = launch_variant(plan, p.mode);
+    int blocks = (n_slots + wpb - 1) / wpb;
+    if (p.P <= 8 && minb < resolve_variant(plan)) {
+        // a tighter launch than the plan's slots were sized for: the blocks that are resident at once
+        blocks = std::max(1, std::min(blocks, std::max(1, sm_count()) * minb));
+        n_slots = std::min(n_slots, blocks * wpb);
+    }
     p.n_slots = n_slots;
-    const int minb = resolve_variant(plan);
     if (p.mode == cs::MODE_SHORTEST) launch_primal_mode<cs::MODE_SHORTEST>(p, p.P, minb, blocks, stream);
     else if (p.mode == cs::MODE_SEGMENT) launch_primal_mode<cs::MODE_SEGMENT>(p, p.P, minb, blocks, stream);
     else if (p.mode == cs::MODE_OD) launch_primal_mode<cs::MODE_OD>(p, p.P, minb, blocks, stream);
@@ -1811,9 +1830,14 @@ void launch_batch_mode(const cs::PrimalParams &p, int minb, int blocks, const cs
 // mode: the jobs' common mode (0 or 1) for a mode-specialised kernel, else -1
 cs_status launch_batch(cs::PrimalParams &p, const cs_plan *plan, const cs_batch_job *jobs_dev, int n_jobs,
                        long long item_lo, long long item_hi, int n_slots, int mode, cudaStream_t stream) {
-    const int blocks = (n_slots + 7) / 8;
+    // mixed-mode launches (and reruns) take the shortest-path budget
+    const int minb = launch_variant(plan, mode == cs::MODE_SEGMENT ? cs::MODE_SEGMENT : cs::MODE_SHORTEST);
+    int blocks = (n_slots + 7) / 8;
+    if (p.P <= 8 && minb < resolve_variant(plan)) {
+        blocks = std::max(1, std::min(blocks, std::max(1, sm_count()) * minb));
+        n_slots = std::min(n_slots, blocks * 8);
+    }
     p.n_slots = n_slots;
-    const int minb = resolve_variant(plan);
     if (mode == cs::MODE_SHORTEST && p.P <= 8 && !p.rerun && phase_sync()) {
         if (minb == 4) cs::batch_sync_kernel<8, 4><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, item_lo, item_hi);
         else if (minb == 3) cs::batch_sync_kernel<8, 3><<<blocks, 256, 0, stream>>>(p, jobs_dev, n_jobs, item_lo, item_hi);
@@ -2060,7 +2084,7 @@ cs_status plan_common(int n_bound, int P, int L, int cap, int max_slots, int64_t
     plan->blocks = (slots + 7) / 8;
     if (plan->delta_seconds != plan->delta_seconds) plan->delta_seconds = 0.0f;
     plan->lanes = L;
-    plan->variant = variant;
+    plan->variant = requested_variant(plan);  // 0: each launch picks its budget by mode
     plan->max_degree = P;
     plan->n_bound = n_bound;
     plan->cta_blocks = cta_blocks;
@@ -2300,7 +2324,7 @@ extern "C" cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, co
     int sms = sm_count();
     if (sms <= 0) return fail(CS_ERR_CUDA, "no CUDA device");
     int bpsm = 0;
-    cudaError_t e = occupancy_blocks(P, resolve_variant(nullptr), &bpsm);
+    cudaError_t e = occupancy_blocks(P, launch_variant(nullptr, cs::MODE_SHORTEST), &bpsm);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
     int slots = std::max(1, sms * std::max(1, bpsm) * 8);
     while (slots > 1 && layout(g->n_bound, slots, cap, P, L).total > kNoAllocScratchBytes) {
@@ -2318,7 +2342,7 @@ extern "C" cs_status cs_centrality_shortest_noalloc(const cs_primal_graph *g, co
     plan.blocks = (slots + 7) / 8;
     plan.delta_seconds = 0.0f;
     plan.lanes = L;
-    plan.variant = resolve_variant(nullptr);
+    plan.variant = launch_variant(nullptr, cs::MODE_SHORTEST);
     plan.max_degree = P;
     const Layout lay = layout(g->n_bound, slots, cap, P, L);
     plan.workspace_bytes = lay.total;
