@@ -131,7 +131,9 @@ typedef struct {
     int32_t blocks;
     float delta_seconds;  /* band width of the label-correcting search; <= 0 picks a default */
     int32_t lanes;        /* accumulator lanes per reached node */
-    int32_t variant;      /* register budget: 3 (default), 4 or 2 resident 256-thread blocks per SM */
+    int32_t variant;      /* register budget: 2, 3 or 4 resident 256-thread blocks per SM for every
+                           * launch; 0 (default): slots sized for 4, and each launch takes 3 for
+                           * shortest-path and OD centrality, 4 for segments, trees and accessibility */
     int32_t max_degree;   /* batches: largest out-degree over the jobs */
     int32_t n_bound;      /* node bound the slot geometry was sized for (set by the planners) */
     int32_t cta_blocks;   /* shortest-path plans: blocks of the block-per-source kernel whose scratch
