@@ -3,6 +3,8 @@ another host package would: the device CSR of a graph, a planned workspace, the 
 output rows of one centrality call, all owned by the returned object (keep it alive while the call
 runs).  `NetworkStructure.centrality_shortest` / `centrality_simplest` do the same and then post-scale
 and compact the rows; the raw rows here are [metric][threshold][node_bound], before any post-scale.
+Calls built for the same graph share that graph's workspace (as the public API's calls do): issue
+them one after another on one stream, never concurrently.
 
     call = abi.shortest_call(ns, distances=[500, 2000])
     rc = abi.library().cs_centrality_shortest(*call.args())
