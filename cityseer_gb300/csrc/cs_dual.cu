@@ -1248,6 +1248,120 @@ __device__ __forceinline__ bool run_dual_source(const DualParams &p, const DSlot
     return ok;
 }
 
+// The same per-source work with the block's warps in lockstep: search, then sort + replay rounds,
+// then accumulation + scratch reset, each phase closed by a block barrier that every warp meets
+// (a warp without a source, or whose source overflowed, runs the phases empty), so that the SM
+// fetches one phase's code at a time.  Returns true when the source was accumulated.
+__device__ __forceinline__ bool run_dual_source_sync(const DualParams &p, const DSlot &s, bool mine, int li,
+                                                     int src, uint32_t *hist, int *cnt, long long *ph,
+                                                     long long &relaxed, long long &settled) {
+    const int lane = lane_id();
+    long long tph = clock64();
+    const int N2 = 2 * p.g.n_bound;
+    const bool exact = (p.pass == 2) || p.force_exact;
+    const bool wide = s.lsec != nullptr;
+    int R = 0;
+    if (mine) {
+        if (exact) R = dual_exact_search(p, s, src);
+        else if (wide) R = dual_search_wide(p, s, src, relaxed);
+        else R = dual_search(p, s, src, relaxed);
+    }
+    dphase(ph, exact ? 6 : 0, tph);
+    __syncthreads();
+    const bool live = mine && R >= 0;
+    if (mine && R < 0) {
+        for (int j = lane; j < N2; j += 32) {
+            s.key[j] = KEY_INF;
+            s.aux[j] = 0u;
+            if (wide) s.lsec[j] = NO_LSEC;
+        }
+        if (lane == 0) {
+            if (p.fail_final) {
+                raise_err(p.hdr, CS_ERR_CAPACITY, 27);
+            } else {
+                const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
+                if (f < (unsigned)p.fail_cap) p.failed[f] = li;
+                else raise_err(p.hdr, CS_ERR_CAPACITY, 23);
+            }
+        }
+        __syncwarp();
+    }
+    bool bad = false;
+    int rr = 1;
+    if (live) {
+        const int rounds = exact ? 1 : max(1, p.replay_rounds) + (wide ? 4 : 0);
+        int rounds_run = 0;
+        int32_t *prev = (int32_t *)s.nbR;
+        int first_change = 0;
+        auto key_of = [&](int S) { return (uint32_t)(__ldcg(&s.key[S]) >> 32); };
+        for (int it = 0; it < rounds && rr == 1; it++) {
+            rounds_run++;
+            int start = 0;
+            if (!exact) {
+                if (it == 0) {
+                    warp_radix_sort(R, s.rl, key_of, s.kb, s.vb, s.rk, s.ord, hist);
+                } else {
+                    const int p0 = max(0, min(first_change, R));
+                    for (int i = p0 + lane; i < R; i += 32) prev[i] = s.ord[i];
+                    __syncwarp();
+                    if (p0 < R) warp_radix_sort(R - p0, s.ord + p0, key_of, s.kb, s.vb, s.rk + p0, s.ord + p0, hist);
+                }
+                __syncwarp();
+                if (it > 0) {
+                    const int p0 = max(0, min(first_change, R));
+                    start = R;
+                    for (int base = p0 & ~31; base < R; base += 32) {
+                        const int i = base + lane;
+                        const unsigned moved = __ballot_sync(FULL, i >= p0 && i < R && __ldcg(&s.ord[i]) != prev[i]);
+                        if (moved) {
+                            start = base + __ffs(moved) - 1;
+                            break;
+                        }
+                    }
+                    start &= ~31;
+                    if (lane == 0) ph[15] += start;
+                }
+            }
+            for (int i = start + lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+            __syncwarp();
+            dphase(ph, 1, tph);
+            rr = dual_replay(p, s, src, R, bad, !exact, it > 0, start, first_change);
+            __syncwarp();
+            dphase(ph, 2, tph);
+        }
+        if (lane == 0) ph[7] += rounds_run;
+    }
+    __syncthreads();
+    tph = clock64();
+    const bool ok = live && rr == 0;
+    if (live) {
+        if (ok) {
+            dual_accumulate(p, s, src, R, cnt, bad, ph);
+            tph = clock64();
+        } else if (lane == 0) {
+            if (exact) raise_err(p.hdr, CS_ERR_INTERNAL, 24);
+            else {
+                const unsigned f = atomicAdd(&p.hdr->n_inexact, 1u);
+                if (f < (unsigned)p.inexact_cap) p.inexact[f] = li;
+                else raise_err(p.hdr, CS_ERR_CAPACITY, 25);
+            }
+        }
+        if (__any_sync(FULL, bad) && lane == 0) raise_err(p.hdr, CS_ERR_INTERNAL, 26);
+        __syncwarp();
+        for (int i = lane; i < R; i += 32) {
+            const int S = s.ord[i];
+            s.key[S] = KEY_INF;
+            s.aux[S] = 0u;
+            if (wide) s.lsec[S] = NO_LSEC;
+        }
+        __syncwarp();
+        dphase(ph, 5, tph);
+        settled += R;
+    }
+    __syncthreads();
+    return ok;
+}
+
 __device__ __forceinline__ void flush_dual_counters(const DualParams &p, const long long *ph, long long relaxed,
                                                     long long settled, long long done_src) {
     const long long rsum = warp_sum_ll(relaxed);
@@ -1259,6 +1373,49 @@ __device__ __forceinline__ void flush_dual_counters(const DualParams &p, const l
         atomicAdd(&p.hdr->nodes_settled, (unsigned long long)settled);
         atomicAdd(&p.hdr->sources_done, (unsigned long long)done_src);
     }
+}
+
+// dual_kernel with the block's warps in lockstep (run_dual_source_sync): a block claims one source per
+// warp at a time; every warp of the block stays in the loop until the block's sources run out.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) dual_sync_kernel(const DualParams p) {
+    __shared__ uint32_t hist_all[8][256];
+    __shared__ int cnt_all[8][MAXK];
+    __shared__ long long ph_all[8][16];
+    __shared__ unsigned long long blk_base;
+    __shared__ unsigned blk_err;
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    const int slot0 = blockIdx.x * (blockDim.x >> 5);
+    const int nw = min((int)(blockDim.x >> 5), p.n_slots - slot0);
+    const bool has_slot = wib < nw;
+    const int slot = has_slot ? slot0 + wib : 0;
+    DSlot s = dslot(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.k, slot, p.geo_n);
+    if (p.pass == 3) s.lsec = (uint32_t *)(p.dense + p.dense_stride * (size_t)(slot + p.lsec_slot_off));
+    long long *ph = ph_all[wib];
+    if (lane < 16) ph[lane] = 0;
+    __syncwarp();
+    long long relaxed = 0, settled = 0, done_src = 0;
+    while (true) {
+        if (threadIdx.x == 0) {
+            blk_base = atomicAdd(p.pass ? &p.hdr->work_next2 : &p.hdr->work_next, (unsigned long long)max(nw, 0));
+            blk_err = __ldcg(&p.hdr->err);
+        }
+        __syncthreads();
+        const unsigned long long b0 = blk_base;
+        const unsigned berr = blk_err;
+        __syncthreads();
+        if (nw <= 0 || b0 >= (unsigned long long)p.n_src || berr != 0u) break;
+        const unsigned long long idx = b0 + wib;
+        const bool mine = has_slot && idx < (unsigned long long)p.n_src;
+        const int li = mine ? (p.remap ? p.remap[idx] : (int)idx) : 0;
+        const int src = mine ? p.src_list[li] : 0;
+        if (run_dual_source_sync(p, s, mine, li, src, hist_all[wib], cnt_all[wib], ph, relaxed, settled)) {
+            done_src++;
+            if (lane == 0) count_progress(p.hdr);
+        }
+    }
+    if (has_slot) flush_dual_counters(p, ph, relaxed, settled, done_src);
 }
 
 template <int MINB>
@@ -1737,9 +1894,21 @@ int dual_minb() {
     return (e && e[0] == '2') ? 2 : ((e && e[0] == '3') ? 3 : 4);
 }
 
+// Lockstep phases for the simplest-path kernel (default; CS_DUAL_SYNC=0 leaves each warp on its own
+// source).  On the 124,500-node curved dual: 270k sources/s at 2 km against 227k, 31.7k against
+// 30.6k at 5 km, with the SMs fetching one phase's code at a time.
+bool dual_sync() {
+    const char *e = getenv("CS_DUAL_SYNC");
+    return !(e && e[0] == '0');
+}
+
 cs_status dlaunch(csd::DualParams &p, int n_slots, cudaStream_t s) {
     p.n_slots = n_slots;
-    if (dual_minb() == 4) csd::dual_kernel<4><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
+    if (dual_sync()) {
+        if (dual_minb() == 4) csd::dual_sync_kernel<4><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
+        else if (dual_minb() == 3) csd::dual_sync_kernel<3><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
+        else csd::dual_sync_kernel<2><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
+    } else if (dual_minb() == 4) csd::dual_kernel<4><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
     else if (dual_minb() == 3) csd::dual_kernel<3><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
     else csd::dual_kernel<2><<<(n_slots + 7) / 8, 256, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
