@@ -1209,6 +1209,97 @@ __device__ __forceinline__ void flush_counters(const PrimalParams &p, long long 
 // ------------------------------------------------------------------------------------------
 // Persistent kernel: each warp owns one scratch slot and pulls sources until the list is empty.
 // ------------------------------------------------------------------------------------------
+// Segment centrality with a block's warps in lockstep (as primal_sync_kernel for shortest paths):
+// search | sort | accumulation + scratch reset, each phase closed by a block barrier that every warp
+// meets (a warp without a source, or whose source overflowed, runs the phases empty).
+template <int PM>
+__device__ __forceinline__ bool run_segment_sync(const PrimalParams &p, const SlotPtrs &s, bool mine, int li, int src,
+                                                 uint32_t *hist, long long *ph, long long &relaxed,
+                                                 long long &settled) {
+    const int lane = lane_id();
+    long long t0 = clock64();
+    float dmax = 0.0f;
+    int R = 0;
+    if (mine) R = warp_search(p, s, src, relaxed, dmax);
+    phase_mark(ph, 0, t0);
+    __syncthreads();
+    const bool live = mine && R >= 0;
+    if (mine && R < 0) {
+        for (int j = lane; j < p.g.n_bound; j += 32) {
+            s.dist[j] = __int_as_float(INF_BITS);
+            s.aux[j] = 0u;
+        }
+        if (lane == 0) {
+            const unsigned f = atomicAdd(&p.hdr->n_failed, 1u);
+            if (f < (unsigned)p.fail_cap) p.failed[f] = li;
+            else raise_err(p.hdr, CS_ERR_CAPACITY, 8);
+        }
+        __syncwarp();
+    }
+    if (live) {
+        warp_sort(p, s, R, dmax, hist);
+        __syncwarp();
+        for (int i = lane; i < R; i += 32) s.aux[s.ord[i]] = (uint32_t)(i + 1);
+        __syncwarp();
+    }
+    phase_mark(ph, 1, t0);
+    __syncthreads();
+    if (live) {
+        segment_accumulate<PM>(p, s, src, R);
+        __syncwarp();
+        t0 = clock64();
+        for (int i = lane; i < R; i += 32) {
+            const int v = s.ord[i];
+            s.dist[v] = __int_as_float(INF_BITS);
+            s.aux[v] = 0u;
+        }
+        __syncwarp();
+        phase_mark(ph, 6, t0);
+        settled += R;
+    }
+    __syncthreads();
+    return live;
+}
+
+template <int PM, int MINB>
+__global__ void __launch_bounds__(256, MINB) segment_sync_kernel(const PrimalParams p) {
+    __shared__ uint32_t hist_all[8][256];
+    __shared__ long long ph_all[8][8];
+    __shared__ unsigned long long blk_base;
+    __shared__ unsigned blk_err;
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    const int slot0 = blockIdx.x * (blockDim.x >> 5);
+    const int nw = min((int)(blockDim.x >> 5), p.n_slots - slot0);
+    const bool has_slot = wib < nw;
+    const SlotPtrs s = slot_ptrs(p.dense, p.dense_stride, p.compact, (size_t)p.cap, p.P, p.L,
+                                 has_slot ? slot0 + wib : 0, p.g.n_bound);
+    long long relaxed = 0, settled = 0, done_src = 0;
+    long long *ph = ph_all[wib];
+    if (lane < 8) ph[lane] = 0;
+    __syncwarp();
+    while (true) {
+        if (threadIdx.x == 0) {
+            blk_base = atomicAdd(p.rerun ? &p.hdr->work_next2 : &p.hdr->work_next, (unsigned long long)max(nw, 0));
+            blk_err = __ldcg(&p.hdr->err);
+        }
+        __syncthreads();
+        const unsigned long long b0 = blk_base;
+        const unsigned berr = blk_err;
+        __syncthreads();
+        if (nw <= 0 || b0 >= (unsigned long long)p.n_src || berr != 0u) break;
+        const unsigned long long idx = b0 + wib;
+        const bool mine = has_slot && idx < (unsigned long long)p.n_src;
+        const int li = mine ? (p.remap ? p.remap[idx] : (int)idx) : 0;
+        const int src = mine ? p.src_list[li] : 0;
+        if (run_segment_sync<PM>(p, s, mine, li, src, hist_all[wib], ph, relaxed, settled)) {
+            done_src++;
+            if (lane == 0) count_progress(p.hdr);
+        }
+    }
+    if (has_slot) flush_counters(p, ph, relaxed, settled, done_src);
+}
+
 template <int PM, int MINB, int MODE>
 __global__ void __launch_bounds__(256, MINB) primal_kernel(const PrimalParams p) {
     __shared__ uint32_t hist_all[8][256];
@@ -1782,6 +1873,12 @@ void launch_primal_mode(const cs::PrimalParams &p, int P, int minb, int blocks, 
         if (minb == 4) cs::primal_sync_kernel<8, 4, 8, 8><<<blocks, 256, 0, stream>>>(p);
         else if (minb == 3) cs::primal_sync_kernel<8, 3, 8, 8><<<blocks, 256, 0, stream>>>(p);
         else cs::primal_sync_kernel<8, 2, 8, 8><<<blocks, 256, 0, stream>>>(p);
+        return;
+    }
+    if (MODE == cs::MODE_SEGMENT && P <= 8 && phase_sync()) {
+        if (minb == 4) cs::segment_sync_kernel<8, 4><<<blocks, 256, 0, stream>>>(p);
+        else if (minb == 3) cs::segment_sync_kernel<8, 3><<<blocks, 256, 0, stream>>>(p);
+        else cs::segment_sync_kernel<8, 2><<<blocks, 256, 0, stream>>>(p);
         return;
     }
     if (P <= 8) {
